@@ -1,0 +1,1129 @@
+// gm_api.cu — the backend context and the C ABI (include/geodesic_cuda.h).
+//
+// gm_ctx mirrors the reference's CpuBackend/GpuBackend (cpu_backend.rs:25-37,
+// gpu_backend.rs:11-22): it owns the atoms, the topology, the neighbour list
+// and the force buffer, on the device.  Host entry points upload the caller's
+// arrays, run the kernels on the context's stream and copy results back;
+// the resident entry points keep everything on the device and run the BAB
+// loop as a CUDA graph (one captured step: half-kick, drift, SHAKE, rebuild
+// check, an IF node holding the list rebuild, forces, half-kick, RATTLE).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gm_internal.cuh"
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr, side = nullptr;
+    gm_params p{};
+    int n = 0;
+    bool fp64 = false;
+    std::string err;
+    long long launches = 0;
+    std::vector<void *> allocs;
+
+    // atoms
+    int ntypes = 0;
+    double *d_mass = nullptr, *d_inv_mass = nullptr, *d_sigma = nullptr, *d_eps = nullptr, *d_charge64 = nullptr;
+    int *d_type = nullptr;
+    float *d_charge = nullptr;
+    float2 *d_tab32 = nullptr;
+    double2 *d_tab64 = nullptr;
+    // state
+    double *d_pos = nullptr, *d_vel = nullptr, *d_ref = nullptr, *d_dref = nullptr, *d_fout = nullptr,
+           *d_host_f = nullptr;
+    long long *d_force = nullptr;
+    // sorted / cells
+    float4 *d_hi = nullptr, *d_lo = nullptr;
+    double4 *d_pos64s = nullptr;
+    int *d_type_sorted = nullptr;
+    int *d_perm = nullptr, *d_cell_of = nullptr, *d_cell_sorted = nullptr, *d_cell_count = nullptr,
+        *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr;
+    int max_cells = 0;
+    GridInfo *d_grid = nullptr;
+    double *d_bbox = nullptr;
+    int bbox_blocks = 0;
+    // list
+    int cap = 0, n_groups = 0;
+    int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr;
+    bool built = false;
+    // exclusions
+    int *d_excl_start = nullptr, *d_excl = nullptr;
+    // bonded
+    int n_bonds = 0, n_angles = 0, n_diheds = 0, bonded_blocks = 0;
+    int *d_bi = nullptr, *d_bj = nullptr, *d_ai = nullptr, *d_aj = nullptr, *d_ak = nullptr, *d_di = nullptr,
+        *d_dj = nullptr, *d_dk = nullptr, *d_dl = nullptr, *d_dn = nullptr;
+    double *d_bk = nullptr, *d_br0 = nullptr, *d_akth = nullptr, *d_ath0 = nullptr, *d_dkphi = nullptr,
+           *d_ddelta = nullptr;
+    // 1-4
+    int n14 = 0, blocks14 = 0;
+    int *d_p14i = nullptr, *d_p14j = nullptr;
+    // constraints
+    int n_constr = 0, n_clusters = 0;
+    int *d_ci = nullptr, *d_cj = nullptr, *d_cl_cstart = nullptr, *d_cl_cons = nullptr, *d_cl_astart = nullptr,
+        *d_cl_atoms = nullptr, *d_cl_acstart = nullptr, *d_cl_acons = nullptr, *d_cl_iters = nullptr,
+        *d_cl_worst_idx = nullptr;
+    double *d_cdsq = nullptr, *d_lam = nullptr, *d_rvec = nullptr, *d_cl_worst = nullptr;
+    std::vector<int> h_ci, h_cj;
+    // energy
+    double *d_epart = nullptr, *d_energy = nullptr, *d_kin_part = nullptr, *d_ke = nullptr;
+    int n_epart = 0;
+    // status
+    DevStatus *d_status = nullptr;
+    DevStatus *h_status = nullptr;  // pinned
+    // graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    double graph_dt = 0.0;
+    int graph_cap = -1;
+    long long launches_per_step = 0;
+    bool forces_current = false;
+    long long rebuild_base = 0;
+    unsigned last_shake_T = 0, last_rattle_T = 0;
+};
+
+namespace {
+
+int fail(gm_ctx *c, int code, const char *fmt, ...) {
+    if (c) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_status(gm_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return GM_OK;
+    if (e == cudaErrorMemoryAllocation) return fail(c, GM_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return fail(c, GM_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+    return fail(c, GM_ERR_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GM_CUDA(ctx, call)                                      \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_status(ctx, e_, #call); \
+    } while (0)
+
+template <typename T>
+int dalloc(gm_ctx *c, T **ptr, size_t count) {
+    *ptr = nullptr;
+    size_t bytes = sizeof(T) * (count > 0 ? count : 1);
+    cudaError_t e = cudaMalloc((void **)ptr, bytes);
+    if (e != cudaSuccess) return cuda_status(c, e, "cudaMalloc");
+    c->allocs.push_back(*ptr);
+    return GM_OK;
+}
+
+template <typename T>
+int dupload(gm_ctx *c, T **ptr, const T *host, size_t count) {
+    int rc = dalloc(c, ptr, count);
+    if (rc) return rc;
+    if (count && host) GM_CUDA(c, cudaMemcpy(*ptr, host, sizeof(T) * count, cudaMemcpyHostToDevice));
+    return GM_OK;
+}
+
+void dfree(gm_ctx *c, void *ptr) {
+    if (!ptr) return;
+    cudaFree(ptr);
+    c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), ptr), c->allocs.end());
+}
+
+std::vector<int> to_int(const uint32_t *a, int64_t n) {
+    std::vector<int> v((size_t)n);
+    for (int64_t i = 0; i < n; i++) v[(size_t)i] = (int)a[i];
+    return v;
+}
+
+bool finite3(const double *x, const double *y, const double *z, int n) {
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i])) return false;
+    return true;
+}
+
+ListArgs list_args(gm_ctx *c) {
+    ListArgs a{};
+    a.n = c->n;
+    a.cap = c->cap;
+    a.pos = c->d_pos;
+    a.hi = c->d_hi;
+    a.lo = c->d_lo;
+    a.pos64s = c->d_pos64s;
+    a.type_sorted = c->d_type_sorted;
+    a.perm = c->d_perm;
+    a.cell_of = c->d_cell_of;
+    a.cell_sorted = c->d_cell_sorted;
+    a.cell_count = c->d_cell_count;
+    a.cell_start = c->d_cell_start;
+    a.cell_cursor = c->d_cell_cursor;
+    a.tmp_atom = c->d_tmp_atom;
+    a.max_cells = c->max_cells;
+    a.type = c->d_type;
+    a.charge = c->d_charge;
+    a.charge64 = c->d_charge64;
+    a.excl_start = c->d_excl_start;
+    a.excl = c->d_excl;
+    a.list = c->d_list;
+    a.count = c->d_count;
+    a.gmax = c->d_gmax;
+    a.ref = c->d_ref;
+    a.force = c->d_force;
+    a.grid = c->d_grid;
+    a.status = c->d_status;
+    a.r_list = c->p.r_skin;
+    for (int d = 0; d < 3; d++) a.box[d] = c->p.box[d];
+    a.periodic = c->p.periodic;
+    a.bbox_scratch = c->d_bbox;
+    a.bbox_blocks = c->bbox_blocks;
+    return a;
+}
+
+ForceArgs force_args(gm_ctx *c) {
+    ForceArgs a{};
+    a.n = c->n;
+    a.n_groups = c->n_groups;
+    a.cap = c->cap;
+    a.hi = c->d_hi;
+    a.lo = c->d_lo;
+    a.pos64s = c->d_pos64s;
+    a.type_sorted = c->d_type_sorted;
+    a.perm = c->d_perm;
+    a.list = c->d_list;
+    a.count = c->d_count;
+    a.gmax = c->d_gmax;
+    a.ntypes = c->ntypes;
+    a.tab32 = c->d_tab32;
+    a.tab64 = c->d_tab64;
+    const double rc = c->p.r_cutoff, rsw = c->p.r_switch;
+    a.rc2 = (float)(rc * rc);
+    a.rsw = (float)rsw;
+    a.rc = (float)rc;
+    a.inv_wsw = (float)(1.0 / (rc - rsw));
+    a.rc2_64 = rc * rc;
+    a.rsw_64 = rsw;
+    a.rc_64 = rc;
+    a.inv_wsw_64 = 1.0 / (rc - rsw);
+    a.coulomb = c->p.coulomb;
+    for (int d = 0; d < 3; d++) {
+        a.box[d] = (float)c->p.box[d];
+        a.inv_box[d] = (float)(1.0 / c->p.box[d]);
+        a.box64[d] = c->p.box[d];
+    }
+    a.periodic = c->p.periodic;
+    a.force = c->d_force;
+    a.epart = c->d_epart;
+    a.status = c->d_status;
+    a.pos = c->d_pos;
+    a.n_bonds = c->n_bonds;
+    a.n_angles = c->n_angles;
+    a.n_diheds = c->n_diheds;
+    a.bond_i = c->d_bi; a.bond_j = c->d_bj; a.bond_k = c->d_bk; a.bond_r0 = c->d_br0;
+    a.angle_i = c->d_ai; a.angle_j = c->d_aj; a.angle_k = c->d_ak; a.angle_kth = c->d_akth; a.angle_th0 = c->d_ath0;
+    a.dihed_i = c->d_di; a.dihed_j = c->d_dj; a.dihed_k = c->d_dk; a.dihed_l = c->d_dl; a.dihed_kphi = c->d_dkphi;
+    a.dihed_n = c->d_dn; a.dihed_delta = c->d_ddelta;
+    a.bonded_blocks = c->bonded_blocks;
+    a.epart_bonded = c->d_epart + c->n_groups;
+    a.n14 = c->n14; a.p14_i = c->d_p14i; a.p14_j = c->d_p14j;
+    a.scale14_lj = c->p.scale14_lj; a.scale14_coul = c->p.scale14_coul;
+    a.sigma = c->d_sigma; a.epsilon = c->d_eps; a.charge64 = c->d_charge64;
+    a.blocks14 = c->blocks14;
+    a.epart14 = c->d_epart + c->n_groups + c->bonded_blocks;
+    a.energy = c->d_energy;
+    a.n_epart_total = c->n_groups + c->bonded_blocks + c->blocks14;
+    return a;
+}
+
+ClusterArgs cluster_args(gm_ctx *c) {
+    ClusterArgs a{};
+    a.n_clusters = c->n_clusters;
+    a.cl_cstart = c->d_cl_cstart; a.cl_cons = c->d_cl_cons;
+    a.cl_astart = c->d_cl_astart; a.cl_atoms = c->d_cl_atoms;
+    a.cl_acstart = c->d_cl_acstart; a.cl_acons = c->d_cl_acons;
+    a.constr_i = c->d_ci; a.constr_j = c->d_cj; a.constr_dsq = c->d_cdsq;
+    a.inv_mass = c->d_inv_mass;
+    a.lam = c->d_lam; a.rvec = c->d_rvec;
+    a.cl_iters = c->d_cl_iters; a.cl_worst = c->d_cl_worst; a.cl_worst_idx = c->d_cl_worst_idx;
+    a.n_constr = c->n_constr;
+    a.max_iter = c->p.max_constr_iter;
+    a.tol = c->p.constr_tol;
+    a.status = c->d_status;
+    return a;
+}
+
+// ---- kernel sequences (each counted for gm_counters[3]) -------------------
+
+int seq_rebuild(gm_ctx *c, cudaStream_t s) {
+    ListArgs a = list_args(c);
+    gm_launch_wrap(a, c->d_pos, s);
+    gm_launch_grid(a, s);
+    gm_launch_bin(a, s);
+    gm_launch_pack(a, c->fp64, s);
+    gm_launch_build(a, s);
+    return (a.periodic ? 1 : 0) + (a.periodic ? 1 : 2) + 4 + 2;  // + 2 memsets
+}
+
+int seq_forces(gm_ctx *c, cudaStream_t s) {
+    ListArgs la = list_args(c);
+    gm_launch_pack(la, c->fp64, s);
+    ForceArgs fa = force_args(c);
+    gm_launch_bonded(fa, c->fp64, s);
+    gm_launch_pair(fa, c->fp64, s);
+    gm_launch_pair14(fa, s);
+    gm_launch_energy(fa, s);
+    return 1 + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + 1;
+}
+
+int check_status(gm_ctx *c, gm_convergence *conv);
+
+// DevStatus travels through the pinned h_status on the context's own stream
+// (the stream is non-blocking, so legacy-stream copies would not be ordered).
+int st_read(gm_ctx *c) {
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    GM_CUDA(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+int st_write(gm_ctx *c) {
+    GM_CUDA(c, cudaMemcpyAsync(c->d_status, c->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, c->stream));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+// Clears error and per-call fields; keeps the rebuild counter and the step.
+int reset_status(gm_ctx *c) {
+    int rc = st_read(c);
+    if (rc) return rc;
+    DevStatus z{};
+    z.fail_step = ~0ull;
+    z.n_rebuilds = c->h_status->n_rebuilds;
+    z.step = c->h_status->step;
+    *c->h_status = z;
+    return st_write(c);
+}
+
+int set_step(gm_ctx *c, uint64_t step) {
+    int rc = st_read(c);
+    if (rc) return rc;
+    c->h_status->step = step;
+    return st_write(c);
+}
+
+int fill_convergence(gm_ctx *c, bool rattle, gm_convergence *conv) {
+    // the reference's worst constraint of the last iteration: max |lambda|,
+    // smallest constraint index on ties (constraint.rs:123-127, 144-151)
+    std::vector<double> w((size_t)c->n_clusters);
+    std::vector<int> wi((size_t)c->n_clusters);
+    GM_CUDA(c, cudaMemcpy(w.data(), c->d_cl_worst, sizeof(double) * w.size(), cudaMemcpyDeviceToHost));
+    GM_CUDA(c, cudaMemcpy(wi.data(), c->d_cl_worst_idx, sizeof(int) * wi.size(), cudaMemcpyDeviceToHost));
+    double best = 0.0;
+    int bi = -1;
+    for (size_t k = 0; k < w.size(); k++) {
+        if (bi < 0 || w[k] > best || (w[k] == best && wi[k] < bi)) {
+            best = w[k];
+            bi = wi[k];
+        }
+    }
+    if (bi < 0) bi = 0;
+    if (conv) {
+        conv->step = c->h_status->fail_step == ~0ull ? c->h_status->step : c->h_status->fail_step;
+        conv->constraint_idx = bi;
+        conv->atom_i = c->h_ci.empty() ? 0 : c->h_ci[(size_t)bi];
+        conv->atom_j = c->h_cj.empty() ? 0 : c->h_cj[(size_t)bi];
+        conv->residual = best;
+        conv->max_iter = c->p.max_constr_iter;
+    }
+    return fail(c, GM_ERR_CONVERGENCE,
+                "%s failed to converge for constraint %d (atoms %lld, %lld) at step %llu: residual %g after %u "
+                "iterations",
+                rattle ? "velocity constraint solver" : "constraint solver", bi,
+                (long long)(conv ? conv->atom_i : 0), (long long)(conv ? conv->atom_j : 0),
+                (unsigned long long)(conv ? conv->step : 0), best, c->p.max_constr_iter);
+}
+
+int check_status(gm_ctx *c, gm_convergence *conv) {
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    GM_CUDA(c, cudaGetLastError());
+    int rc0 = st_read(c);
+    if (rc0) return rc0;
+    const unsigned e = c->h_status->error;
+    c->last_shake_T = c->h_status->shake_T;
+    c->last_rattle_T = c->h_status->rattle_T;
+    if (!e) return GM_OK;
+    if (e & GM_DEV_LIST_OVERFLOW) return fail(c, GM_ERR_LIST_OVERFLOW, "neighbour list capacity %d exceeded", c->cap);
+    if (e & GM_DEV_NONFINITE_POS)
+        return fail(c, GM_ERR_NONFINITE, "non-finite position at step %llu", (unsigned long long)c->h_status->step);
+    if (e & GM_DEV_SHAKE_FAIL) return fill_convergence(c, false, conv);
+    if (e & GM_DEV_RATTLE_FAIL) return fill_convergence(c, true, conv);
+    if (e & GM_DEV_NONFINITE_FORCE)
+        return fail(c, GM_ERR_NONFINITE, "non-finite force at step %llu", (unsigned long long)c->h_status->step);
+    if (e & GM_DEV_FIX_OVERFLOW)
+        return fail(c, GM_ERR_FIXED_POINT_OVERFLOW, "a force contribution exceeded the fixed-point range (|F| >= 2^22)");
+    if (e & GM_DEV_EXTENT)
+        return fail(c, GM_ERR_UNSUPPORTED,
+                    "non-periodic system extent plus the list radius reaches half the box: the reference's "
+                    "min-image would fold pairs; use a larger box");
+    if (e & GM_DEV_CELL_OVERFLOW) return fail(c, GM_ERR_UNSUPPORTED, "cell grid overflow");
+    if (e & GM_DEV_ITER_MISMATCH)
+        return fail(c, GM_ERR_UNSUPPORTED, "constraint cluster iteration counts disagree with the global stop rule");
+    return fail(c, GM_ERR_DEVICE, "device status 0x%x", e);
+}
+
+int ensure_list_buffers(gm_ctx *c, int cap) {
+    if (cap == c->cap && c->d_list) return GM_OK;
+    dfree(c, c->d_list);
+    c->d_list = nullptr;
+    c->cap = cap;
+    size_t entries = (size_t)c->n_groups * 32 * (size_t)cap;
+    int rc = dalloc(c, &c->d_list, entries);
+    if (rc) return rc;
+    // captured graphs hold the old pointer
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+    return GM_OK;
+}
+
+int estimate_cap(gm_ctx *c, const double *px, const double *py, const double *pz) {
+    double vol;
+    if (c->p.periodic) vol = c->p.box[0] * c->p.box[1] * c->p.box[2];
+    else {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        const double *P[3] = {px, py, pz};
+        for (int i = 0; i < c->n; i++)
+            for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], P[d][i]); hi[d] = std::max(hi[d], P[d][i]); }
+        vol = 1.0;
+        for (int d = 0; d < 3; d++) vol *= std::max(hi[d] - lo[d], 2.0);
+    }
+    const double rho = c->n / std::max(vol, 1.0);
+    const double rl = c->p.r_skin;
+    double est = 1.35 * (4.0 / 3.0) * M_PI * rl * rl * rl * rho + 48.0;
+    est = std::min(est, (double)c->n + 32.0);
+    int cap = ((int)std::ceil(est) + 31) / 32 * 32;
+    return std::max(cap, 32);
+}
+
+int do_build(gm_ctx *c) {
+    // list build on the resident positions, growing the capacity on overflow
+    for (int attempt = 0; attempt < 6; attempt++) {
+        int rc = reset_status(c);
+        if (rc) return rc;
+        c->launches += seq_rebuild(c, c->stream);
+        rc = check_status(c, nullptr);
+        if (rc == GM_ERR_LIST_OVERFLOW) {
+            int newcap = ((int)(c->cap * 1.5) + 31) / 32 * 32;
+            rc = ensure_list_buffers(c, newcap);
+            if (rc) return rc;
+            continue;
+        }
+        if (rc) return rc;
+        c->built = true;
+        c->forces_current = false;
+        return GM_OK;
+    }
+    return fail(c, GM_ERR_LIST_OVERFLOW, "neighbour list capacity could not be sized");
+}
+
+int upload3(gm_ctx *c, double *dst, const double *x, const double *y, const double *z) {
+    const size_t b = sizeof(double) * (size_t)c->n;
+    if (!c->n) return GM_OK;
+    GM_CUDA(c, cudaMemcpyAsync(dst, x, b, cudaMemcpyHostToDevice, c->stream));
+    GM_CUDA(c, cudaMemcpyAsync(dst + c->n, y, b, cudaMemcpyHostToDevice, c->stream));
+    GM_CUDA(c, cudaMemcpyAsync(dst + 2 * c->n, z, b, cudaMemcpyHostToDevice, c->stream));
+    return GM_OK;
+}
+
+int download3(gm_ctx *c, const double *src, double *x, double *y, double *z) {
+    const size_t b = sizeof(double) * (size_t)c->n;
+    if (!c->n) return GM_OK;
+    if (x) GM_CUDA(c, cudaMemcpyAsync(x, src, b, cudaMemcpyDeviceToHost, c->stream));
+    if (y) GM_CUDA(c, cudaMemcpyAsync(y, src + c->n, b, cudaMemcpyDeviceToHost, c->stream));
+    if (z) GM_CUDA(c, cudaMemcpyAsync(z, src + 2 * c->n, b, cudaMemcpyDeviceToHost, c->stream));
+    return GM_OK;
+}
+
+// One BAB + RATTLE step (lib.rs:292-323) issued on stream s.  With a graph
+// conditional handle the rebuild runs inside an IF node; otherwise the check
+// result is read back on the host.
+int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, long long *count) {
+    long long k = 0;
+    const int n = c->n;
+    const bool constrained = c->n_clusters > 0;
+    gm_launch_half_kick(n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+    gm_launch_drift(n, c->d_pos, c->d_vel, c->d_dref, dt, !constrained, c->d_status, s); k++;
+    if (constrained) {
+        gm_launch_shake(cluster_args(c), n, c->d_dref, c->d_pos, s); k += 4;
+        gm_launch_resync(n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, s); k++;
+    }
+    const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
+    gm_launch_check(n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, cond, gm_check_blocks(n), s); k++;
+    *count += k;
+    return GM_OK;
+}
+
+int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
+    long long k = seq_forces(c, s);
+    gm_launch_half_kick(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+    if (c->n_clusters) { gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, s); k += 3; }
+    gm_launch_step(c->d_status, s); k++;
+    *count += k;
+    return GM_OK;
+}
+
+int capture_graph(gm_ctx *c, double dt) {
+    if (c->graph_exec && c->graph_dt == dt && c->graph_cap == c->cap) return GM_OK;
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+    cudaGraph_t g;
+    GM_CUDA(c, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    GM_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    GM_CUDA(c, cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    long long count = 0;
+    issue_step(c, c->stream, dt, (unsigned long long)h, &count);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t ndeps = 0;
+    cudaGraph_t capg = nullptr;
+    GM_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &capg, &deps, &edges, &ndeps));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    GM_CUDA(c, cudaGraphAddNode(&cnode, capg, deps, edges, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    GM_CUDA(c, cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    seq_rebuild(c, c->side);
+    GM_CUDA(c, cudaStreamEndCapture(c->side, &body));
+    GM_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    issue_step_tail(c, c->stream, dt, &count);
+    GM_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+    GM_CUDA(c, cudaGraphInstantiate(&c->graph_exec, g, 0));
+    c->graph = g;
+    c->graph_dt = dt;
+    c->graph_cap = c->cap;
+    c->launches_per_step = count;
+    return GM_OK;
+}
+
+int ensure_forces(gm_ctx *c) {
+    // the first half-kick of a step needs forces at the current positions
+    if (c->forces_current) return GM_OK;
+    if (!c->built) {
+        int rc = do_build(c);
+        if (rc) return rc;
+    }
+    c->launches += seq_forces(c, c->stream);
+    c->forces_current = true;
+    return GM_OK;
+}
+
+void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int> &cj, std::vector<int> &cstart,
+                    std::vector<int> &cons, std::vector<int> &astart, std::vector<int> &atoms,
+                    std::vector<int> &acstart, std::vector<int> &acons) {
+    // connected components of the constraint graph (union-find over atoms)
+    const int nc = (int)ci.size();
+    std::vector<int> parent((size_t)c->n);
+    std::iota(parent.begin(), parent.end(), 0);
+    auto find = [&](int x) {
+        while (parent[(size_t)x] != x) { parent[(size_t)x] = parent[(size_t)parent[(size_t)x]]; x = parent[(size_t)x]; }
+        return x;
+    };
+    for (int k = 0; k < nc; k++) {
+        int a = find(ci[(size_t)k]), b = find(cj[(size_t)k]);
+        if (a != b) parent[(size_t)std::max(a, b)] = std::min(a, b);
+    }
+    std::map<int, int> root_id;
+    std::vector<std::vector<int>> ccons, catoms;
+    for (int k = 0; k < nc; k++) {
+        int r = find(ci[(size_t)k]);
+        auto it = root_id.find(r);
+        if (it == root_id.end()) { it = root_id.emplace(r, (int)ccons.size()).first; ccons.emplace_back(); catoms.emplace_back(); }
+        ccons[(size_t)it->second].push_back(k);  // ascending k
+    }
+    cstart.assign(1, 0);
+    astart.assign(1, 0);
+    acstart.assign(1, 0);
+    cons.clear(); atoms.clear(); acons.clear();
+    for (size_t q = 0; q < ccons.size(); q++) {
+        std::vector<int> at;
+        for (int k : ccons[q]) { at.push_back(ci[(size_t)k]); at.push_back(cj[(size_t)k]); }
+        std::sort(at.begin(), at.end());
+        at.erase(std::unique(at.begin(), at.end()), at.end());
+        for (int k : ccons[q]) cons.push_back(k);
+        cstart.push_back((int)cons.size());
+        for (int a : at) {
+            atoms.push_back(a);
+            for (int k : ccons[q]) {
+                // per atom, its constraints in ascending order; i side negative
+                if (ci[(size_t)k] == a) acons.push_back(-k - 1);
+                if (cj[(size_t)k] == a) acons.push_back(k);
+            }
+            acstart.push_back((int)acons.size());
+        }
+        astart.push_back((int)atoms.size());
+    }
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *params, int32_t *status) {
+    int32_t dummy;
+    if (!status) status = &dummy;
+    *status = GM_OK;
+    if (!atoms || !t || !params || atoms->n_atoms < 0 || atoms->n_atoms > INT32_MAX / 2) {
+        *status = GM_ERR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    const gm_params &p = *params;
+    // config.rs:213-248 validation
+    if (!(p.r_switch < p.r_cutoff && p.r_cutoff < p.r_skin) || !(p.box[0] > 0 && p.box[1] > 0 && p.box[2] > 0) ||
+        p.max_constr_iter == 0 || !(p.constr_tol > 0) ||
+        (p.precision != GM_PRECISION_MIXED && p.precision != GM_PRECISION_FP64)) {
+        *status = GM_ERR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || p.device < 0 || p.device >= ndev) {
+        cudaGetLastError();
+        *status = GM_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    gm_ctx *c = new gm_ctx();
+    c->device = p.device;
+    c->p = p;
+    c->n = (int)atoms->n_atoms;
+    c->fp64 = p.precision == GM_PRECISION_FP64;
+    const int n = c->n;
+    auto bail = [&](int code) -> gm_ctx * {
+        *status = code;
+        gm_destroy(c);
+        return nullptr;
+    };
+    if (cudaSetDevice(c->device) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    int rc;
+#define TRY(x) do { rc = (x); if (rc) return bail(rc); } while (0)
+    // ---- atoms: deduplicate (sigma, epsilon) into types
+    std::map<std::pair<double, double>, int> types;
+    std::vector<int> type((size_t)n);
+    std::vector<double> tsig, teps;
+    for (int i = 0; i < n; i++) {
+        auto key = std::make_pair(atoms->sigma[i], atoms->epsilon[i]);
+        auto it = types.find(key);
+        if (it == types.end()) {
+            it = types.emplace(key, (int)tsig.size()).first;
+            tsig.push_back(key.first);
+            teps.push_back(key.second);
+        }
+        type[(size_t)i] = it->second;
+    }
+    c->ntypes = std::max((int)tsig.size(), 1);
+    if (c->ntypes > GM_MAX_TYPES) {
+        fail(c, GM_ERR_UNSUPPORTED, "%d distinct (sigma, epsilon) pairs; at most %d are supported", c->ntypes, GM_MAX_TYPES);
+        return bail(GM_ERR_UNSUPPORTED);
+    }
+    std::vector<float2> tab32((size_t)c->ntypes * c->ntypes);
+    std::vector<double2> tab64((size_t)c->ntypes * c->ntypes);
+    for (int a = 0; a < (int)tsig.size(); a++)
+        for (int b = 0; b < (int)tsig.size(); b++) {
+            // nonbonded.rs:46-47 Lorentz-Berthelot, evaluated as the reference does
+            const double sg = 0.5 * (tsig[(size_t)a] + tsig[(size_t)b]);
+            const double ep = std::sqrt(teps[(size_t)a] * teps[(size_t)b]);
+            tab64[(size_t)a * c->ntypes + b] = make_double2(sg, ep);
+            tab32[(size_t)a * c->ntypes + b] = make_float2((float)(sg * sg), (float)ep);
+        }
+    std::vector<double> inv_mass((size_t)n), charge64((size_t)n);
+    std::vector<float> charge((size_t)n);
+    for (int i = 0; i < n; i++) {
+        inv_mass[(size_t)i] = 1.0 / atoms->mass[i];  // integrator.rs:16, constraint.rs:110
+        charge64[(size_t)i] = atoms->charge ? atoms->charge[i] : 0.0;
+        charge[(size_t)i] = (float)charge64[(size_t)i];
+    }
+    TRY(dupload(c, &c->d_mass, atoms->mass, (size_t)n));
+    TRY(dupload(c, &c->d_inv_mass, inv_mass.data(), (size_t)n));
+    TRY(dupload(c, &c->d_sigma, atoms->sigma, (size_t)n));
+    TRY(dupload(c, &c->d_eps, atoms->epsilon, (size_t)n));
+    TRY(dupload(c, &c->d_charge64, charge64.data(), (size_t)n));
+    TRY(dupload(c, &c->d_charge, charge.data(), (size_t)n));
+    TRY(dupload(c, &c->d_type, type.data(), (size_t)n));
+    TRY(dupload(c, &c->d_tab32, tab32.data(), tab32.size()));
+    TRY(dupload(c, &c->d_tab64, tab64.data(), tab64.size()));
+    // ---- exclusions: symmetric CSR, ascending (neighbor.rs:18-23 set semantics)
+    std::vector<std::vector<int>> ex((size_t)n);
+    for (int64_t e = 0; e < t->n_excl; e++) {
+        const uint32_t i = t->excl_i[e], j = t->excl_j[e];
+        if ((int64_t)i >= n || (int64_t)j >= n) { fail(c, GM_ERR_INVALID_ARGUMENT, "exclusion %lld out of range", (long long)e); return bail(GM_ERR_INVALID_ARGUMENT); }
+        if (i == j) continue;
+        ex[i].push_back((int)j);
+        ex[j].push_back((int)i);
+    }
+    std::vector<int> excl_start((size_t)n + 1, 0), excl;
+    for (int i = 0; i < n; i++) {
+        auto &v = ex[(size_t)i];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        excl.insert(excl.end(), v.begin(), v.end());
+        excl_start[(size_t)i + 1] = (int)excl.size();
+    }
+    TRY(dupload(c, &c->d_excl_start, excl_start.data(), excl_start.size()));
+    TRY(dupload(c, &c->d_excl, excl.data(), excl.size()));
+    // ---- bonded
+    auto check_idx = [&](const uint32_t *a, int64_t cnt) {
+        for (int64_t k = 0; k < cnt; k++) if ((int64_t)a[k] >= n) return false;
+        return true;
+    };
+    if (!check_idx(t->bond_i, t->n_bonds) || !check_idx(t->bond_j, t->n_bonds) || !check_idx(t->angle_i, t->n_angles) ||
+        !check_idx(t->angle_j, t->n_angles) || !check_idx(t->angle_k, t->n_angles) || !check_idx(t->dihed_i, t->n_diheds) ||
+        !check_idx(t->dihed_j, t->n_diheds) || !check_idx(t->dihed_k, t->n_diheds) || !check_idx(t->dihed_l, t->n_diheds) ||
+        !check_idx(t->constr_i, t->n_constr) || !check_idx(t->constr_j, t->n_constr)) {
+        fail(c, GM_ERR_INVALID_ARGUMENT, "topology index out of range");
+        return bail(GM_ERR_INVALID_ARGUMENT);
+    }
+    c->n_bonds = (int)t->n_bonds;
+    c->n_angles = (int)t->n_angles;
+    c->n_diheds = (int)t->n_diheds;
+    c->bonded_blocks = gm_bonded_blocks(c->n_bonds, c->n_angles, c->n_diheds);
+    auto v = [](const uint32_t *a, int64_t cnt) { return to_int(a, cnt); };
+    TRY(dupload(c, &c->d_bi, v(t->bond_i, t->n_bonds).data(), (size_t)t->n_bonds));
+    TRY(dupload(c, &c->d_bj, v(t->bond_j, t->n_bonds).data(), (size_t)t->n_bonds));
+    TRY(dupload(c, &c->d_bk, t->bond_k, (size_t)t->n_bonds));
+    TRY(dupload(c, &c->d_br0, t->bond_r0, (size_t)t->n_bonds));
+    TRY(dupload(c, &c->d_ai, v(t->angle_i, t->n_angles).data(), (size_t)t->n_angles));
+    TRY(dupload(c, &c->d_aj, v(t->angle_j, t->n_angles).data(), (size_t)t->n_angles));
+    TRY(dupload(c, &c->d_ak, v(t->angle_k, t->n_angles).data(), (size_t)t->n_angles));
+    TRY(dupload(c, &c->d_akth, t->angle_kth, (size_t)t->n_angles));
+    TRY(dupload(c, &c->d_ath0, t->angle_th0, (size_t)t->n_angles));
+    TRY(dupload(c, &c->d_di, v(t->dihed_i, t->n_diheds).data(), (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_dj, v(t->dihed_j, t->n_diheds).data(), (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_dk, v(t->dihed_k, t->n_diheds).data(), (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_dl, v(t->dihed_l, t->n_diheds).data(), (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_dkphi, t->dihed_kphi, (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_dn, v(t->dihed_n, t->n_diheds).data(), (size_t)t->n_diheds));
+    TRY(dupload(c, &c->d_ddelta, t->dihed_delta, (size_t)t->n_diheds));
+    // ---- scaled 1-4 pairs (beyond the reference; off by default)
+    if (p.scale14_lj != 0.0 || (p.coulomb && p.scale14_coul != 0.0)) {
+        std::vector<std::pair<int, int>> close;
+        for (int64_t b = 0; b < t->n_bonds; b++)
+            close.emplace_back(std::min(t->bond_i[b], t->bond_j[b]), std::max(t->bond_i[b], t->bond_j[b]));
+        for (int64_t a = 0; a < t->n_angles; a++)
+            close.emplace_back(std::min(t->angle_i[a], t->angle_k[a]), std::max(t->angle_i[a], t->angle_k[a]));
+        std::sort(close.begin(), close.end());
+        std::vector<std::pair<int, int>> p14;
+        for (int64_t d = 0; d < t->n_diheds; d++) {
+            int i = (int)t->dihed_i[d], l = (int)t->dihed_l[d];
+            if (i == l) continue;
+            auto key = std::make_pair(std::min(i, l), std::max(i, l));
+            if (std::binary_search(close.begin(), close.end(), key)) continue;
+            p14.push_back(key);
+        }
+        std::sort(p14.begin(), p14.end());
+        p14.erase(std::unique(p14.begin(), p14.end()), p14.end());
+        std::vector<int> a((size_t)p14.size()), b((size_t)p14.size());
+        for (size_t k = 0; k < p14.size(); k++) { a[k] = p14[k].first; b[k] = p14[k].second; }
+        c->n14 = (int)p14.size();
+        c->blocks14 = (c->n14 + 255) / 256;
+        TRY(dupload(c, &c->d_p14i, a.data(), a.size()));
+        TRY(dupload(c, &c->d_p14j, b.data(), b.size()));
+    }
+    // ---- constraints as independent clusters
+    c->n_constr = (int)t->n_constr;
+    c->h_ci = v(t->constr_i, t->n_constr);
+    c->h_cj = v(t->constr_j, t->n_constr);
+    if (c->n_constr) {
+        std::vector<int> cstart, cons, astart, cat, acstart, acons;
+        build_clusters(c, c->h_ci, c->h_cj, cstart, cons, astart, cat, acstart, acons);
+        c->n_clusters = (int)cstart.size() - 1;
+        TRY(dupload(c, &c->d_ci, c->h_ci.data(), c->h_ci.size()));
+        TRY(dupload(c, &c->d_cj, c->h_cj.data(), c->h_cj.size()));
+        TRY(dupload(c, &c->d_cdsq, t->constr_dsq, (size_t)c->n_constr));
+        TRY(dupload(c, &c->d_cl_cstart, cstart.data(), cstart.size()));
+        TRY(dupload(c, &c->d_cl_cons, cons.data(), cons.size()));
+        TRY(dupload(c, &c->d_cl_astart, astart.data(), astart.size()));
+        TRY(dupload(c, &c->d_cl_atoms, cat.data(), cat.size()));
+        TRY(dupload(c, &c->d_cl_acstart, acstart.data(), acstart.size()));
+        TRY(dupload(c, &c->d_cl_acons, acons.data(), acons.size()));
+        TRY(dalloc(c, &c->d_lam, (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_rvec, 3 * (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_cl_iters, (size_t)c->n_clusters));
+        TRY(dalloc(c, &c->d_cl_worst, (size_t)c->n_clusters));
+        TRY(dalloc(c, &c->d_cl_worst_idx, (size_t)c->n_clusters));
+    }
+    // ---- state, sorted copies, cells
+    TRY(dalloc(c, &c->d_pos, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_vel, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_ref, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_dref, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_fout, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_host_f, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_force, 3 * (size_t)n));
+    TRY(dalloc(c, &c->d_hi, (size_t)n));
+    TRY(dalloc(c, &c->d_lo, (size_t)n));
+    if (c->fp64) {
+        TRY(dalloc(c, &c->d_pos64s, (size_t)n));
+        TRY(dalloc(c, &c->d_type_sorted, (size_t)n));
+    }
+    TRY(dalloc(c, &c->d_perm, (size_t)n));
+    TRY(dalloc(c, &c->d_cell_of, (size_t)n));
+    TRY(dalloc(c, &c->d_cell_sorted, (size_t)n));
+    TRY(dalloc(c, &c->d_tmp_atom, (size_t)n));
+    c->max_cells = std::max(2 * n, 4096);
+    TRY(dalloc(c, &c->d_cell_count, (size_t)c->max_cells));
+    TRY(dalloc(c, &c->d_cell_cursor, (size_t)c->max_cells));
+    TRY(dalloc(c, &c->d_cell_start, (size_t)c->max_cells + 1));
+    TRY(dalloc(c, &c->d_grid, 1));
+    c->bbox_blocks = std::max(1, std::min(256, (n + 255) / 256));
+    TRY(dalloc(c, &c->d_bbox, 6 * (size_t)c->bbox_blocks));
+    c->n_groups = (n + 31) / 32;
+    TRY(dalloc(c, &c->d_count, (size_t)c->n_groups * 32));
+    TRY(dalloc(c, &c->d_gmax, (size_t)c->n_groups));
+    c->n_epart = c->n_groups + c->bonded_blocks + c->blocks14;
+    TRY(dalloc(c, &c->d_epart, (size_t)c->n_epart));
+    TRY(dalloc(c, &c->d_energy, 1));
+    TRY(dalloc(c, &c->d_kin_part, 256));
+    TRY(dalloc(c, &c->d_ke, 1));
+    TRY(dalloc(c, &c->d_status, 1));
+    if (cudaMallocHost((void **)&c->h_status, sizeof(DevStatus)) != cudaSuccess) return bail(GM_ERR_OUT_OF_MEMORY);
+    DevStatus z{};
+    z.fail_step = ~0ull;
+    if (cudaMemcpy(c->d_status, &z, sizeof z, cudaMemcpyHostToDevice) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (n) {
+        cudaMemset(c->d_force, 0, sizeof(long long) * 3 * (size_t)n);
+        cudaMemset(c->d_pos, 0, sizeof(double) * 3 * (size_t)n);
+        cudaMemset(c->d_vel, 0, sizeof(double) * 3 * (size_t)n);
+        cudaMemset(c->d_ref, 0, sizeof(double) * 3 * (size_t)n);
+    }
+#undef TRY
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(GM_ERR_DEVICE);
+    return c;
+}
+
+int32_t gm_destroy(gm_ctx *c) {
+    if (!c) return GM_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    for (void *ptr : c->allocs) cudaFree(ptr);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    delete c;
+    return GM_OK;
+}
+
+int32_t gm_n_threads(const gm_ctx *) { return 1; }
+
+int32_t gm_last_error(const gm_ctx *c, char *buf, int64_t len) {
+    if (!buf || len <= 0) return GM_ERR_INVALID_ARGUMENT;
+    const char *m = c ? c->err.c_str() : "no context";
+    snprintf(buf, (size_t)len, "%s", m);
+    return GM_OK;
+}
+
+int32_t gm_build_list(gm_ctx *c, double *px, double *py, double *pz) {
+    if (!c || (!px && c->n)) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position passed to build_neighbor_list");
+    if (!c->d_list) {
+        int rc = ensure_list_buffers(c, estimate_cap(c, px, py, pz));
+        if (rc) return rc;
+    }
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (rc) return rc;
+    rc = do_build(c);
+    if (rc) return rc;
+    if (c->p.periodic) {
+        rc = download3(c, c->d_pos, px, py, pz);  // neighbor.rs:13-15 wraps the caller's state
+        if (rc) return rc;
+        GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return GM_OK;
+}
+
+int32_t gm_compute_forces(gm_ctx *c, const double *px, const double *py, const double *pz, double *fx, double *fy,
+                          double *fz, double *energy) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    auto poison = [&](int code) {
+        // compute_forces is infallible in the trait: NaN forces make the run
+        // loop's check_forces_finite (lib.rs:307) stop the run
+        const double nan = std::nan("");
+        for (int i = 0; i < c->n; i++) { if (fx) fx[i] = nan; if (fy) fy[i] = nan; if (fz) fz[i] = nan; }
+        if (energy) *energy = nan;
+        return code;
+    };
+    if (cudaSetDevice(c->device) != cudaSuccess) return poison(GM_ERR_DEVICE);
+    if (!c->built) return poison(fail(c, GM_ERR_NOT_BUILT, "compute_forces before build_neighbor_list"));
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (rc) return poison(rc);
+    rc = reset_status(c);
+    if (rc) return poison(rc);
+    c->launches += seq_forces(c, c->stream);
+    gm_launch_forces_out(c->n, c->d_force, c->d_fout, c->stream);
+    c->launches++;
+    rc = download3(c, c->d_fout, fx, fy, fz);
+    if (rc) return poison(rc);
+    if (energy) GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    rc = check_status(c, nullptr);
+    if (rc) return poison(rc);
+    c->forces_current = true;
+    return GM_OK;
+}
+
+int32_t gm_needs_rebuild(gm_ctx *c, const double *px, const double *py, const double *pz, int32_t *result) {
+    if (!c || !result) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!c->built) { *result = 1; return GM_OK; }
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (rc) return rc;
+    rc = reset_status(c);
+    if (rc) return rc;
+    const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;
+    gm_launch_check(c->n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, 0ull, gm_check_blocks(c->n), c->stream);
+    c->launches++;
+    rc = st_read(c);
+    if (rc) return rc;
+    *result = c->h_status->rebuild ? 1 : 0;
+    return GM_OK;
+}
+
+int32_t gm_geodesic_drift(gm_ctx *c, double *px, double *py, double *pz, double *vx, double *vy, double *vz,
+                          double dt, uint64_t step, gm_convergence *err) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    rc = reset_status(c);
+    if (!rc) rc = set_step(c, step);
+    if (rc) return rc;
+    const bool constrained = c->n_clusters > 0;
+    gm_launch_drift(c->n, c->d_pos, c->d_vel, c->d_dref, dt, !constrained, c->d_status, c->stream);
+    c->launches++;
+    if (constrained) {
+        gm_launch_shake(cluster_args(c), c->n, c->d_dref, c->d_pos, c->stream);
+        gm_launch_resync(c->n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, c->stream);
+        c->launches += 5;
+    }
+    rc = download3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = download3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    c->forces_current = false;
+    return check_status(c, err);
+}
+
+int32_t gm_half_kick(gm_ctx *c, double *vx, double *vy, double *vz, const double *fx, const double *fy,
+                     const double *fz, double dt_half) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (!rc) rc = upload3(c, c->d_host_f, fx, fy, fz);
+    if (rc) return rc;
+    gm_launch_half_kick_f64(c->n, c->d_vel, c->d_host_f, c->d_inv_mass, dt_half, c->stream);
+    c->launches++;
+    rc = download3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+int32_t gm_constrain_velocities(gm_ctx *c, const double *px, const double *py, const double *pz, double *vx,
+                                double *vy, double *vz, uint64_t step, gm_convergence *err) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!c->n_clusters) return GM_OK;  // constraint.rs:183-186
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    rc = reset_status(c);
+    if (!rc) rc = set_step(c, step);
+    if (rc) return rc;
+    gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, c->stream);
+    c->launches += 3;
+    rc = download3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    return check_status(c, err);
+}
+
+int32_t gm_kinetic_energy(gm_ctx *c, const double *vx, const double *vy, const double *vz, double *ke) {
+    if (!c || !ke) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    gm_launch_kinetic(c->n, c->d_vel, c->d_mass, c->d_kin_part, 64, c->d_ke, c->stream);
+    c->launches += 2;
+    GM_CUDA(c, cudaMemcpyAsync(ke, c->d_ke, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+int32_t gm_get_pairs(gm_ctx *c, int64_t cap, uint32_t *pair_i, uint32_t *pair_j, int64_t *n_pairs) {
+    if (!c || !n_pairs) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!c->built) return fail(c, GM_ERR_NOT_BUILT, "no neighbour list");
+    const int n = c->n;
+    std::vector<int> perm((size_t)n), count((size_t)c->n_groups * 32), list((size_t)c->n_groups * 32 * c->cap);
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (n) {
+        GM_CUDA(c, cudaMemcpy(perm.data(), c->d_perm, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+        GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+        GM_CUDA(c, cudaMemcpy(list.data(), c->d_list, sizeof(int) * list.size(), cudaMemcpyDeviceToHost));
+    }
+    std::vector<uint64_t> keys;
+    for (int s = 0; s < n; s++) {
+        const int g = s / 32, l = s % 32;
+        for (int e = 0; e < count[(size_t)s]; e++) {
+            const int j = list[(size_t)g * 32 * c->cap + (size_t)e * 32 + l];
+            const uint32_t a = (uint32_t)perm[(size_t)s], b = (uint32_t)perm[(size_t)j];
+            if (a < b) keys.push_back(((uint64_t)a << 32) | b);
+        }
+    }
+    std::sort(keys.begin(), keys.end());
+    *n_pairs = (int64_t)keys.size();
+    if (pair_i && pair_j) {
+        const int64_t m = std::min<int64_t>(cap, (int64_t)keys.size());
+        for (int64_t k = 0; k < m; k++) { pair_i[k] = (uint32_t)(keys[(size_t)k] >> 32); pair_j[k] = (uint32_t)keys[(size_t)k]; }
+    }
+    return GM_OK;
+}
+
+int32_t gm_upload_state(gm_ctx *c, const double *px, const double *py, const double *pz, const double *vx,
+                        const double *vy, const double *vz) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position");
+    if (!c->d_list) {
+        int rc = ensure_list_buffers(c, estimate_cap(c, px, py, pz));
+        if (rc) return rc;
+    }
+    int rc = upload3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    c->built = false;
+    c->forces_current = false;
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+int32_t gm_download_state(gm_ctx *c, double *px, double *py, double *pz, double *vx, double *vy, double *vz) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = download3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = download3(c, c->d_vel, vx, vy, vz);
+    if (rc) return rc;
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return GM_OK;
+}
+
+int32_t gm_forces_resident(gm_ctx *c) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!c->built) {
+        int rc = do_build(c);
+        if (rc) return rc;
+    }
+    c->launches += seq_forces(c, c->stream);
+    c->forces_current = true;
+    return GM_OK;
+}
+
+int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps) {
+    if (!c || !(dt > 0) || n_steps < 0) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = reset_status(c);
+    if (!rc) rc = set_step(c, first_step);
+    if (rc) return rc;
+    rc = ensure_forces(c);
+    if (rc) return rc;
+    rc = capture_graph(c, dt);
+    if (rc) return rc;
+    for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+    c->launches += c->launches_per_step * n_steps;
+    return GM_OK;
+}
+
+int32_t gm_synchronize(gm_ctx *c, gm_convergence *err) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    return check_status(c, err);
+}
+
+void *gm_stream(gm_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double dt,
+                 uint64_t first_step, int64_t n_steps, double *fx, double *fy, double *fz, double *energy,
+                 int64_t *n_rebuilds, gm_convergence *err) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    int rc = gm_upload_state(c, px, py, pz, vx, vy, vz);
+    if (rc) return rc;
+    rc = st_read(c);
+    if (rc) return rc;
+    const unsigned long long r0 = c->h_status->n_rebuilds;
+    rc = gm_run_resident(c, dt, first_step, n_steps);
+    if (rc) return rc;
+    rc = check_status(c, err);
+    const unsigned long long r1 = c->h_status->n_rebuilds;
+    if (n_rebuilds) *n_rebuilds = (int64_t)(r1 - r0);
+    int rc2 = download3(c, c->d_pos, px, py, pz);
+    if (!rc2) rc2 = download3(c, c->d_vel, vx, vy, vz);
+    if (!rc2 && (fx || fy || fz)) {
+        gm_launch_forces_out(c->n, c->d_force, c->d_fout, c->stream);
+        c->launches++;
+        rc2 = download3(c, c->d_fout, fx, fy, fz);
+    }
+    if (!rc2 && energy) GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return rc ? rc : rc2;
+}
+
+int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {
+    if (!cc || !out) return GM_ERR_INVALID_ARGUMENT;
+    gm_ctx *c = const_cast<gm_ctx *>(cc);
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = st_read(c);
+    if (rc) return rc;
+    const DevStatus st = *c->h_status;
+    int64_t v[8] = {0, (int64_t)st.n_rebuilds, c->cap, c->launches, (int64_t)st.shake_T, (int64_t)st.rattle_T,
+                    c->launches_per_step, 0};
+    if (c->built && n > 0) {
+        // pairs in the current list (half of the symmetric entries)
+        std::vector<int> count((size_t)c->n);
+        if (c->n) GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)c->n, cudaMemcpyDeviceToHost));
+        long long s = 0;
+        for (int x : count) s += x;
+        v[0] = s / 2;
+    }
+    for (int64_t k = 0; k < n && k < 8; k++) out[k] = v[k];
+    return GM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,414 @@
+// gm_force.cu — force and energy kernels.
+//
+// Nonbonded (force/nonbonded.rs:20-82 physics): one lane per cell-sorted atom
+// i walks its own column of the symmetric neighbour list, gathers each j's
+// float4 pair (hi, lo) through the read-only path and accumulates the force
+// on i only, so no atomics are needed and every atom's sum has a fixed order.
+// In mixed precision the pair arithmetic is FP32; per-lane partial sums over
+// chunks of 32 entries are folded into int64 fixed point (2^-40 kcal/mol/A),
+// and the energy into FP64.  Each pair is evaluated by both of its atoms
+// (the list is symmetric), the energy total is halved.
+// Bonded terms (force/bonded.rs) use one thread per term and int64 atomics;
+// integer addition is associative, so the result is run-to-run identical.
+#include "gm_internal.cuh"
+
+namespace {
+
+constexpr int kPairWarps = 4;
+constexpr int kChunk = 32;
+constexpr float kCoulomb = 332.0522173f;
+constexpr double kCoulomb64 = 332.0522173;
+
+template <bool PERIODIC, bool COULOMB>
+__global__ void __launch_bounds__(kPairWarps * 32)
+pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
+                const int *__restrict__ gmax, int ntypes, const float2 *__restrict__ tab, float rc2, float rsw,
+                float inv_wsw, float bx, float by, float bz, float ibx, float iby, float ibz,
+                long long *__restrict__ force, double *__restrict__ epart, DevStatus *st) {
+    extern __shared__ float2 s_tab[];
+    for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab[t] = tab[t];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int group = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    if (group * 32 >= n) return;
+    const int s = group * 32 + lane;
+    const bool valid = s < n;
+    float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
+    int cnt = 0;
+    if (valid) { mh = hi[s]; ml = lo[s]; cnt = count[s]; }
+    const float2 *trow = s_tab + (valid ? __float_as_int(mh.w) : 0) * ntypes;
+    const float qi = ml.w * kCoulomb;
+    const int gm = gmax[group];
+    const int *L = list + (size_t)group * 32 * cap + lane;
+    long long ax = 0, ay = 0, az = 0;
+    double eacc = 0.0;
+    unsigned int bad = 0;
+    for (int e0 = 0; e0 < gm; e0 += kChunk) {
+        float fx = 0.f, fy = 0.f, fz = 0.f, ev = 0.f;
+        const int e1 = min(e0 + kChunk, gm);
+#pragma unroll 4
+        for (int e = e0; e < e1; e++) {
+            if (e < cnt) {
+                const int j = __ldg(L + (size_t)e * 32);
+                const float4 jh = __ldg(hi + j);
+                const float4 jl = __ldg(lo + j);
+                float dx = (jh.x - mh.x) + (jl.x - ml.x);
+                float dy = (jh.y - mh.y) + (jl.y - ml.y);
+                float dz = (jh.z - mh.z) + (jl.z - ml.z);
+                if (PERIODIC) {
+                    dx -= bx * rintf(dx * ibx);
+                    dy -= by * rintf(dy * iby);
+                    dz -= bz * rintf(dz * ibz);
+                }
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 <= rc2 && r2 > 0.f) {
+                    const float2 p = trow[__float_as_int(jh.w)];
+                    const float rinv = rsqrtf(r2);
+                    const float rinv2 = rinv * rinv;
+                    const float s2 = p.x * rinv2;
+                    const float s6 = s2 * s2 * s2;
+                    const float s12 = s6 * s6;
+                    float v = 4.f * p.y * (s12 - s6);
+                    float fr = 24.f * p.y * (2.f * s12 - s6) * rinv2;  // F_r / r
+                    if (COULOMB) {
+                        const float vc = qi * jl.w * rinv;
+                        v += vc;
+                        fr += vc * rinv2;
+                    }
+                    const float r = r2 * rinv;
+                    if (r > rsw) {
+                        const float u = (r - rsw) * inv_wsw;
+                        const float u2 = u * u;
+                        const float sw = 1.f + u2 * u * (-10.f + u * (15.f - 6.f * u));
+                        const float dsw = -30.f * u2 * (1.f - u) * (1.f - u) * inv_wsw;
+                        fr = fr * sw - v * dsw * rinv;
+                        v *= sw;
+                    }
+                    fx -= fr * dx;
+                    fy -= fr * dy;
+                    fz -= fr * dz;
+                    ev += v;
+                }
+            }
+        }
+        ax += gm_to_fix_checked(fx, bad);
+        ay += gm_to_fix_checked(fy, bad);
+        az += gm_to_fix_checked(fz, bad);
+        eacc += (double)ev;
+    }
+    if (valid) {
+        const int a = perm[s];
+        gm_atomic_fix_add(force + a, ax);
+        gm_atomic_fix_add(force + n + a, ay);
+        gm_atomic_fix_add(force + 2 * n + a, az);
+    }
+    for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
+    if (lane == 0) epart[group] = 0.5 * eacc;
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && lane == 0) atomicOr(&st->error, bad);
+}
+
+template <bool PERIODIC, bool COULOMB>
+__global__ void __launch_bounds__(kPairWarps * 32)
+pair_kernel_f64(int n, int cap, const double4 *__restrict__ p64, const int *__restrict__ type_s,
+                const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
+                const int *__restrict__ gmax, int ntypes, const double2 *__restrict__ tab, double rc2, double rsw,
+                double rc, double bx, double by, double bz, long long *__restrict__ force,
+                double *__restrict__ epart, DevStatus *st) {
+    extern __shared__ double2 s_tab64[];
+    for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab64[t] = tab[t];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int group = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    if (group * 32 >= n) return;
+    const int s = group * 32 + lane;
+    const bool valid = s < n;
+    double4 mi = make_double4(0, 0, 0, 0);
+    int cnt = 0, ti = 0;
+    if (valid) { mi = p64[s]; cnt = count[s]; ti = type_s[s]; }
+    const double2 *trow = s_tab64 + ti * ntypes;
+    const double qi = mi.w * kCoulomb64;
+    const int gm = gmax[group];
+    const int *L = list + (size_t)group * 32 * cap + lane;
+    double fx = 0, fy = 0, fz = 0, eacc = 0;
+    const double wsw = rc - rsw;
+    for (int e = 0; e < gm; e++) {
+        if (e >= cnt) continue;
+        const int j = __ldg(L + (size_t)e * 32);
+        const double4 pj = p64[j];
+        double dx = pj.x - mi.x, dy = pj.y - mi.y, dz = pj.z - mi.z;
+        if (PERIODIC) {
+            dx -= bx * round(dx / bx);
+            dy -= by * round(dy / by);
+            dz -= bz * round(dz / bz);
+        }
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 > rc2 || r2 == 0.0) continue;
+        const double r = sqrt(r2);
+        const double rinv = 1.0 / r;
+        const double2 p = trow[type_s[j]];
+        double v = 0.0, fr = 0.0;  // fr = F_r (radial magnitude)
+        if (p.y != 0.0) {
+            const double sr = p.x * rinv;
+            const double s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
+            v = 4.0 * p.y * (s12 - s6);
+            fr = 24.0 * p.y * rinv * (2.0 * s12 - s6);
+        }
+        if (COULOMB) {
+            const double vc = qi * pj.w * rinv;
+            v += vc;
+            fr += vc * rinv;
+        }
+        if (r > rsw) {
+            const double u = (r - rsw) / wsw;
+            const double u2 = u * u;
+            const double sw = 1.0 - 10.0 * u2 * u + 15.0 * u2 * u2 - 6.0 * u2 * u2 * u;
+            const double dsw = -30.0 * u2 * (1.0 - u) * (1.0 - u) / wsw;
+            fr = fr * sw - v * dsw;
+            v *= sw;
+        }
+        const double g = fr * rinv;
+        fx -= g * dx;
+        fy -= g * dy;
+        fz -= g * dz;
+        eacc += v;
+    }
+    unsigned int bad = 0;
+    if (valid) {
+        const int a = perm[s];
+        gm_atomic_fix_add(force + a, gm_to_fix_checked(fx, bad));
+        gm_atomic_fix_add(force + n + a, gm_to_fix_checked(fy, bad));
+        gm_atomic_fix_add(force + 2 * n + a, gm_to_fix_checked(fz, bad));
+    }
+    for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
+    if (lane == 0) epart[group] = 0.5 * eacc;
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && lane == 0) atomicOr(&st->error, bad);
+}
+
+// ----------------------------------------------------------------- bonded
+
+template <typename T>
+struct V3 { T x, y, z; };
+
+template <typename T>
+__device__ __forceinline__ V3<T> diff(const double *pos, int n, int a, int b) {
+    // pos[a] - pos[b], differenced in FP64 before any narrowing
+    return {(T)(pos[a] - pos[b]), (T)(pos[n + a] - pos[n + b]), (T)(pos[2 * n + a] - pos[2 * n + b])};
+}
+template <typename T>
+__device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename T>
+__device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+template <typename T>
+__device__ __forceinline__ void add_force(long long *f, int n, int a, T x, T y, T z, unsigned &bad) {
+    gm_atomic_fix_add(f + a, gm_to_fix_checked(x, bad));
+    gm_atomic_fix_add(f + n + a, gm_to_fix_checked(y, bad));
+    gm_atomic_fix_add(f + 2 * n + a, gm_to_fix_checked(z, bad));
+}
+
+__device__ __forceinline__ float gm_acos(float x) { return acosf(x); }
+__device__ __forceinline__ double gm_acos(double x) { return acos(x); }
+__device__ __forceinline__ float gm_atan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double gm_atan2(double y, double x) { return atan2(y, x); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    double e = 0.0;
+    unsigned bad = 0;
+    if (t < a.n_bonds) {
+        // force/bonded.rs:5-40, V = k (r - r0)^2
+        const int i = a.bond_i[t], j = a.bond_j[t];
+        const double dx64 = a.pos[j] - a.pos[i], dy64 = a.pos[n + j] - a.pos[n + i], dz64 = a.pos[2 * n + j] - a.pos[2 * n + i];
+        const double k = a.bond_k[t], r0 = a.bond_r0[t];
+        const double r2 = dx64 * dx64 + dy64 * dy64 + dz64 * dz64;
+        if (r2 > 0.0) {
+            T r, dr;
+            if (sizeof(T) == 4) {
+                // r - r0 = (r^2 - r0^2) / (r + r0) keeps the stretch accurate in FP32
+                r = sqrtf((float)r2);
+                dr = (T)(r2 - r0 * r0) / (r + (T)r0);
+            } else {
+                r = (T)sqrt(r2);
+                dr = r - (T)r0;
+            }
+            const T dv_dr = (T)2 * (T)k * dr;
+            e = (double)((T)k * dr * dr);
+            const T g = dv_dr / r;
+            const T fx = g * (T)dx64, fy = g * (T)dy64, fz = g * (T)dz64;
+            add_force<T>(a.force, n, i, fx, fy, fz, bad);
+            add_force<T>(a.force, n, j, -fx, -fy, -fz, bad);
+        }
+    } else if (t < a.n_bonds + a.n_angles) {
+        // force/bonded.rs:44-102, V = k (theta - theta0)^2
+        const int q = t - a.n_bonds;
+        const int i = a.angle_i[q], j = a.angle_j[q], kk = a.angle_k[q];
+        const V3<T> b1 = diff<T>(a.pos, n, i, j), b2 = diff<T>(a.pos, n, kk, j);
+        const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
+        if (r1 != (T)0 && r2 != (T)0) {
+            T c = dot(b1, b2) / (r1 * r2);
+            c = c < (T)-1 ? (T)-1 : (c > (T)1 ? (T)1 : c);
+            T sn = sqrt((T)1 - c * c);
+            sn = sn > (T)1e-8 ? sn : (T)1e-8;
+            const T th = gm_acos(c);
+            const T k = (T)a.angle_kth[q], th0 = (T)a.angle_th0[q];
+            e = (double)(k * (th - th0) * (th - th0));
+            const T aa = (T)2 * k * (th - th0) / sn;
+            const T ir12 = (T)1 / (r1 * r2), ir11 = (T)1 / (r1 * r1), ir22 = (T)1 / (r2 * r2);
+            const V3<T> fi = {aa * (b2.x * ir12 - c * b1.x * ir11), aa * (b2.y * ir12 - c * b1.y * ir11),
+                              aa * (b2.z * ir12 - c * b1.z * ir11)};
+            const V3<T> fk = {aa * (b1.x * ir12 - c * b2.x * ir22), aa * (b1.y * ir12 - c * b2.y * ir22),
+                              aa * (b1.z * ir12 - c * b2.z * ir22)};
+            add_force<T>(a.force, n, i, fi.x, fi.y, fi.z, bad);
+            add_force<T>(a.force, n, kk, fk.x, fk.y, fk.z, bad);
+            add_force<T>(a.force, n, j, -(fi.x + fk.x), -(fi.y + fk.y), -(fi.z + fk.z), bad);
+        }
+    } else if (t < a.n_bonds + a.n_angles + a.n_diheds) {
+        // force/bonded.rs:112-164, V = k [1 + cos(n phi - delta)]
+        const int q = t - a.n_bonds - a.n_angles;
+        const int i = a.dihed_i[q], j = a.dihed_j[q], k = a.dihed_k[q], l = a.dihed_l[q];
+        const V3<T> b1 = diff<T>(a.pos, n, j, i), b2 = diff<T>(a.pos, n, k, j), b3 = diff<T>(a.pos, n, l, k);
+        const V3<T> m = cross(b1, b2), nv = cross(b2, b3);
+        const T m2 = dot(m, m), n2 = dot(nv, nv), b2l = sqrt(dot(b2, b2));
+        if (m2 != (T)0 && n2 != (T)0 && b2l != (T)0) {
+            const T x = dot(m, nv);
+            const T y = dot(cross(m, nv), b2) / b2l;
+            const T phi = gm_atan2(y, x);
+            const T kphi = (T)a.dihed_kphi[q], mult = (T)a.dihed_n[q], delta = (T)a.dihed_delta[q];
+            const T arg = mult * phi - delta;
+            e = (double)(kphi * ((T)1 + cos(arg)));
+            const T dv = kphi * mult * sin(arg);  // -dV/dphi
+            const T si = -dv * b2l / m2, sl = dv * b2l / n2;
+            const V3<T> fi = {m.x * si, m.y * si, m.z * si}, fl = {nv.x * sl, nv.y * sl, nv.z * sl};
+            const T ib = (T)1 / (b2l * b2l);
+            const T p = dot(b1, b2) * ib, qq = dot(b3, b2) * ib;
+            const V3<T> fj = {-(p + (T)1) * fi.x + qq * fl.x, -(p + (T)1) * fi.y + qq * fl.y, -(p + (T)1) * fi.z + qq * fl.z};
+            const V3<T> fk = {p * fi.x - (qq + (T)1) * fl.x, p * fi.y - (qq + (T)1) * fl.y, p * fi.z - (qq + (T)1) * fl.z};
+            add_force<T>(a.force, n, i, fi.x, fi.y, fi.z, bad);
+            add_force<T>(a.force, n, j, fj.x, fj.y, fj.z, bad);
+            add_force<T>(a.force, n, k, fk.x, fk.y, fk.z, bad);
+            add_force<T>(a.force, n, l, fl.x, fl.y, fl.z, bad);
+        }
+    }
+    // fixed-order block reduction of the energy
+    __shared__ double se[256];
+    se[threadIdx.x] = e;
+    __syncthreads();
+    for (int s2 = 128; s2 > 0; s2 >>= 1) {
+        if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.epart_bonded[blockIdx.x] = se[0];
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
+}
+
+// Scaled 1-4 pairs (beyond the reference): unswitched, no cutoff; LJ scaled by
+// scale14_lj, Coulomb by scale14_coul.  FP64 arithmetic, few pairs.
+__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = a.n;
+    double e = 0.0;
+    unsigned bad = 0;
+    if (t < a.n14) {
+        const int i = a.p14_i[t], j = a.p14_j[t];
+        const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 > 0.0) {
+            const double r = sqrt(r2), rinv = 1.0 / r;
+            double v = 0.0, fr = 0.0;
+            const double sg = 0.5 * (a.sigma[i] + a.sigma[j]), ep = sqrt(a.epsilon[i] * a.epsilon[j]);
+            if (a.scale14_lj != 0.0 && ep != 0.0) {
+                const double sr = sg * rinv, s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
+                v += a.scale14_lj * (4.0 * ep * (s12 - s6));
+                fr += a.scale14_lj * (24.0 * ep * rinv * (2.0 * s12 - s6));
+            }
+            if (a.coulomb && a.scale14_coul != 0.0) {
+                const double qq = kCoulomb64 * a.charge64[i] * a.charge64[j];
+                v += a.scale14_coul * qq * rinv;
+                fr += a.scale14_coul * qq * rinv * rinv;
+            }
+            e = v;
+            const double g = fr * rinv;
+            add_force<double>(a.force, n, i, -g * dx, -g * dy, -g * dz, bad);
+            add_force<double>(a.force, n, j, g * dx, g * dy, g * dz, bad);
+        }
+    }
+    __shared__ double se[256];
+    se[threadIdx.x] = e;
+    __syncthreads();
+    for (int s2 = 128; s2 > 0; s2 >>= 1) {
+        if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.epart14[blockIdx.x] = se[0];
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
+}
+
+// Fixed-order sum of all energy partials (pair groups, bonded blocks, 1-4
+// blocks) into the FP64 total: deterministic for a given launch shape.
+__global__ void __launch_bounds__(1024) energy_kernel(const double *epart, int n, double *out) {
+    __shared__ double s[1024];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += epart[i];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = 512; k > 0; k >>= 1) {
+        if (threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+}  // namespace
+
+int gm_bonded_blocks(int nb, int na, int nd) {
+    const long long t = (long long)nb + na + nd;
+    return (int)((t + 255) / 256);
+}
+
+void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int blocks = (a.n_groups + kPairWarps - 1) / kPairWarps;
+    if (!fp64) {
+        const size_t smem = sizeof(float2) * (size_t)a.ntypes * a.ntypes;
+#define GM_PAIR32(P, Q)                                                                                   \
+    pair_kernel_f32<P, Q><<<blocks, kPairWarps * 32, smem, s>>>(                                          \
+        a.n, a.cap, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, a.inv_wsw, \
+        a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status)
+        if (a.periodic) { if (a.coulomb) GM_PAIR32(true, true); else GM_PAIR32(true, false); }
+        else { if (a.coulomb) GM_PAIR32(false, true); else GM_PAIR32(false, false); }
+#undef GM_PAIR32
+    } else {
+        const size_t smem = sizeof(double2) * (size_t)a.ntypes * a.ntypes;
+#define GM_PAIR64(P, Q)                                                                                        \
+    pair_kernel_f64<P, Q><<<blocks, kPairWarps * 32, smem, s>>>(                                               \
+        a.n, a.cap, a.pos64s, a.type_sorted, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab64, a.rc2_64,     \
+        a.rsw_64, a.rc_64, a.box64[0], a.box64[1], a.box64[2], a.force, a.epart, a.status)
+        if (a.periodic) { if (a.coulomb) GM_PAIR64(true, true); else GM_PAIR64(true, false); }
+        else { if (a.coulomb) GM_PAIR64(false, true); else GM_PAIR64(false, false); }
+#undef GM_PAIR64
+    }
+}
+
+void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s) {
+    if (a.bonded_blocks == 0) return;
+    if (fp64) bonded_kernel<double><<<a.bonded_blocks, 256, 0, s>>>(a);
+    else bonded_kernel<float><<<a.bonded_blocks, 256, 0, s>>>(a);
+}
+
+void gm_launch_pair14(const ForceArgs &a, cudaStream_t s) {
+    if (a.blocks14 == 0) return;
+    pair14_kernel<<<a.blocks14, 256, 0, s>>>(a);
+}
+
+void gm_launch_energy(const ForceArgs &a, cudaStream_t s) {
+    energy_kernel<<<1, 1024, 0, s>>>(a.epart, a.n_epart_total, a.energy);
+}

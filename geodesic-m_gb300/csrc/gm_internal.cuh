@@ -1,0 +1,203 @@
+// gm_internal.cuh — definitions shared by the CUDA translation units of the
+// GB300 backend: fixed-point force format, device status word, cell-grid
+// description and the launchers each kernel file exports.
+//
+// Data layout in HBM (one system, N atoms):
+//   * FP64 state in the caller's atom order: pos/vel/ref as x|y|z rows of N.
+//   * int64 fixed-point force accumulators F (x|y|z rows, caller order),
+//     value = F * 2^-40 kcal/mol/A.  Integer sums are associative, so
+//     atomics from any thread order give bit-identical totals.
+//   * Cell-sorted copies for the pair kernel: perm[s] = caller index of
+//     sorted slot s; hi[s] = (float(x-o), float(y-o), float(z-o), type bits),
+//     lo[s] = (float residues of the same, charge) so hi+lo carries each
+//     coordinate to ~2^-48 relative; FP64 mode keeps a sorted double4 copy.
+//   * Full (symmetric) neighbour list in warp-interleaved columns: the 32
+//     atoms of group g own a slab of 32*cap ints; entry e of lane l sits at
+//     g*32*cap + e*32 + l, so one list row is a 128-byte coalesced load.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "geodesic_cuda.h"
+
+#define GM_FIX_SCALE 1099511627776.0        // 2^40
+#define GM_FIX_INV (1.0 / 1099511627776.0)  // 2^-40
+#define GM_FIX_SCALE_F 1099511627776.0f
+#define GM_FIX_LIMIT 4194304.0              // 2^22: |contribution| must stay below
+
+// Ceiling on distinct (sigma, epsilon) parameter pairs: the pair table lives
+// in shared memory (64 x 64 x 8 B = 32 KB).
+#define GM_MAX_TYPES 64
+#define GM_WARP 32
+
+// Device status bits (DevStatus::error).
+enum : unsigned int {
+    GM_DEV_NONFINITE_POS = 1u << 0,
+    GM_DEV_NONFINITE_FORCE = 1u << 1,
+    GM_DEV_FIX_OVERFLOW = 1u << 2,
+    GM_DEV_LIST_OVERFLOW = 1u << 3,
+    GM_DEV_SHAKE_FAIL = 1u << 4,
+    GM_DEV_RATTLE_FAIL = 1u << 5,
+    GM_DEV_EXTENT = 1u << 6,       // non-periodic extent too large for min-image
+    GM_DEV_CELL_OVERFLOW = 1u << 7,
+    GM_DEV_ITER_MISMATCH = 1u << 8,
+};
+
+struct DevStatus {
+    unsigned int error;
+    unsigned int rebuild;          // 1 when the list must be rebuilt
+    unsigned int blocks_done;      // last-block-done counter of the rebuild check
+    unsigned int shake_T;          // iteration count of the last SHAKE call
+    unsigned int rattle_T;
+    unsigned int pad0;
+    unsigned long long n_rebuilds;
+    unsigned long long step;       // current step of the resident loop
+    unsigned long long fail_step;  // first step whose projection failed (init ~0)
+};
+
+struct GridInfo {
+    double origin[3];   // coordinate origin of the float copies
+    float lo[3];        // grid lower corner, origin-relative
+    float inv_w[3];     // 1 / cell width
+    float box[3], inv_box[3];
+    int nc[3];
+    int ncell;
+    int periodic;
+    int full[3];        // scan the whole dimension (periodic, fewer than 5 cells)
+};
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ long long gm_to_fix(double v) { return __double2ll_rn(v * GM_FIX_SCALE); }
+
+// A float force contribution to fixed point; flags non-finite / overflow.
+__device__ __forceinline__ long long gm_to_fix_checked(float v, unsigned int &bad) {
+    if (!isfinite(v)) bad |= GM_DEV_NONFINITE_FORCE;
+    else if (fabsf(v) >= (float)GM_FIX_LIMIT) bad |= GM_DEV_FIX_OVERFLOW;
+    return __float2ll_rn(v * GM_FIX_SCALE_F);
+}
+__device__ __forceinline__ long long gm_to_fix_checked(double v, unsigned int &bad) {
+    if (!isfinite(v)) bad |= GM_DEV_NONFINITE_FORCE;
+    else if (fabs(v) >= GM_FIX_LIMIT) bad |= GM_DEV_FIX_OVERFLOW;
+    return __double2ll_rn(v * GM_FIX_SCALE);
+}
+
+__device__ __forceinline__ void gm_atomic_fix_add(long long *p, long long v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
+}
+
+// ------------------------------------------------------- launcher exports
+
+struct ListArgs {
+    int n;
+    int cap;                 // list entries per atom
+    const double *pos;       // FP64 x|y|z, caller order
+    float4 *hi, *lo;         // sorted
+    double4 *pos64s;         // sorted FP64 copy (FP64 mode) or nullptr
+    int *type_sorted;        // sorted types (FP64 mode)
+    int *perm;               // sorted -> caller
+    int *cell_of;            // caller order
+    int *cell_sorted;        // sorted
+    int *cell_count, *cell_start, *cell_cursor;
+    int *tmp_slot;           // caller -> unsorted slot
+    int *tmp_atom;           // unsorted slot -> caller
+    int max_cells;
+    const int *type;         // caller order
+    const float *charge;     // caller order
+    const double *charge64;  // caller order (FP64 mode)
+    const int *excl_start, *excl;   // caller-order CSR (both directions, sorted)
+    int *list, *count, *gmax;
+    double *ref;             // FP64 x|y|z copy at the build
+    long long *force;        // zeroed with the pack
+    GridInfo *grid;
+    DevStatus *status;
+    double r_list, box[3];
+    int periodic;
+    double *bbox_scratch;    // 6 * blocks
+    int bbox_blocks;
+};
+
+void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s);
+void gm_launch_grid(const ListArgs &a, cudaStream_t s);
+void gm_launch_bin(const ListArgs &a, cudaStream_t s);
+void gm_launch_build(const ListArgs &a, cudaStream_t s);
+void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s);
+
+struct ForceArgs {
+    int n, n_groups, cap;
+    const float4 *hi, *lo;
+    const double4 *pos64s;
+    const int *type_sorted;  // FP64 mode
+    const int *perm;
+    const int *list, *count, *gmax;
+    int ntypes;
+    const float2 *tab32;     // (sigma_ij^2, epsilon_ij) per type pair
+    const double2 *tab64;    // (sigma_ij, epsilon_ij)
+    float rc2, rsw, rc, inv_wsw;
+    double rc2_64, rsw_64, rc_64, inv_wsw_64;
+    int coulomb;
+    float box[3], inv_box[3];
+    double box64[3];
+    int periodic;
+    long long *force;
+    double *epart;           // per group
+    DevStatus *status;
+    const double *pos;       // caller order FP64 (bonded)
+    // bonded, caller order
+    int n_bonds, n_angles, n_diheds;
+    const int *bond_i, *bond_j; const double *bond_k, *bond_r0;
+    const int *angle_i, *angle_j, *angle_k; const double *angle_kth, *angle_th0;
+    const int *dihed_i, *dihed_j, *dihed_k, *dihed_l; const double *dihed_kphi; const int *dihed_n;
+    const double *dihed_delta;
+    double *epart_bonded;    // per block
+    int bonded_blocks;
+    // scaled 1-4 pairs
+    int n14; const int *p14_i, *p14_j; double scale14_lj, scale14_coul;
+    const double *sigma, *epsilon, *charge64;
+    double *epart14; int blocks14;
+    double *energy;          // total
+    int n_epart_total;       // epart has n_groups + bonded_blocks + blocks14 entries
+};
+
+void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s);
+void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s);
+void gm_launch_pair14(const ForceArgs &a, cudaStream_t s);
+void gm_launch_energy(const ForceArgs &a, cudaStream_t s);
+int gm_bonded_blocks(int n_bonds, int n_angles, int n_diheds);
+
+struct ClusterArgs {
+    int n_clusters;
+    const int *cl_cstart, *cl_cons;       // cluster -> constraints (ascending)
+    const int *cl_astart, *cl_atoms;      // cluster -> atoms
+    const int *cl_acstart, *cl_acons;     // cluster-atom slot -> signed constraint refs (ascending)
+    const int *constr_i, *constr_j;
+    const double *constr_dsq;
+    const double *inv_mass;               // 1.0 / mass (caller order)
+    double *lam;                          // per constraint scratch
+    double *rvec;                         // per constraint reference vector (3 x C)
+    int *cl_iters;                        // per cluster iteration count
+    double *cl_worst;                     // per cluster last max |lambda|
+    int *cl_worst_idx;                    // per cluster constraint of that max
+    int n_constr;
+    unsigned int max_iter;
+    double tol;
+    DevStatus *status;
+};
+
+void gm_launch_half_kick(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                         const DevStatus *st, cudaStream_t s);
+void gm_launch_half_kick_f64(int n, double *vel, const double *force, const double *inv_mass, double dt_half,
+                             cudaStream_t s);
+void gm_launch_drift(int n, double *pos, double *vel, double *dref, double dt, bool resync, const DevStatus *st,
+                     cudaStream_t s);
+void gm_launch_resync(int n, const double *pos, double *vel, const double *dref, double dt, const DevStatus *st,
+                      cudaStream_t s);
+void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
+                     unsigned long long cond_handle, int blocks, cudaStream_t s);
+void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, double *pos, cudaStream_t s);
+void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s);
+void gm_launch_step(DevStatus *st, cudaStream_t s);
+void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,
+                       cudaStream_t s);
+void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s);
+int gm_check_blocks(int n);

@@ -1,0 +1,408 @@
+// gm_list.cu — Verlet list build on the device (neighbor.rs:8-55 semantics).
+//
+// Pipeline at each rebuild (all on the context's stream, no host sync):
+//   wrap (periodic only) -> bbox partials -> grid setup -> cell assignment +
+//   counting-sort histogram -> scan -> scatter -> in-cell rank by caller
+//   index (deterministic order) -> pack -> list build.
+// The list build gives each warp 32 consecutive cell-sorted atoms; the warp
+// streams every candidate in the union of their 5x5x5 half-cell stencils
+// through shared memory and each lane tests it against its own atom.  The
+// test runs in FP32 on hi+lo coordinates; candidates within `margin` of the
+// list radius are re-decided with the reference's exact FP64 expression
+// (min-image, then dx*dx + dy*dy + dz*dz, no fused multiply-add), so the pair
+// set equals the reference's bit for bit.
+#include <cfloat>
+
+#include "gm_internal.cuh"
+
+namespace {
+
+constexpr int kBuildWarps = 4;
+
+__device__ __forceinline__ double exact_min_image(double d, double L) {
+    // neighbor.rs:74-76: d - L * round(d / L), no contraction
+    return __dsub_rn(d, __dmul_rn(L, round(__ddiv_rn(d, L))));
+}
+
+__device__ __forceinline__ double exact_wrap(double x, double L) {
+    // neighbor.rs:86-88: x - L * floor(x / L)
+    return __dsub_rn(x, __dmul_rn(L, floor(__ddiv_rn(x, L))));
+}
+
+__global__ void wrap_kernel(int n, double *pos, double b0, double b1, double b2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pos[i] = exact_wrap(pos[i], b0);
+    pos[n + i] = exact_wrap(pos[n + i], b1);
+    pos[2 * n + i] = exact_wrap(pos[2 * n + i], b2);
+}
+
+__global__ void bbox_kernel(int n, const double *pos, double *partial) {
+    // per block: min x,y,z then max x,y,z
+    __shared__ double sm[6][256];
+    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int d = 0; d < 3; d++) {
+            double v = pos[d * n + i];
+            mn[d] = fmin(mn[d], v);
+            mx[d] = fmax(mx[d], v);
+        }
+    }
+    for (int d = 0; d < 3; d++) { sm[d][threadIdx.x] = mn[d]; sm[3 + d][threadIdx.x] = mx[d]; }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int d = 0; d < 3; d++) {
+                sm[d][threadIdx.x] = fmin(sm[d][threadIdx.x], sm[d][threadIdx.x + s]);
+                sm[3 + d][threadIdx.x] = fmax(sm[3 + d][threadIdx.x], sm[3 + d][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+__global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevStatus *st, double r_list,
+                            double b0, double b1, double b2, int periodic, int max_cells) {
+    if (threadIdx.x != 0) return;
+    const double box[3] = {b0, b1, b2};
+    const double wmin = r_list * 0.5 * (1.0 + 1e-5) + 1e-6;
+    int nc[3];
+    double w[3], lo[3];
+    g->periodic = periodic;
+    for (int d = 0; d < 3; d++) {
+        g->box[d] = (float)box[d];
+        g->inv_box[d] = (float)(1.0 / box[d]);
+    }
+    if (periodic) {
+        for (int d = 0; d < 3; d++) {
+            nc[d] = (int)floor(box[d] / wmin);
+            if (nc[d] < 1) nc[d] = 1;
+            g->origin[d] = 0.5 * box[d];
+            lo[d] = -0.5 * box[d];
+        }
+    } else {
+        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        for (int b = 0; b < blocks; b++)
+            for (int d = 0; d < 3; d++) {
+                mn[d] = fmin(mn[d], partial[b * 6 + d]);
+                mx[d] = fmax(mx[d], partial[b * 6 + 3 + d]);
+            }
+        for (int d = 0; d < 3; d++) {
+            double ext = mx[d] - mn[d];
+            if (!(ext == ext) || mx[d] < mn[d]) { ext = 0.0; mn[d] = mx[d] = 0.0; }
+            // min-image of the reference folds pairs farther apart than box/2;
+            // the cell search assumes it never does
+            if (ext + r_list >= 0.5 * box[d]) atomicOr(&st->error, (unsigned)GM_DEV_EXTENT);
+            const double pad = 1e-3 * (1.0 + ext);
+            g->origin[d] = 0.5 * (mx[d] + mn[d]);
+            lo[d] = (mn[d] - g->origin[d]) - pad;
+            double span = ext + 2.0 * pad;
+            nc[d] = (int)floor(span / wmin);
+            if (nc[d] < 1) nc[d] = 1;
+        }
+        // keep the cell count within the allocation by coarsening the grid
+        while ((long long)nc[0] * nc[1] * nc[2] > max_cells) {
+            for (int d = 0; d < 3; d++) nc[d] = nc[d] > 1 ? (nc[d] * 3) / 4 : 1;
+        }
+    }
+    for (int d = 0; d < 3; d++) {
+        double span = periodic ? box[d] : -2.0 * lo[d];
+        w[d] = span / nc[d];
+        g->nc[d] = nc[d];
+        g->lo[d] = (float)lo[d];
+        g->inv_w[d] = (float)(1.0 / w[d]);
+        g->full[d] = periodic && nc[d] < 5;
+    }
+    g->ncell = nc[0] * nc[1] * nc[2];
+    if (g->ncell > max_cells) atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+    st->rebuild = 0;
+    st->n_rebuilds += 1;
+}
+
+__device__ __forceinline__ int cell_coord(float h, float lo, float inv_w, int nc) {
+    float t = floorf((h - lo) * inv_w);
+    int c = (int)t;  // NaN converts to 0
+    return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+__global__ void assign_kernel(int n, const double *pos, double *ref, const GridInfo *g, int *cell_of,
+                              int *cell_count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c3[3];
+    for (int d = 0; d < 3; d++) {
+        double x = pos[d * n + i];
+        ref[d * n + i] = x;  // NeighborList::ref_{x,y,z} (neighbor.rs:48-50)
+        c3[d] = cell_coord((float)(x - g->origin[d]), g->lo[d], g->inv_w[d], g->nc[d]);
+    }
+    int c = (c3[2] * g->nc[1] + c3[1]) * g->nc[0] + c3[0];
+    cell_of[i] = c;
+    atomicAdd(&cell_count[c], 1);
+}
+
+// Exclusive scan of cell_count[0..ncell) into cell_start[0..ncell] (one block).
+__global__ void scan_kernel(const GridInfo *g, const int *cell_count, int *cell_start) {
+    __shared__ int warp_sums[32];
+    __shared__ int carry;
+    const int ncell = g->ncell;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ncell; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = i < ncell ? cell_count[i] : 0;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int nw = blockDim.x >> 5;
+            int s = lane < nw ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        int excl = x - v + (w > 0 ? warp_sums[w - 1] : 0) + carry;
+        if (i < ncell) cell_start[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cell_start[ncell] = carry;
+}
+
+__global__ void scatter_kernel(int n, const int *cell_of, const int *cell_start, int *cell_cursor, int *tmp_atom) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = cell_of[i];
+    int slot = cell_start[c] + atomicAdd(&cell_cursor[c], 1);
+    tmp_atom[slot] = i;
+}
+
+// Within a cell, atoms are ordered by caller index: the rank of an atom is
+// the number of cell members with a smaller index.  Independent of the
+// atomic order of the scatter, so the sorted layout is deterministic.
+__global__ void rank_kernel(int n, const int *cell_of, const int *cell_start, const int *tmp_atom, int *perm,
+                            int *cell_sorted, DevStatus *st) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int a = tmp_atom[k];
+    int c = cell_of[a];
+    int s0 = cell_start[c], s1 = cell_start[c + 1];
+    if (s1 - s0 > 65536) {
+        // no physical system packs this many atoms into one half cell; keep
+        // the quadratic rank bounded and report it
+        atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+        perm[k] = a;
+        cell_sorted[k] = c;
+        return;
+    }
+    int rank = 0;
+    for (int m = s0; m < s1; m++) rank += tmp_atom[m] < a;
+    perm[s0 + rank] = a;
+    cell_sorted[s0 + rank] = c;
+}
+
+__global__ void pack_kernel(int n, const double *pos, const int *perm, const int *type, const float *charge,
+                            const GridInfo *g, float4 *hi, float4 *lo, double4 *pos64s, int *type_sorted,
+                            const double *charge64, long long *force) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int a = perm[s];
+    double x = pos[a], y = pos[n + a], z = pos[2 * n + a];
+    double dx = x - g->origin[0], dy = y - g->origin[1], dz = z - g->origin[2];
+    float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+    hi[s] = make_float4(hx, hy, hz, __int_as_float(type[a]));
+    lo[s] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), charge[a]);
+    if (pos64s) {
+        pos64s[s] = make_double4(x, y, z, charge64[a]);
+        type_sorted[s] = type[a];
+    }
+    force[a] = 0;
+    force[n + a] = 0;
+    force[2 * n + a] = 0;
+}
+
+struct Range { int lo, hi, nc, wrap; };
+
+__device__ __forceinline__ Range dim_range(int mn, int mx, int nc, int periodic, int full) {
+    Range r;
+    r.nc = nc;
+    if (full) { r.lo = 0; r.hi = nc - 1; r.wrap = 0; return r; }
+    r.lo = mn - 2;
+    r.hi = mx + 2;
+    if (periodic) {
+        if (r.hi - r.lo + 1 >= nc) { r.lo = 0; r.hi = nc - 1; r.wrap = 0; }
+        else r.wrap = 1;
+    } else {
+        r.lo = r.lo < 0 ? 0 : r.lo;
+        r.hi = r.hi >= nc ? nc - 1 : r.hi;
+        r.wrap = 0;
+    }
+    return r;
+}
+
+__device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c >= nc ? c - nc : c); }
+
+__global__ void __launch_bounds__(kBuildWarps * 32)
+build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+             const int *__restrict__ perm, const int *__restrict__ cell_sorted, const int *__restrict__ cell_start,
+             const GridInfo *__restrict__ gp, const double *__restrict__ pos, const int *__restrict__ excl_start,
+             const int *__restrict__ excl, int *__restrict__ list, int *__restrict__ count, int *__restrict__ gmax,
+             DevStatus *st, float rl2_lo, float rl2_hi, double rl2_64, double b0, double b1, double b2) {
+    __shared__ float4 s_hi[kBuildWarps][32];
+    __shared__ float4 s_lo[kBuildWarps][32];
+    __shared__ int s_orig[kBuildWarps][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int group = blockIdx.x * kBuildWarps + wib;
+    const int s = group * 32 + lane;
+    if (group * 32 >= n) return;
+    const bool valid = s < n;
+    const GridInfo g = *gp;
+    float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
+    int my_orig = -1, my_cell = 0;
+    if (valid) {
+        mh = hi[s];
+        ml = lo[s];
+        my_orig = perm[s];
+        my_cell = cell_sorted[s];
+    }
+    // own exclusions (caller indices, ascending); up to 8 kept in registers
+    int e0 = 0, e1 = 0;
+    int ex[8];
+    if (valid) { e0 = excl_start[my_orig]; e1 = excl_start[my_orig + 1]; }
+    const int ne = e1 - e0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) ex[k] = (k < ne) ? excl[e0 + k] : -1;
+    // group cell box
+    int cx = my_cell % g.nc[0], cy = (my_cell / g.nc[0]) % g.nc[1], cz = my_cell / (g.nc[0] * g.nc[1]);
+    int mn[3] = {valid ? cx : INT_MAX, valid ? cy : INT_MAX, valid ? cz : INT_MAX};
+    int mx[3] = {valid ? cx : INT_MIN, valid ? cy : INT_MIN, valid ? cz : INT_MIN};
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+    Range rx = dim_range(mn[0], mx[0], g.nc[0], g.periodic, g.full[0]);
+    Range ry = dim_range(mn[1], mx[1], g.nc[1], g.periodic, g.full[1]);
+    Range rz = dim_range(mn[2], mx[2], g.nc[2], g.periodic, g.full[2]);
+    int *my_list = list + (size_t)group * 32 * cap + lane;
+    int cnt = 0;
+    const double bx[3] = {b0, b1, b2};
+    for (int zz = rz.lo; zz <= rz.hi; zz++) {
+        const int z = rz.wrap ? wrapi(zz, g.nc[2]) : zz;
+        for (int yy = ry.lo; yy <= ry.hi; yy++) {
+            const int y = ry.wrap ? wrapi(yy, g.nc[1]) : yy;
+            // the x extent as one or two runs of consecutive cells
+            int seg_lo[2], seg_hi[2], nseg;
+            if (!rx.wrap) { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
+            else if (rx.lo < 0) { seg_lo[0] = rx.lo + g.nc[0]; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi; nseg = 2; }
+            else if (rx.hi >= g.nc[0]) { seg_lo[0] = rx.lo; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi - g.nc[0]; nseg = 2; }
+            else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
+            for (int sg = 0; sg < nseg; sg++) {
+                const int row = (z * g.nc[1] + y) * g.nc[0];
+                const int a0 = cell_start[row + seg_lo[sg]], a1 = cell_start[row + seg_hi[sg] + 1];
+                for (int base = a0; base < a1; base += 32) {
+                    const int t = base + lane;
+                    __syncwarp();
+                    if (t < a1) {
+                        s_hi[wib][lane] = hi[t];
+                        s_lo[wib][lane] = lo[t];
+                        s_orig[wib][lane] = perm[t];
+                    }
+                    __syncwarp();
+                    const int m = min(32, a1 - base);
+                    for (int k = 0; k < m; k++) {
+                        const int j = base + k;
+                        if (!valid || j == s) continue;
+                        const float4 ch = s_hi[wib][k], cl = s_lo[wib][k];
+                        float dx = (ch.x - mh.x) + (cl.x - ml.x);
+                        float dy = (ch.y - mh.y) + (cl.y - ml.y);
+                        float dz = (ch.z - mh.z) + (cl.z - ml.z);
+                        if (g.periodic) {
+                            dx -= g.box[0] * rintf(dx * g.inv_box[0]);
+                            dy -= g.box[1] * rintf(dy * g.inv_box[1]);
+                            dz -= g.box[2] * rintf(dz * g.inv_box[2]);
+                        }
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 > rl2_hi) continue;
+                        const int jo = s_orig[wib][k];
+                        bool in = r2 <= rl2_lo;
+                        if (!in) {
+                            // the reference's own FP64 decision
+                            double ex_ = exact_min_image(__dsub_rn(pos[jo], pos[my_orig]), bx[0]);
+                            double ey_ = exact_min_image(__dsub_rn(pos[n + jo], pos[n + my_orig]), bx[1]);
+                            double ez_ = exact_min_image(__dsub_rn(pos[2 * n + jo], pos[2 * n + my_orig]), bx[2]);
+                            double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
+                            in = rr <= rl2_64;
+                        }
+                        if (!in) continue;
+                        bool excluded = false;
+#pragma unroll
+                        for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
+                        if (ne > 8)
+                            for (int q = e0 + 8; q < e1; q++) excluded |= (excl[q] == jo);
+                        if (excluded) continue;
+                        if (cnt < cap) my_list[(size_t)cnt * 32] = j;
+                        cnt++;
+                    }
+                }
+            }
+        }
+    }
+    if (valid) {
+        count[s] = cnt < cap ? cnt : cap;
+        if (cnt > cap) atomicOr(&st->error, (unsigned)GM_DEV_LIST_OVERFLOW);
+    }
+    int c = valid ? (cnt < cap ? cnt : cap) : 0;
+    for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
+    if (lane == 0) gmax[group] = c;
+}
+
+}  // namespace
+
+void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s) {
+    if (!a.periodic || a.n == 0) return;
+    wrap_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.n, pos, a.box[0], a.box[1], a.box[2]);
+}
+
+void gm_launch_grid(const ListArgs &a, cudaStream_t s) {
+    if (!a.periodic && a.n > 0) bbox_kernel<<<a.bbox_blocks, 256, 0, s>>>(a.n, a.pos, a.bbox_scratch);
+    grid_kernel<<<1, 32, 0, s>>>(a.bbox_scratch, a.periodic || a.n == 0 ? 0 : a.bbox_blocks, a.grid, a.status,
+                                 a.r_list, a.box[0], a.box[1], a.box[2], a.periodic, a.max_cells);
+}
+
+void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
+    cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)a.max_cells, s);
+    cudaMemsetAsync(a.cell_cursor, 0, sizeof(int) * (size_t)a.max_cells, s);
+    const int nb = (a.n + 255) / 256;
+    if (a.n > 0) assign_kernel<<<nb, 256, 0, s>>>(a.n, a.pos, a.ref, a.grid, a.cell_of, a.cell_count);
+    scan_kernel<<<1, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start);
+    if (a.n > 0) {
+        scatter_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.cell_cursor, a.tmp_atom);
+        rank_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.tmp_atom, a.perm, a.cell_sorted, a.status);
+    }
+}
+
+void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s) {
+    if (a.n == 0) return;
+    pack_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.n, a.pos, a.perm, a.type, a.charge, a.grid, a.hi, a.lo,
+                                                   fp64 ? a.pos64s : nullptr, a.type_sorted, a.charge64, a.force);
+}
+
+void gm_launch_build(const ListArgs &a, cudaStream_t s) {
+    if (a.n == 0) return;
+    const int groups = (a.n + 31) / 32;
+    const double rl2 = a.r_list * a.r_list;  // neighbor.rs:25
+    const double margin = 1e-3 * (rl2 > 144.0 ? rl2 / 144.0 : 1.0);
+    build_kernel<<<(groups + kBuildWarps - 1) / kBuildWarps, kBuildWarps * 32, 0, s>>>(
+        a.n, a.cap, a.hi, a.lo, a.perm, a.cell_sorted, a.cell_start, a.grid, a.pos, a.excl_start, a.excl, a.list,
+        a.count, a.gmax, a.status, (float)(rl2 - margin), (float)(rl2 + margin), rl2, a.box[0], a.box[1], a.box[2]);
+}

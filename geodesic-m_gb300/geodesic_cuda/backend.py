@@ -1,0 +1,333 @@
+"""Python host mirror of the reference's `ComputeBackend` trait over the C ABI.
+
+`CudaBackend` has the trait's methods with the same meaning
+(geodesic-core/src/backend.rs:11-23): it owns the atoms and topology, keeps
+the neighbour list and forces on the GPU, and returns forces in the reference
+layout (three float64 rows of N).  The engine free functions the run loop
+calls directly (integrator::half_kick, constraint::constrain_velocities and
+the kinetic-energy sum of lib.rs:68-77) are methods here too, so a run loop
+can drive the whole step through this object.
+
+There is no CPU fallback: constructing a backend without the compiled
+library or without a CUDA device raises `BackendError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+from . import _build
+
+GM_OK = 0
+STATUS_NAMES = {
+    1: "INVALID_ARGUMENT", 2: "NO_DEVICE", 3: "OUT_OF_MEMORY", 4: "DEVICE", 5: "CONVERGENCE", 6: "NONFINITE",
+    7: "LIST_OVERFLOW", 8: "UNSUPPORTED", 9: "FIXED_POINT_OVERFLOW", 10: "NOT_BUILT",
+}
+PRECISION_MIXED, PRECISION_FP64 = 0, 1
+
+_u32p = C.POINTER(C.c_uint32)
+_f64p = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class BackendError(RuntimeError):
+    """BackendError (geodesic-core/src/error.rs:81-91) and the other status codes."""
+
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class NumericalError(BackendError):
+    """NumericalError (error.rs:34-48): non-finite force or position."""
+
+
+class ConvergenceError(BackendError):
+    """ConvergenceError::ConstraintSolver (error.rs:50-63)."""
+
+    def __init__(self, status, message, conv):
+        super().__init__(status, message)
+        self.step, self.constraint_idx = int(conv.step), int(conv.constraint_idx)
+        self.atom_i, self.atom_j = int(conv.atom_i), int(conv.atom_j)
+        self.residual, self.max_iter = float(conv.residual), int(conv.max_iter)
+
+
+class GmAtoms(C.Structure):
+    _fields_ = [("n_atoms", C.c_int64), ("sigma", _f64p), ("epsilon", _f64p), ("mass", _f64p),
+                ("charge", _f64p), ("element", _u8p)]
+
+
+class GmTopology(C.Structure):
+    _fields_ = [("n_bonds", C.c_int64), ("bond_i", _u32p), ("bond_j", _u32p), ("bond_k", _f64p), ("bond_r0", _f64p),
+                ("n_angles", C.c_int64), ("angle_i", _u32p), ("angle_j", _u32p), ("angle_k", _u32p),
+                ("angle_kth", _f64p), ("angle_th0", _f64p),
+                ("n_diheds", C.c_int64), ("dihed_i", _u32p), ("dihed_j", _u32p), ("dihed_k", _u32p),
+                ("dihed_l", _u32p), ("dihed_kphi", _f64p), ("dihed_n", _u32p), ("dihed_delta", _f64p),
+                ("n_constr", C.c_int64), ("constr_i", _u32p), ("constr_j", _u32p), ("constr_dsq", _f64p),
+                ("n_excl", C.c_int64), ("excl_i", _u32p), ("excl_j", _u32p)]
+
+
+class GmParams(C.Structure):
+    _fields_ = [("box", C.c_double * 3), ("periodic", C.c_int32), ("precision", C.c_int32),
+                ("r_cutoff", C.c_double), ("r_skin", C.c_double), ("r_switch", C.c_double),
+                ("max_constr_iter", C.c_uint32), ("constr_tol", C.c_double), ("coulomb", C.c_int32),
+                ("scale14_lj", C.c_double), ("scale14_coul", C.c_double), ("device", C.c_int32)]
+
+
+class GmConvergence(C.Structure):
+    _fields_ = [("step", C.c_uint64), ("constraint_idx", C.c_int64), ("atom_i", C.c_int64), ("atom_j", C.c_int64),
+                ("residual", C.c_double), ("max_iter", C.c_uint32)]
+
+
+@dataclasses.dataclass
+class SimParams:
+    """The SimParams fields on the path (geodesic-core/src/params.rs:4-23) plus
+    the backend's own options."""
+
+    box_size: tuple = (1000.0, 1000.0, 1000.0)
+    periodic: bool = False
+    r_cutoff: float = 12.0
+    r_skin: float = 14.0
+    r_switch: float = 10.0
+    max_constr_iter: int = 100
+    constr_tol: float = 1e-10
+    precision: int = PRECISION_MIXED
+    coulomb: bool = False
+    scale14_lj: float = 0.0
+    scale14_coul: float = 0.0
+    device: int = 0
+
+    def to_c(self) -> GmParams:
+        return GmParams((C.c_double * 3)(*self.box_size), int(self.periodic), int(self.precision), self.r_cutoff,
+                        self.r_skin, self.r_switch, int(self.max_constr_iter), self.constr_tol, int(self.coulomb),
+                        self.scale14_lj, self.scale14_coul, int(self.device))
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.CUDA_LIB
+
+
+def lib():
+    """Loads the in-tree C-ABI library; raises if it was never built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise BackendError(2, f"CUDA backend library not built: {path} (run __graft_entry__.build())")
+        L = C.CDLL(path)
+        P = C.POINTER
+        L.gm_create.restype = C.c_void_p
+        L.gm_create.argtypes = [P(GmAtoms), P(GmTopology), P(GmParams), P(C.c_int32)]
+        L.gm_destroy.argtypes = [C.c_void_p]
+        L.gm_build_list.argtypes = [C.c_void_p, _f64p, _f64p, _f64p]
+        L.gm_compute_forces.argtypes = [C.c_void_p] + [_f64p] * 7
+        L.gm_needs_rebuild.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, P(C.c_int32)]
+        L.gm_geodesic_drift.argtypes = [C.c_void_p] + [_f64p] * 6 + [C.c_double, C.c_uint64, P(GmConvergence)]
+        L.gm_half_kick.argtypes = [C.c_void_p] + [_f64p] * 6 + [C.c_double]
+        L.gm_constrain_velocities.argtypes = [C.c_void_p] + [_f64p] * 6 + [C.c_uint64, P(GmConvergence)]
+        L.gm_kinetic_energy.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, _f64p]
+        L.gm_n_threads.argtypes = [C.c_void_p]
+        L.gm_get_pairs.argtypes = [C.c_void_p, C.c_int64, _u32p, _u32p, P(C.c_int64)]
+        L.gm_steps.argtypes = [C.c_void_p] + [_f64p] * 6 + [C.c_double, C.c_uint64, C.c_int64] + [_f64p] * 4 + [
+            P(C.c_int64), P(GmConvergence)]
+        L.gm_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_int64]
+        L.gm_upload_state.argtypes = [C.c_void_p] + [_f64p] * 6
+        L.gm_download_state.argtypes = [C.c_void_p] + [_f64p] * 6
+        L.gm_run_resident.argtypes = [C.c_void_p, C.c_double, C.c_uint64, C.c_int64]
+        L.gm_forces_resident.argtypes = [C.c_void_p]
+        L.gm_synchronize.argtypes = [C.c_void_p, P(GmConvergence)]
+        L.gm_stream.restype = C.c_void_p
+        L.gm_stream.argtypes = [C.c_void_p]
+        L.gm_counters.argtypes = [C.c_void_p, P(C.c_int64), C.c_int64]
+        for f in ("gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
+                  "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
+                  "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
+                  "gm_forces_resident", "gm_synchronize", "gm_counters"):
+            getattr(L, f).restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _rows(a):
+    """Three contiguous float64 rows of a (3, N) array, with their pointers."""
+    assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape[0] == 3, "expect C-contiguous float64 (3, N)"
+    return _p(a[0]), _p(a[1]), _p(a[2])
+
+
+class CudaBackend:
+    """`ComputeBackend` for `backend = "cuda"` (geodesic-core/src/backend.rs:11-23)."""
+
+    def __init__(self, atoms, topology, params: SimParams):
+        L = lib()
+        self._atoms, self._topo, self.params = atoms, topology, params
+        self.n = int(len(atoms.mass))
+        keep = []
+
+        def f(a):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return _p(a)
+
+        def u(a):
+            a = np.ascontiguousarray(a, dtype=np.uint32)
+            keep.append(a)
+            return _p(a, C.c_uint32)
+
+        el = getattr(atoms, "element", None)
+        elp = None
+        if el is not None:
+            el = np.ascontiguousarray(el, dtype=np.uint8)
+            keep.append(el)
+            elp = _p(el, C.c_uint8)
+        ca = GmAtoms(self.n, f(atoms.sigma), f(atoms.epsilon), f(atoms.mass),
+                     f(getattr(atoms, "charge", np.zeros(self.n))), elp)
+        t = topology
+        ct = GmTopology(len(t.bond_i), u(t.bond_i), u(t.bond_j), f(t.bond_k), f(t.bond_r0),
+                        len(t.angle_i), u(t.angle_i), u(t.angle_j), u(t.angle_k), f(t.angle_kth), f(t.angle_th0),
+                        len(t.dihed_i), u(t.dihed_i), u(t.dihed_j), u(t.dihed_k), u(t.dihed_l), f(t.dihed_kphi),
+                        u(t.dihed_n), f(t.dihed_delta), len(t.constr_i), u(t.constr_i), u(t.constr_j),
+                        f(t.constr_dsq), len(t.excl_i), u(t.excl_i), u(t.excl_j))
+        st = C.c_int32()
+        cp = params.to_c()
+        self._h = L.gm_create(C.byref(ca), C.byref(ct), C.byref(cp), C.byref(st))
+        if not self._h:
+            raise BackendError(st.value, "gm_create failed")
+        self._forces = np.zeros((3, self.n))
+        self._energy = 0.0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, conv=None):
+        if rc == GM_OK:
+            return
+        buf = C.create_string_buffer(1024)
+        lib().gm_last_error(self._h, buf, 1024)
+        msg = buf.value.decode(errors="replace")
+        if rc == 5 and conv is not None:
+            raise ConvergenceError(rc, msg, conv)
+        if rc == 6:
+            raise NumericalError(rc, msg)
+        raise BackendError(rc, msg)
+
+    # ---------------------------------------------------------- trait
+    def build_neighbor_list(self, pos: np.ndarray) -> None:
+        """backend.rs:14: wraps `pos` in place when periodic."""
+        self._check(lib().gm_build_list(self._h, *_rows(pos)))
+
+    def compute_forces(self, pos: np.ndarray) -> np.ndarray:
+        """backend.rs:15: forces (3, N) at `pos`; energy in potential_energy()."""
+        e = C.c_double()
+        rc = lib().gm_compute_forces(self._h, *_rows(np.ascontiguousarray(pos)), *_rows(self._forces), C.byref(e))
+        self._energy = e.value
+        self._check(rc)
+        return self._forces
+
+    def geodesic_drift(self, pos: np.ndarray, vel: np.ndarray, dt: float, step: int = 0) -> None:
+        """backend.rs:16: drift + SHAKE + velocity resync, in place."""
+        conv = GmConvergence()
+        self._check(lib().gm_geodesic_drift(self._h, *_rows(pos), *_rows(vel), dt, step, C.byref(conv)), conv)
+
+    def reduce_forces(self) -> np.ndarray:
+        """backend.rs:17"""
+        return self._forces.copy()
+
+    def potential_energy(self) -> float:
+        """backend.rs:18"""
+        return self._energy
+
+    def atoms(self):
+        return self._atoms
+
+    def topology(self):
+        return self._topo
+
+    def needs_rebuild(self, pos: np.ndarray) -> bool:
+        """backend.rs:21"""
+        r = C.c_int32()
+        self._check(lib().gm_needs_rebuild(self._h, *_rows(np.ascontiguousarray(pos)), C.byref(r)))
+        return bool(r.value)
+
+    def n_threads(self) -> int:
+        return int(lib().gm_n_threads(self._h))
+
+    # ------------------------------------------ engine free functions
+    def half_kick(self, vel: np.ndarray, force: np.ndarray, dt_half: float) -> None:
+        """integrator::half_kick (integrator.rs:14-21)."""
+        self._check(lib().gm_half_kick(self._h, *_rows(vel), *_rows(np.ascontiguousarray(force)), dt_half))
+
+    def constrain_velocities(self, pos: np.ndarray, vel: np.ndarray, step: int = 0) -> None:
+        """constraint::constrain_velocities (constraint.rs:170-259)."""
+        conv = GmConvergence()
+        self._check(lib().gm_constrain_velocities(self._h, *_rows(np.ascontiguousarray(pos)), *_rows(vel), step,
+                                                  C.byref(conv)), conv)
+
+    def kinetic_energy(self, vel: np.ndarray) -> float:
+        """lib.rs:68-77"""
+        ke = C.c_double()
+        self._check(lib().gm_kinetic_energy(self._h, *_rows(np.ascontiguousarray(vel)), C.byref(ke)))
+        return ke.value
+
+    # ---------------------------------------------------- extras
+    def pairs(self):
+        """The current list as the reference's NeighborList pair_i/pair_j."""
+        L = lib()
+        cnt = C.c_int64()
+        self._check(L.gm_get_pairs(self._h, 0, None, None, C.byref(cnt)))
+        pi = np.zeros(max(cnt.value, 1), np.uint32)
+        pj = np.zeros(max(cnt.value, 1), np.uint32)
+        self._check(L.gm_get_pairs(self._h, cnt.value, _p(pi, C.c_uint32), _p(pj, C.c_uint32), C.byref(cnt)))
+        return pi[:cnt.value], pj[:cnt.value]
+
+    def steps(self, pos, vel, dt, n_steps, first_step=0, want_forces=False):
+        """Device-resident BAB + RATTLE steps (lib.rs:292-323), state in place.
+        Returns (potential energy, list rebuilds, forces or None)."""
+        conv = GmConvergence()
+        e = C.c_double()
+        nr = C.c_int64()
+        f = np.zeros((3, self.n)) if want_forces else None
+        fr = _rows(f) if want_forces else (None, None, None)
+        self._check(lib().gm_steps(self._h, *_rows(pos), *_rows(vel), dt, first_step, n_steps, *fr, C.byref(e),
+                                   C.byref(nr), C.byref(conv)), conv)
+        self._energy = e.value
+        return e.value, nr.value, f
+
+    def upload_state(self, pos, vel):
+        self._check(lib().gm_upload_state(self._h, *_rows(np.ascontiguousarray(pos)), *_rows(np.ascontiguousarray(vel))))
+
+    def download_state(self, pos, vel):
+        self._check(lib().gm_download_state(self._h, *_rows(pos), *_rows(vel)))
+
+    def run_resident(self, dt, n_steps, first_step=0):
+        self._check(lib().gm_run_resident(self._h, dt, first_step, n_steps))
+
+    def forces_resident(self):
+        self._check(lib().gm_forces_resident(self._h))
+
+    def synchronize(self):
+        conv = GmConvergence()
+        self._check(lib().gm_synchronize(self._h, C.byref(conv)), conv)
+
+    def stream(self) -> int:
+        return int(lib().gm_stream(self._h) or 0)
+
+    def counters(self) -> dict:
+        out = (C.c_int64 * 8)()
+        self._check(lib().gm_counters(self._h, out, 8))
+        return dict(pairs=out[0], rebuilds=out[1], cap=out[2], launches=out[3], shake_iters=out[4],
+                    rattle_iters=out[5], launches_per_step=out[6])

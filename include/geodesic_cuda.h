@@ -1,0 +1,175 @@
+/*
+ * geodesic_cuda.h — C ABI of the GB300 (sm_103a) compute backend for
+ * GEODESIC-M, selected as `backend = "cuda"` beside "cpu" and "gpu".
+ *
+ * The entry points mirror the reference's `ComputeBackend` trait
+ * (geodesic-core/src/backend.rs:11-23) plus the three engine free functions
+ * the run loop calls directly (integrator::half_kick, constraint::
+ * constrain_velocities, lib.rs:68-77 kinetic energy).  All arrays are plain
+ * caller-owned host pointers in the reference's SoA layout (f64 x/y/z rows,
+ * u32 indices); they are read or written only during the call.  Device
+ * buffers are owned by the context.  Every call returns a gm_status (0 = ok).
+ *
+ * Thread safety: a context may be driven from any one thread at a time (the
+ * trait is `Send`, not `Sync`); each entry point makes the context's device
+ * current itself and uses the context's own stream.
+ */
+#ifndef GEODESIC_CUDA_H
+#define GEODESIC_CUDA_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The Rust binding maps them onto the reference's errors:
+ * NO_DEVICE -> BackendError::NoAdapter, OUT_OF_MEMORY ->
+ * BackendError::OutOfGpuMemory, DEVICE -> BackendError::DeviceLost,
+ * CONVERGENCE -> ConvergenceError::ConstraintSolver (details in
+ * gm_convergence), NONFINITE -> NumericalError, others -> ConfigError. */
+typedef enum {
+    GM_OK = 0,
+    GM_ERR_INVALID_ARGUMENT = 1,
+    GM_ERR_NO_DEVICE = 2,
+    GM_ERR_OUT_OF_MEMORY = 3,
+    GM_ERR_DEVICE = 4,
+    GM_ERR_CONVERGENCE = 5,
+    GM_ERR_NONFINITE = 6,
+    GM_ERR_LIST_OVERFLOW = 7,
+    GM_ERR_UNSUPPORTED = 8,
+    GM_ERR_FIXED_POINT_OVERFLOW = 9,
+    GM_ERR_NOT_BUILT = 10
+} gm_status;
+
+/* Arithmetic of the force path. */
+typedef enum {
+    GM_PRECISION_MIXED = 0, /* FP32 pair/bonded math, int64 fixed-point sums, FP64 energy and integrator */
+    GM_PRECISION_FP64 = 1   /* FP64 everywhere (int64 fixed-point sums) */
+} gm_precision;
+
+/* AtomData (geodesic-core/src/atoms.rs:3-12); element: 0 = hydrogen. */
+typedef struct {
+    int64_t n_atoms;
+    const double *sigma, *epsilon, *mass, *charge;
+    const uint8_t *element; /* may be NULL (no hydrogen information) */
+} gm_atoms;
+
+/* BondedTopology (geodesic-core/src/topology.rs:4-37). */
+typedef struct {
+    int64_t n_bonds;  const uint32_t *bond_i, *bond_j; const double *bond_k, *bond_r0;
+    int64_t n_angles; const uint32_t *angle_i, *angle_j, *angle_k; const double *angle_kth, *angle_th0;
+    int64_t n_diheds; const uint32_t *dihed_i, *dihed_j, *dihed_k, *dihed_l;
+    const double *dihed_kphi; const uint32_t *dihed_n; const double *dihed_delta;
+    int64_t n_constr; const uint32_t *constr_i, *constr_j; const double *constr_dsq;
+    int64_t n_excl;   const uint32_t *excl_i, *excl_j;
+} gm_topology;
+
+/* SimParams (geodesic-core/src/params.rs:4-23), fields on the path. */
+typedef struct {
+    double box[3];
+    int32_t periodic;
+    int32_t precision;        /* gm_precision */
+    double r_cutoff, r_skin, r_switch;
+    uint32_t max_constr_iter;
+    double constr_tol;
+    /* beyond the reference (0 = off = reference behaviour) */
+    int32_t coulomb;          /* q_i q_j 332.0522173 / r with the LJ switch */
+    double scale14_lj, scale14_coul;
+    int32_t device;           /* CUDA device ordinal */
+} gm_params;
+
+/* ConvergenceError::ConstraintSolver (geodesic-core/src/error.rs:50-63). */
+typedef struct {
+    uint64_t step;
+    int64_t constraint_idx, atom_i, atom_j;
+    double residual;
+    uint32_t max_iter;
+} gm_convergence;
+
+typedef struct gm_ctx gm_ctx;
+
+/* CpuBackend::new / GpuBackend::try_new (cpu_backend.rs:50-83,
+ * gpu_backend.rs:24-53).  Copies atoms and topology to the device.  Returns
+ * NULL and sets *status on failure. */
+gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *topo, const gm_params *params, int32_t *status);
+
+/* Drop of the backend. */
+int32_t gm_destroy(gm_ctx *ctx);
+
+/* ComputeBackend::build_neighbor_list (backend.rs:14, neighbor.rs:8-55).
+ * Wraps positions in place when periodic; the list is kept on the device. */
+int32_t gm_build_list(gm_ctx *ctx, double *px, double *py, double *pz);
+
+/* ComputeBackend::compute_forces + potential_energy (backend.rs:15,18,
+ * cpu_backend.rs:92-182): bonded + nonbonded forces at the given positions
+ * into fx/fy/fz (overwritten), total potential into *energy.  On failure the
+ * forces are NaN-poisoned so the caller's finiteness check stops the run. */
+int32_t gm_compute_forces(gm_ctx *ctx, const double *px, const double *py, const double *pz,
+                          double *fx, double *fy, double *fz, double *energy);
+
+/* ComputeBackend::needs_rebuild (backend.rs:21, neighbor.rs:60-72). */
+int32_t gm_needs_rebuild(gm_ctx *ctx, const double *px, const double *py, const double *pz, int32_t *result);
+
+/* ComputeBackend::geodesic_drift (backend.rs:16, integrator.rs:32-71):
+ * r += dt v, SHAKE projection, v = (r_new - r_old)/dt.  On non-convergence
+ * returns GM_ERR_CONVERGENCE with *err filled (positions left partially
+ * corrected, as the reference does). */
+int32_t gm_geodesic_drift(gm_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz,
+                          double dt, uint64_t step, gm_convergence *err);
+
+/* integrator::half_kick (integrator.rs:14-21). */
+int32_t gm_half_kick(gm_ctx *ctx, double *vx, double *vy, double *vz, const double *fx, const double *fy,
+                     const double *fz, double dt_half);
+
+/* constraint::constrain_velocities (constraint.rs:170-259), RATTLE. */
+int32_t gm_constrain_velocities(gm_ctx *ctx, const double *px, const double *py, const double *pz,
+                                double *vx, double *vy, double *vz, uint64_t step, gm_convergence *err);
+
+/* lib.rs:68-77 */
+int32_t gm_kinetic_energy(gm_ctx *ctx, const double *vx, const double *vy, const double *vz, double *ke);
+
+/* ComputeBackend::n_threads (backend.rs:22): always 1 (gpu_backend.rs:99). */
+int32_t gm_n_threads(const gm_ctx *ctx);
+
+/* Copies the current half pair list out as the reference's NeighborList
+ * pair_i/pair_j (topology.rs:42-55): i < j, sorted by (i, then j).  With
+ * pair_i == NULL only *n_pairs is returned. */
+int32_t gm_get_pairs(gm_ctx *ctx, int64_t cap, uint32_t *pair_i, uint32_t *pair_j, int64_t *n_pairs);
+
+/* Device-resident BAB + RATTLE loop (lib.rs:292-323 without I/O): uploads
+ * (p, v), runs n_steps steps with the list rebuilt on the device whenever an
+ * atom moved more than half the skin, downloads (p, v) and the last forces
+ * (fx/fy/fz may be NULL) and potential energy.  *n_rebuilds (nullable)
+ * receives the number of list rebuilds. */
+int32_t gm_steps(gm_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz,
+                 double dt, uint64_t first_step, int64_t n_steps, double *fx, double *fy, double *fz,
+                 double *energy, int64_t *n_rebuilds, gm_convergence *err);
+
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int32_t gm_last_error(const gm_ctx *ctx, char *buf, int64_t len);
+
+/* ---- resident-state interface (benchmarks, batching) ------------------ */
+
+/* Uploads positions and velocities to the device state. */
+int32_t gm_upload_state(gm_ctx *ctx, const double *px, const double *py, const double *pz,
+                        const double *vx, const double *vy, const double *vz);
+/* Downloads positions and velocities from the device state. */
+int32_t gm_download_state(gm_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz);
+/* Runs n_steps BAB steps on the resident state (asynchronous on the
+ * context's stream; call gm_synchronize to collect errors). */
+int32_t gm_run_resident(gm_ctx *ctx, double dt, uint64_t first_step, int64_t n_steps);
+/* Evaluates forces on the resident positions only (asynchronous). */
+int32_t gm_forces_resident(gm_ctx *ctx);
+/* Waits for the stream and reports device-side errors. */
+int32_t gm_synchronize(gm_ctx *ctx, gm_convergence *err);
+/* The context's cudaStream_t, for callers that time work on it. */
+void *gm_stream(gm_ctx *ctx);
+/* Counters: [0] pairs in the current list, [1] list rebuilds so far,
+ * [2] list capacity per atom, [3] kernel launches issued so far,
+ * [4] last SHAKE iteration count, [5] last RATTLE iteration count. */
+int32_t gm_counters(const gm_ctx *ctx, int64_t *out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
