@@ -1,0 +1,368 @@
+"""Throughput of the GEODESIC-M CUDA backend: ns/day and pair interactions/s.
+
+Workload (one "step" = one geodesic-BAB + RATTLE step, lib.rs:292-323): the
+seeded 50,000-atom synthetic system -- jittered cubic lattice (2.15 A, +-0.3
+A), serpentine bond/angle/dihedral chain, 8 Lorentz-Berthelot types, charges
++-0.5 e net zero, Coulomb and scaled 1-4 pairs (LJ 1/2.0, Coulomb 1/1.2),
+cutoff 10 / switch 8 / list radius 12 A (rebuild when an atom moves > 1 A),
+non-periodic 10^4 A box, Maxwell-Boltzmann 300 K, dt = 2 fs -- in mixed
+precision, inputs resident on the device.  The FP64 device path is timed on
+the same system for the mixed/FP64 ratio.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
+
+--impl reference times the oracle (the FP64 C restatement of the reference
+CPU path, static thread strips over all host cores) on the same workload.
+With torchrun and N > 1 every rank runs an independent replica ("replicas
+only": the path has no exchange step) and rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "geodesic-m_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+N_ATOMS = 50_000
+SEED = 20261203
+DT_PS = 0.002
+METRIC = "ns/day & pairs/s at 50k atoms: mixed vs FP64 GPU path at ≤1e-5 rel force err"
+PHYS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
+            scale14_lj=0.5, scale14_coul=1.0 / 1.2, max_constr_iter=100, constr_tol=1e-10)
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def ns_per_day(steps, seconds):
+    return DT_PS * 1e-3 * steps / seconds * 86400.0
+
+
+def workload(rank=0):
+    from geodesic_cuda import synth
+    # the lattice is over-compressed for its sigma range: FIRE-minimise it
+    # (1000 iterations, two stages) so NVE starts near 300 K instead of
+    # converting ~25 kcal/mol/atom of compression energy into heat
+    return synth.generate(N_ATOMS, seed=SEED + rank, temperature=300.0, relax_iters=1000)
+
+
+def config_dict(extra=None):
+    d = {"workload": "synthetic lattice chain, 50,000 atoms (cube 79.6 A), mixed precision, 2 fs BAB + RATTLE",
+         "n_atoms": N_ATOMS, "seed": SEED, "cutoff_A": 10.0, "switch_A": 8.0, "list_radius_A": 12.0,
+         "coulomb": True, "scale14": [0.5, 1 / 1.2], "periodic": False, "dt_fs": 2.0,
+         "l2": "flushed between timed steps (256 MB memset outside the timed span)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def pinned_like(a):
+    """A pinned host copy (torch page-locked memory) viewed as numpy."""
+    import torch
+    t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+    v = t.numpy()
+    v[...] = a
+    return t, v
+
+
+def run_cuda(args, rank, world):
+    import torch
+
+    from geodesic_cuda import backend
+    import oracle
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    atoms, topo, state, info = workload(rank)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, device=dev, **PHYS)
+    be = backend.CudaBackend(atoms, topo, p)
+    be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
+    be.forces_resident()
+    be.run_resident(DT_PS, args.warmup)
+    be.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+    c0 = be.counters()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                               flush_bytes=L2_FLUSH_BYTES)
+        t1 = time.perf_counter()
+    torch.cuda.synchronize()
+    c1 = be.counters()
+    sec = dev_ms / 1e3
+    if world > 1:
+        tt = torch.tensor([sec], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        sec = float(tt.item())
+    pairs = c1["pairs"]
+    result = dict(sec=sec, wall=t1 - t0, pairs=pairs, rebuilds=c1["rebuilds"] - c0["rebuilds"],
+                  launches=c1["launches"] - c0["launches"], clocks=clk.summary())
+    if rank != 0:
+        return None
+    # steady state: back-to-back steps, no flush (L2 keeps part of the list)
+    t_bb = be.time_steps(DT_PS, min(args.steps, 2000), first_step=args.warmup + args.steps) / 1e3
+    # roofline of the pair kernel: SURVEY algorithmic bytes 4 P + 52 N per launch
+    t_pair = be.profile("pair", 30) / 1e3
+    t_bonded = be.profile("bonded", 30) / 1e3
+    t_rebuild = be.profile("rebuild", 5) / 1e3
+    alg_bytes = 4 * pairs + 52 * N_ATOMS
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / t_pair / 1e9
+    # force / energy error of both device paths vs the FP64 oracle at step 0
+    pos0 = np.ascontiguousarray(state.pos)
+    op = oracle.make_params(box=PHYS["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0,
+                            n_threads=0, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2)
+    oarr_pi, oarr_pj = oracle.neighbor_build(pos0.copy(), atoms, topo, op, cells=True)
+    ob = oracle.CpuBackend(atoms, topo, op)
+    ob.set_pairs(oarr_pi, oarr_pj, pos0)
+    f_ref = ob.compute_forces(pos0)
+    e_ref = ob.potential_energy
+    errs = {}
+    fp64_nsday = None
+    for name, prec in (("mixed", backend.PRECISION_MIXED), ("fp64", backend.PRECISION_FP64)):
+        b2 = backend.CudaBackend(atoms, topo, backend.SimParams(precision=prec, device=dev, **PHYS))
+        pp = pos0.copy()
+        b2.build_neighbor_list(pp)
+        f = b2.compute_forces(pp).copy()
+        errs[name] = dict(force_rel_l2=float(np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref)),
+                          force_max_rel=float(np.max(np.abs(f - f_ref) / np.maximum(np.abs(f_ref), 1.0))),
+                          energy_rel=float(abs(b2.potential_energy() - e_ref) / abs(e_ref)))
+        if prec == backend.PRECISION_FP64:
+            b2.upload_state(pos0, np.ascontiguousarray(state.vel))
+            b2.forces_resident()
+            b2.run_resident(DT_PS, 3)
+            b2.synchronize()
+            n64 = max(50, min(args.steps, 300))
+            s64 = b2.time_steps(DT_PS, n64, first_step=3, flush_ptr=flush.data_ptr(),
+                                flush_bytes=L2_FLUSH_BYTES) / 1e3
+            fp64_nsday = ns_per_day(n64, s64)
+        b2.close()
+    # e2e: the public API with host buffers, one gm_steps call per step
+    # (H2D of positions+velocities from pinned memory, one device step, D2H
+    # of positions+velocities and the energy)
+    tp, hp = pinned_like(state.pos)
+    tv, hv = pinned_like(state.vel)
+    be.download_state(hp, hv)
+    n_e2e = max(20, min(args.steps, 500))
+    be.steps(hp, hv, DT_PS, 1)
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        be.steps(hp, hv, DT_PS, 1)
+    t_e2e = time.perf_counter() - t0
+    h2d = 6 * 8 * N_ATOMS
+    d2h = 6 * 8 * N_ATOMS + 8
+    # CPU baseline: the oracle on this host's cores, bounded sample
+    cpu = cpu_baseline_sample(atoms, topo, state, result["rebuilds"] / max(args.steps, 1))
+    steps_per_s = args.steps / sec
+    line = {
+        "metric": METRIC, "value": round(world * ns_per_day(args.steps, sec), 3), "unit": "ns/day",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * sec / args.steps, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 pair math, int64 fixed-point forces, fp64 state/energy",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": config_dict({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                               "list_rebuilds_in_timed_region": result["rebuilds"]}),
+        "pairs_per_s": round(world * pairs * steps_per_s, 1), "half_list_pairs": pairs,
+        "fp64_path_ns_per_day": round(fp64_nsday, 3) if fp64_nsday else None,
+        "mixed_over_fp64": round(ns_per_day(args.steps, sec) / fp64_nsday, 2) if fp64_nsday else None,
+        "steady_state_ns_per_day": round(ns_per_day(min(args.steps, 2000), t_bb), 3),
+        "errors_vs_fp64_oracle_step0": errs,
+        "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
+                      "list_rebuild": round(t_rebuild * 1e3, 4)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "pair_kernel_f32", "algorithmic_bytes": alg_bytes},
+        "e2e": {"value": round(ns_per_day(n_e2e, t_e2e), 3), "unit": "ns/day", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
+        "gpu_launches": int(result["launches"]),
+        "clocks": result["clocks"],
+        "cpu_baseline": cpu,
+    }
+    return line
+
+
+def cpu_baseline_sample(atoms, topo, state, rebuilds_per_step):
+    """Oracle (C restatement, static strips over all host cores) on the same
+    system: five force evaluations on the reference's pair list, plus the
+    reference's O(N^2) serial list build timed on the first N/4 atoms and
+    scaled by 16, combined per BAB step at the GPU run's rebuild rate."""
+    import oracle
+    nthreads = oracle.host_threads()
+    op = oracle.make_params(box=PHYS["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0,
+                            n_threads=nthreads, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2)
+    pos = np.ascontiguousarray(state.pos)
+    pi, pj = oracle.neighbor_build(pos.copy(), atoms, topo, op, cells=True)
+    ob = oracle.CpuBackend(atoms, topo, op)
+    ob.set_pairs(pi, pj, pos)
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ob.compute_forces(pos)
+        ts.append(time.perf_counter() - t0)
+    t_force = float(np.median(ts))
+    ns = N_ATOMS // 4
+    sub = _Sub(atoms, ns)
+    t0 = time.perf_counter()
+    oracle.neighbor_build(np.ascontiguousarray(pos[:, :ns]), sub, _sub_topo(topo, ns), op)
+    t_build = (time.perf_counter() - t0) * (N_ATOMS / ns) ** 2
+    t_step = t_force + t_build * rebuilds_per_step
+    return {"value": round(ns_per_day(1, t_step), 4), "unit": "ns/day", "cores": nthreads, "kind": "port",
+            "sample": (f"oracle CpuBackend forces {t_force:.3f} s/eval (median of 5, {nthreads} threads) + "
+                       f"reference O(N^2) serial list build timed on {ns} atoms and scaled x16 ({t_build:.1f} s) "
+                       f"at {rebuilds_per_step:.4f} rebuilds/step; integrator O(N) terms neglected")}
+
+
+class _Sub:
+    def __init__(self, atoms, n):
+        self.sigma, self.epsilon, self.mass = atoms.sigma[:n], atoms.epsilon[:n], atoms.mass[:n]
+        self.charge, self.element = atoms.charge[:n], atoms.element[:n]
+
+
+def _sub_topo(topo, n):
+    from geodesic_cuda import amber
+    t = amber.BondedTopology.empty()
+    keep = (topo.excl_i < n) & (topo.excl_j < n)
+    t.excl_i, t.excl_j = topo.excl_i[keep], topo.excl_j[keep]
+    return t
+
+
+def run_reference(args):
+    """Times the oracle's BAB loop (the reference CPU path restated in C, all
+    host cores) on the same workload; min(K, 20) timed steps after W warm-up
+    steps, reported per step."""
+    import oracle
+    atoms, topo, state, info = workload(0)
+    nthreads = oracle.host_threads()
+    op = oracle.make_params(box=PHYS["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0,
+                            n_threads=nthreads, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2,
+                            max_constr_iter=100, constr_tol=1e-10)
+    pos = np.ascontiguousarray(state.pos.copy())
+    vel = np.ascontiguousarray(state.vel.copy())
+    b = oracle.CpuBackend(atoms, topo, op)
+    pi, pj = oracle.neighbor_build(pos.copy(), atoms, topo, op, cells=True)
+    b.set_pairs(pi, pj, pos)  # the reference's pair set, without timing its O(N^2) build here
+    f = b.compute_forces(pos)
+    n_w = min(args.warmup, 3)
+    n_t = max(1, min(args.steps, 20))
+    t_total, n_reb = 0.0, 0
+    for k in range(n_w + n_t):
+        t0 = time.perf_counter()
+        oracle.half_kick(vel, f, atoms.mass, DT_PS / 2)
+        b.geodesic_drift(pos, vel, DT_PS, k)
+        if b.needs_rebuild(pos):
+            b.build_neighbor_list(pos)  # the reference's O(N^2) serial build
+            n_reb += k >= n_w
+        f = b.compute_forces(pos)
+        oracle.half_kick(vel, f, atoms.mass, DT_PS / 2)
+        dt = time.perf_counter() - t0
+        if k >= n_w:
+            t_total += dt
+    val = ns_per_day(n_t, t_total)
+    return {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "ns/day", "n_gpus": 1,
+            "steps": n_t, "warmup": n_w, "ms_per_step": round(1e3 * t_total / n_t, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded generator)",
+            "config": config_dict({"steps_requested": args.steps}),
+            "cpu_baseline": {"value": round(val, 4), "unit": "ns/day", "cores": nthreads, "kind": "port",
+                             "sample": f"{n_t} BAB steps of the oracle loop after {n_w} warm-up steps "
+                                       f"({n_reb} O(N^2) list rebuilds in the timed steps)"},
+            "e2e": {"value": round(val, 4), "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    line = run_cuda(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -531,11 +531,27 @@ int capture_graph(gm_ctx *c, double dt) {
 }
 
 int ensure_forces(gm_ctx *c) {
-    // the first half-kick of a step needs forces at the current positions
+    // the first half-kick of a step needs forces at the current positions;
+    // an existing list stays valid while no atom moved more than half the
+    // skin from its build position (neighbor.rs:60-72)
     if (c->forces_current) return GM_OK;
     if (!c->built) {
         int rc = do_build(c);
         if (rc) return rc;
+    } else {
+        int rc = reset_status(c);
+        if (rc) return rc;
+        const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;
+        gm_launch_check(c->n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, 0ull, gm_check_blocks(c->n),
+                        c->stream);
+        c->launches++;
+        rc = st_read(c);
+        if (rc) return rc;
+        if (c->h_status->error & GM_DEV_NONFINITE_POS) return fail(c, GM_ERR_NONFINITE, "non-finite position");
+        if (c->h_status->rebuild) {
+            rc = do_build(c);
+            if (rc) return rc;
+        }
     }
     c->launches += seq_forces(c, c->stream);
     c->forces_current = true;
@@ -624,6 +640,10 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     c->fp64 = p.precision == GM_PRECISION_FP64;
     const int n = c->n;
     auto bail = [&](int code) -> gm_ctx * {
+        // no context survives to carry the message: report it on stderr
+        const cudaError_t le = cudaGetLastError();
+        fprintf(stderr, "gm_create: status %d (%s; last CUDA error: %s)\n", code,
+                c->err.empty() ? "setup failed" : c->err.c_str(), cudaGetErrorString(le));
         *status = code;
         gm_destroy(c);
         return nullptr;
@@ -1025,13 +1045,73 @@ int32_t gm_upload_state(gm_ctx *c, const double *px, const double *py, const dou
         int rc = ensure_list_buffers(c, estimate_cap(c, px, py, pz));
         if (rc) return rc;
     }
-    int rc = upload3(c, c->d_pos, px, py, pz);
-    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
+    int rc;
+    if (c->forces_current) {
+        // forces stay valid when the caller hands back the resident positions
+        rc = upload3(c, c->d_dref, px, py, pz);
+        if (rc) return rc;
+        rc = reset_status(c);
+        if (rc) return rc;
+        gm_launch_differs(c->n, c->d_dref, c->d_pos, &c->d_status->differs, c->stream);
+        c->launches++;
+        rc = st_read(c);
+        if (rc) return rc;
+        if (c->h_status->differs) {
+            c->forces_current = false;
+            GM_CUDA(c, cudaMemcpyAsync(c->d_pos, c->d_dref, sizeof(double) * 3 * (size_t)c->n,
+                                       cudaMemcpyDeviceToDevice, c->stream));
+        }
+    } else {
+        rc = upload3(c, c->d_pos, px, py, pz);
+        if (rc) return rc;
+    }
+    rc = upload3(c, c->d_vel, vx, vy, vz);
     if (rc) return rc;
-    c->built = false;
-    c->forces_current = false;
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     return GM_OK;
+}
+
+// Average duration of one kernel (or sequence) measured with CUDA events on
+// the context's stream: which = 0 pair kernel, 1 bonded kernel, 2 list
+// rebuild sequence, 3 one captured BAB step (graph launch), 4 pack kernel.
+int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *avg_ms) {
+    if (!c || !avg_ms || n_iter <= 0) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = ensure_forces(c);
+    if (rc) return rc;
+    if (which == 3) {
+        rc = capture_graph(c, dt);
+        if (rc) return rc;
+    }
+    cudaEvent_t e0, e1;
+    GM_CUDA(c, cudaEventCreate(&e0));
+    GM_CUDA(c, cudaEventCreate(&e1));
+    double total = 0.0;
+    ForceArgs fa = force_args(c);
+    ListArgs la = list_args(c);
+    for (int k = 0; k < n_iter; k++) {
+        cudaEventRecord(e0, c->stream);
+        switch (which) {
+            case 0: gm_launch_pair(fa, c->fp64, c->stream); break;
+            case 1: gm_launch_bonded(fa, c->fp64, c->stream); break;
+            case 2: seq_rebuild(c, c->stream); break;
+            case 3: cudaGraphLaunch(c->graph_exec, c->stream); break;
+            default: gm_launch_pack(la, c->fp64, c->stream); break;
+        }
+        cudaEventRecord(e1, c->stream);
+        GM_CUDA(c, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *avg_ms = total / n_iter;
+    // the pair/bonded kernels add into the force buffer: recompute it
+    c->forces_current = false;
+    rc = ensure_forces(c);
+    if (rc) return rc;
+    return check_status(c, nullptr);
 }
 
 int32_t gm_download_state(gm_ctx *c, double *px, double *py, double *pz, double *vx, double *vy, double *vz) {
@@ -1069,6 +1149,40 @@ int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_ste
     for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
     c->launches += c->launches_per_step * n_steps;
     return GM_OK;
+}
+
+int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps, void *flush_buf,
+                      int64_t flush_bytes, double *total_ms) {
+    if (!c || !(dt > 0) || n_steps <= 0 || !total_ms) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = reset_status(c);
+    if (!rc) rc = set_step(c, first_step);
+    if (!rc) rc = ensure_forces(c);
+    if (!rc) rc = capture_graph(c, dt);
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev((size_t)(2 * n_steps));
+    for (auto &e : ev) GM_CUDA(c, cudaEventCreate(&e));
+    if (flush_buf && flush_bytes > 0)
+        GM_CUDA(c, cudaMemsetAsync(flush_buf, 0, (size_t)flush_bytes, c->stream));
+    for (int64_t k = 0; k < n_steps; k++) {
+        GM_CUDA(c, cudaEventRecord(ev[(size_t)(2 * k)], c->stream));
+        GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        GM_CUDA(c, cudaEventRecord(ev[(size_t)(2 * k + 1)], c->stream));
+        // evict the step's working set so every timed step starts from HBM
+        if (flush_buf && flush_bytes > 0)
+            GM_CUDA(c, cudaMemsetAsync(flush_buf, (int)((k + 1) & 0xff), (size_t)flush_bytes, c->stream));
+    }
+    c->launches += c->launches_per_step * n_steps;
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    double total = 0.0;
+    for (int64_t k = 0; k < n_steps; k++) {
+        float ms = 0.f;
+        GM_CUDA(c, cudaEventElapsedTime(&ms, ev[(size_t)(2 * k)], ev[(size_t)(2 * k + 1)]));
+        total += ms;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    *total_ms = total;
+    return check_status(c, nullptr);
 }
 
 int32_t gm_synchronize(gm_ctx *c, gm_convergence *err) {

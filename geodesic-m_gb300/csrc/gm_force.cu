@@ -223,27 +223,21 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
     double e = 0.0;
     unsigned bad = 0;
     if (t < a.n_bonds) {
-        // force/bonded.rs:5-40, V = k (r - r0)^2
+        // force/bonded.rs:5-40, V = k (r - r0)^2.  FP64 in both paths: a bond
+        // stretched across a wrapped periodic boundary carries forces ~1e5
+        // kcal/mol/A whose FP32 rounding would swamp small net forces (the
+        // reference's GPU backend also keeps bonded terms in FP64).
         const int i = a.bond_i[t], j = a.bond_j[t];
-        const double dx64 = a.pos[j] - a.pos[i], dy64 = a.pos[n + j] - a.pos[n + i], dz64 = a.pos[2 * n + j] - a.pos[2 * n + i];
+        const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
         const double k = a.bond_k[t], r0 = a.bond_r0[t];
-        const double r2 = dx64 * dx64 + dy64 * dy64 + dz64 * dz64;
+        const double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 > 0.0) {
-            T r, dr;
-            if (sizeof(T) == 4) {
-                // r - r0 = (r^2 - r0^2) / (r + r0) keeps the stretch accurate in FP32
-                r = sqrtf((float)r2);
-                dr = (T)(r2 - r0 * r0) / (r + (T)r0);
-            } else {
-                r = (T)sqrt(r2);
-                dr = r - (T)r0;
-            }
-            const T dv_dr = (T)2 * (T)k * dr;
-            e = (double)((T)k * dr * dr);
-            const T g = dv_dr / r;
-            const T fx = g * (T)dx64, fy = g * (T)dy64, fz = g * (T)dz64;
-            add_force<T>(a.force, n, i, fx, fy, fz, bad);
-            add_force<T>(a.force, n, j, -fx, -fy, -fz, bad);
+            const double r = sqrt(r2);
+            const double dr = r - r0;
+            e = k * dr * dr;
+            const double g = 2.0 * k * dr / r;
+            add_force<double>(a.force, n, i, g * dx, g * dy, g * dz, bad);
+            add_force<double>(a.force, n, j, -g * dx, -g * dy, -g * dz, bad);
         }
     } else if (t < a.n_bonds + a.n_angles) {
         // force/bonded.rs:44-102, V = k (theta - theta0)^2

@@ -276,6 +276,13 @@ __global__ void kinetic_final(const double *partial, int blocks, double *out) {
     *out = 0.5 * sum * (1.0 / (20.455 * 20.455));  // lib.rs:25,76
 }
 
+__global__ void differs_kernel(int n3, const double *a, const double *b, unsigned int *flag) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int d = 0;
+    if (i < n3) d = __double_as_longlong(a[i]) != __double_as_longlong(b[i]);
+    if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
 __global__ void forces_out_kernel(int n3, const long long *force, double *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n3) out[i] = (double)force[i] * GM_FIX_INV;
@@ -333,6 +340,10 @@ void gm_launch_kinetic(int n, const double *vel, const double *mass, double *par
                        cudaStream_t s) {
     kinetic_partial<<<blocks, 256, 0, s>>>(n, vel, mass, partials);
     kinetic_final<<<1, 32, 0, s>>>(partials, blocks, out);
+}
+
+void gm_launch_differs(int n, const double *a, const double *b, unsigned int *flag, cudaStream_t s) {
+    if (n) differs_kernel<<<(3 * n + 255) / 256, 256, 0, s>>>(3 * n, a, b, flag);
 }
 
 void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s) {

@@ -49,7 +49,7 @@ struct DevStatus {
     unsigned int blocks_done;      // last-block-done counter of the rebuild check
     unsigned int shake_T;          // iteration count of the last SHAKE call
     unsigned int rattle_T;
-    unsigned int pad0;
+    unsigned int differs;          // uploaded positions differ from the resident ones
     unsigned long long n_rebuilds;
     unsigned long long step;       // current step of the resident loop
     unsigned long long fail_step;  // first step whose projection failed (init ~0)
@@ -200,4 +200,5 @@ void gm_launch_step(DevStatus *st, cudaStream_t s);
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,
                        cudaStream_t s);
 void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s);
+void gm_launch_differs(int n, const double *a, const double *b, unsigned int *flag, cudaStream_t s);
 int gm_check_blocks(int n);

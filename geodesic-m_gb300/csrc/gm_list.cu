@@ -100,10 +100,11 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
             nc[d] = (int)floor(span / wmin);
             if (nc[d] < 1) nc[d] = 1;
         }
-        // keep the cell count within the allocation by coarsening the grid
-        while ((long long)nc[0] * nc[1] * nc[2] > max_cells) {
-            for (int d = 0; d < 3; d++) nc[d] = nc[d] > 1 ? (nc[d] * 3) / 4 : 1;
-        }
+    }
+    // keep the cell count within the allocation by coarsening the grid
+    // (coarser cells only widen the 5x5x5 search, never miss a pair)
+    while ((long long)nc[0] * nc[1] * nc[2] > max_cells) {
+        for (int d = 0; d < 3; d++) nc[d] = nc[d] > 1 ? (nc[d] * 3) / 4 : 1;
     }
     for (int d = 0; d < 3; d++) {
         double span = periodic ? box[d] : -2.0 * lo[d];
@@ -113,8 +114,7 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
         g->inv_w[d] = (float)(1.0 / w[d]);
         g->full[d] = periodic && nc[d] < 5;
     }
-    g->ncell = nc[0] * nc[1] * nc[2];
-    if (g->ncell > max_cells) atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+    g->ncell = nc[0] * nc[1] * nc[2];  // <= max_cells by construction
     st->rebuild = 0;
     st->n_rebuilds += 1;
 }
@@ -126,7 +126,7 @@ __device__ __forceinline__ int cell_coord(float h, float lo, float inv_w, int nc
 }
 
 __global__ void assign_kernel(int n, const double *pos, double *ref, const GridInfo *g, int *cell_of,
-                              int *cell_count) {
+                              int *cell_count, int max_cells, DevStatus *st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int c3[3];
@@ -136,15 +136,19 @@ __global__ void assign_kernel(int n, const double *pos, double *ref, const GridI
         c3[d] = cell_coord((float)(x - g->origin[d]), g->lo[d], g->inv_w[d], g->nc[d]);
     }
     int c = (c3[2] * g->nc[1] + c3[1]) * g->nc[0] + c3[0];
+    if (c < 0 || c >= max_cells) {
+        atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+        c = 0;
+    }
     cell_of[i] = c;
     atomicAdd(&cell_count[c], 1);
 }
 
 // Exclusive scan of cell_count[0..ncell) into cell_start[0..ncell] (one block).
-__global__ void scan_kernel(const GridInfo *g, const int *cell_count, int *cell_start) {
+__global__ void scan_kernel(const GridInfo *g, const int *cell_count, int *cell_start, int max_cells) {
     __shared__ int warp_sums[32];
     __shared__ int carry;
-    const int ncell = g->ncell;
+    const int ncell = min(g->ncell, max_cells);
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (int base = 0; base < ncell; base += blockDim.x) {
@@ -383,8 +387,9 @@ void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
     cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)a.max_cells, s);
     cudaMemsetAsync(a.cell_cursor, 0, sizeof(int) * (size_t)a.max_cells, s);
     const int nb = (a.n + 255) / 256;
-    if (a.n > 0) assign_kernel<<<nb, 256, 0, s>>>(a.n, a.pos, a.ref, a.grid, a.cell_of, a.cell_count);
-    scan_kernel<<<1, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start);
+    if (a.n > 0)
+        assign_kernel<<<nb, 256, 0, s>>>(a.n, a.pos, a.ref, a.grid, a.cell_of, a.cell_count, a.max_cells, a.status);
+    scan_kernel<<<1, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start, a.max_cells);
     if (a.n > 0) {
         scatter_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.cell_cursor, a.tmp_atom);
         rank_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.tmp_atom, a.perm, a.cell_sorted, a.status);

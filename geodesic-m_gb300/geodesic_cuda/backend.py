@@ -145,10 +145,13 @@ def lib():
         L.gm_stream.restype = C.c_void_p
         L.gm_stream.argtypes = [C.c_void_p]
         L.gm_counters.argtypes = [C.c_void_p, P(C.c_int64), C.c_int64]
+        L.gm_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_double, P(C.c_double)]
+        L.gm_time_steps.argtypes = [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_void_p, C.c_int64,
+                                    P(C.c_double)]
         for f in ("gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
-                  "gm_forces_resident", "gm_synchronize", "gm_counters"):
+                  "gm_forces_resident", "gm_synchronize", "gm_counters", "gm_profile", "gm_time_steps"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -322,6 +325,22 @@ class CudaBackend:
     def synchronize(self):
         conv = GmConvergence()
         self._check(lib().gm_synchronize(self._h, C.byref(conv)), conv)
+
+    def profile(self, which: str, n_iter: int = 20, dt: float = 0.002) -> float:
+        """Average device milliseconds of one launch (CUDA events)."""
+        code = {"pair": 0, "bonded": 1, "rebuild": 2, "step": 3, "pack": 4}[which]
+        ms = C.c_double()
+        self._check(lib().gm_profile(self._h, code, n_iter, dt, C.byref(ms)))
+        return ms.value
+
+    def time_steps(self, dt: float, n_steps: int, first_step: int = 0, flush_ptr: int = 0,
+                   flush_bytes: int = 0) -> float:
+        """Sum of per-step device milliseconds over n_steps resident steps
+        (L2 flushed between steps when a flush buffer is given)."""
+        ms = C.c_double()
+        self._check(lib().gm_time_steps(self._h, dt, first_step, n_steps, C.c_void_p(flush_ptr or None),
+                                        flush_bytes, C.byref(ms)))
+        return ms.value
 
     def stream(self) -> int:
         return int(lib().gm_stream(self._h) or 0)

@@ -51,7 +51,7 @@ def _get():
 
 
 def generate(n_atoms: int, seed: int, h_fraction: float = 0.0, temperature: float = 300.0,
-             relax_iters: int = 60, n_threads: int = 0):
+             relax_iters: int = 300, n_threads: int = 0):
     """Returns (AtomData, BondedTopology, State, info dict)."""
     L = _get()
     nt = n_threads or min(os.cpu_count() or 1, 32)

@@ -8,7 +8,8 @@
  * (boustrophedon) path through the lattice, so path neighbours are lattice
  * neighbours.  Bonds: path pairs (k = 300 kcal/mol/A^2, r0 = ideal lattice
  * distance).  Angles: path triples (k = 50 kcal/mol/rad^2, theta0 = ideal
- * lattice angle).  Dihedrals: path quads (k = 1 kcal/mol, n = 3, delta = 0).
+ * lattice angle).  Dihedrals: path quads (k = 1 kcal/mol, n = 3, delta = 0;
+ * k = 0 where either lattice angle of the quad is straight).
  * Exclusions: 1-2, 1-3 and 1-4 path pairs (AMBER lists 1-4 pairs as
  * excluded; a scaled 1-4 term adds them back when enabled).  Nonbonded:
  * 8 types, sigma U[2.0, 3.8] A, epsilon U[0.02, 0.2] kcal/mol, mass
@@ -21,10 +22,14 @@
  * keep the serpentine chain.  H atoms get H-X-Y angles (k = 35) and the
  * matching 1-2/1-3 exclusions.
  *
- * Pre-relaxation: a fixed number of capped steepest-descent iterations in
- * FP64 (bonded terms plus LJ truncated at 5 A) removes the close contacts the
- * jitter creates; it is deterministic (gather per atom, fixed order) for any
- * thread count.  Everything derives from the 64-bit seed (splitmix64).
+ * Pre-relaxation: FIRE minimisation in FP64 of bonds, angles, the scaled 1-4
+ * pairs (LJ x 1/2, Coulomb x 1/1.2) and LJ + Coulomb with the quintic switch
+ * over [8, 10] A -- the MD potential without dihedrals (at most relax_iters iterations,
+ * stopping when the largest force is below 1 kcal/mol/A).  The lattice's
+ * sigma range is wide for its 2.15 A spacing, so without it the compression
+ * energy heats the system to thousands of kelvin and the droplet flies apart
+ * in vacuum.  Deterministic for any thread count (gather per atom, fixed
+ * order).  Everything derives from the 64-bit seed (splitmix64).
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -226,20 +231,64 @@ static double lattice_angle(const double a[3], const double b[3], const double c
 
 /* ----------------------------------------------------------- relaxation */
 
+/* FIRE minimisation (Bitzek et al., PRL 97, 170201 (2006)) of the MD
+ * potential without dihedrals: bonds, angles, scaled 1-4 pairs, and LJ plus
+ * Coulomb switched over [RELAX_SWITCH, RELAX_CUT].  Nonbonded pairs come from a Verlet list (cutoff +
+ * RELAX_SKIN, rebuilt when an atom moved RELAX_SKIN/2); each atom gathers its
+ * own neighbours in a fixed order, so the result does not depend on the
+ * thread count. */
+#define RELAX_SKIN 1.5
+#define COUL_K 332.0522173
+
 typedef struct {
     int64_t n;
-    const double *pos;
-    const double *sigma, *epsilon;
-    const int64_t *cell_start, *cell_atoms, *cell_of;
-    int nc[3];
-    double lo[3], w[3];
+    double rc, rs;  /* cutoff and switch onset of this stage */
+    const double *pos, *sigma, *epsilon, *charge;
+    const int64_t *nb_start;
+    const uint32_t *nb;
     double *force;
+    double *energy;   /* per thread */
     int64_t a0, a1;
-    const uint64_t *excl_keys;
-    int64_t n_excl;
-} lj_job;
+    int t;
+} nb_job;
 
-#define RELAX_CUT 5.0
+static void *nb_worker(void *arg) {
+    nb_job *J = (nb_job *)arg;
+    int64_t n = J->n;
+    const double *x = J->pos, *y = J->pos + n, *z = J->pos + 2 * n;
+    const double rc2 = J->rc * J->rc, RELAX_CUT = J->rc, RELAX_SWITCH = J->rs;
+    double e = 0.0;
+    for (int64_t i = J->a0; i < J->a1; i++) {
+        double f[3] = {0, 0, 0};
+        for (int64_t m = J->nb_start[i]; m < J->nb_start[i + 1]; m++) {
+            uint32_t j = J->nb[m];
+            double dx = x[j] - x[i], dy = y[j] - y[i], dz = z[j] - z[i];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 > rc2 || r2 == 0.0) continue;
+            /* the MD potential: LJ + Coulomb, quintic switch over [8, 10] A */
+            double sg = 0.5 * (J->sigma[i] + J->sigma[j]);
+            double ep = sqrt(J->epsilon[i] * J->epsilon[j]);
+            double r = sqrt(r2);
+            double s2 = sg * sg / r2, s6 = s2 * s2 * s2;
+            double qq = COUL_K * J->charge[i] * J->charge[j];
+            double v = 4.0 * ep * (s6 * s6 - s6) + qq / r;
+            double fr = 24.0 * ep * (2.0 * s6 * s6 - s6) / r + qq / r2;   /* F_r */
+            if (r > RELAX_SWITCH) {
+                double u = (r - RELAX_SWITCH) / (RELAX_CUT - RELAX_SWITCH), u2 = u * u;
+                double sw = 1.0 - 10.0 * u2 * u + 15.0 * u2 * u2 - 6.0 * u2 * u2 * u;
+                double dsw = -30.0 * u2 * (1.0 - u) * (1.0 - u) / (RELAX_CUT - RELAX_SWITCH);
+                fr = fr * sw - v * dsw;
+                v *= sw;
+            }
+            fr /= r;
+            e += 0.5 * v;
+            f[0] -= fr * dx; f[1] -= fr * dy; f[2] -= fr * dz;
+        }
+        J->force[i] += f[0]; J->force[n + i] += f[1]; J->force[2 * n + i] += f[2];
+    }
+    J->energy[J->t] = e;
+    return NULL;
+}
 
 static int excluded(const uint64_t *keys, int64_t nk, uint32_t i, uint32_t j) {
     if (i > j) { uint32_t t = i; i = j; j = t; }
@@ -253,57 +302,107 @@ static int excluded(const uint64_t *keys, int64_t nk, uint32_t i, uint32_t j) {
     return 0;
 }
 
-static void *lj_worker(void *arg) {
-    lj_job *J = (lj_job *)arg;
-    int64_t n = J->n;
-    const double *x = J->pos, *y = J->pos + n, *z = J->pos + 2 * n;
-    double rc2 = RELAX_CUT * RELAX_CUT;
-    for (int64_t i = J->a0; i < J->a1; i++) {
-        int64_t c = J->cell_of[i];
-        int ci[3] = {(int)(c % J->nc[0]), (int)((c / J->nc[0]) % J->nc[1]), (int)(c / ((int64_t)J->nc[0] * J->nc[1]))};
-        double f[3] = {0, 0, 0};
-        for (int dz = -1; dz <= 1; dz++)
-            for (int dy = -1; dy <= 1; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
-                    if (cx < 0 || cy < 0 || cz < 0 || cx >= J->nc[0] || cy >= J->nc[1] || cz >= J->nc[2]) continue;
-                    int64_t cell = ((int64_t)cz * J->nc[1] + cy) * J->nc[0] + cx;
-                    for (int64_t m = J->cell_start[cell]; m < J->cell_start[cell + 1]; m++) {
-                        int64_t j = J->cell_atoms[m];
-                        if (j == i) continue;
-                        double ddx = x[j] - x[i], ddy = y[j] - y[i], ddz = z[j] - z[i];
-                        double r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                        if (r2 > rc2 || r2 == 0.0) continue;
-                        if (excluded(J->excl_keys, J->n_excl, (uint32_t)i, (uint32_t)j)) continue;
-                        double sg = 0.5 * (J->sigma[i] + J->sigma[j]);
-                        double ep = sqrt(J->epsilon[i] * J->epsilon[j]);
-                        double s2 = sg * sg / r2, s6 = s2 * s2 * s2;
-                        double fr = 24.0 * ep * (2.0 * s6 * s6 - s6) / r2;
-                        f[0] -= fr * ddx; f[1] -= fr * ddy; f[2] -= fr * ddz;
-                    }
-                }
-        J->force[i] += f[0]; J->force[n + i] += f[1]; J->force[2 * n + i] += f[2];
-    }
-    return NULL;
-}
-
 static int cmp64(const void *a, const void *b) {
     uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
     return (x > y) - (x < y);
 }
 
-static void bonded_relax_forces(int64_t n, const double *p, const gs_sizes *S, const gs_out *o, double *F) {
+/* full Verlet list within RELAX_CUT + RELAX_SKIN, exclusions removed */
+static void build_verlet(int64_t n, const double *pos, const uint64_t *keys, int64_t nk, int64_t **start_out,
+                         uint32_t **nb_out, int64_t *cap, double rc) {
+    const double rl = rc + RELAX_SKIN, rl2 = rl * rl;
+    double lo[3], hi[3], w[3];
+    int nc[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = INFINITY; hi[d] = -INFINITY;
+        for (int64_t i = 0; i < n; i++) { double v = pos[d * n + i]; if (v < lo[d]) lo[d] = v; if (v > hi[d]) hi[d] = v; }
+        nc[d] = (int)floor((hi[d] - lo[d]) / (rl * 1.001));
+        if (nc[d] < 1) nc[d] = 1;
+        if (nc[d] > 256) nc[d] = 256;
+        w[d] = (hi[d] - lo[d]) / nc[d];
+        if (w[d] <= 0) w[d] = 1.0;
+    }
+    int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];
+    int64_t *cs = (int64_t *)calloc((size_t)ncell + 1, sizeof(int64_t));
+    int64_t *cof = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    int64_t *cat = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        int c3[3];
+        for (int d = 0; d < 3; d++) {
+            int c = (int)floor((pos[d * n + i] - lo[d]) / w[d]);
+            c3[d] = c < 0 ? 0 : (c >= nc[d] ? nc[d] - 1 : c);
+        }
+        cof[i] = ((int64_t)c3[2] * nc[1] + c3[1]) * nc[0] + c3[0];
+        cs[cof[i] + 1]++;
+    }
+    for (int64_t c = 0; c < ncell; c++) cs[c + 1] += cs[c];
+    int64_t *cur = (int64_t *)malloc(sizeof(int64_t) * (size_t)ncell);
+    memcpy(cur, cs, sizeof(int64_t) * (size_t)ncell);
+    for (int64_t i = 0; i < n; i++) cat[cur[cof[i]]++] = i;  /* ascending i within a cell */
+    free(cur);
+    int64_t *start = *start_out;
+    uint32_t *nb = *nb_out;
+    int64_t used = 0;
+    for (int64_t i = 0; i < n; i++) {
+        start[i] = used;
+        int64_t c = cof[i];
+        int ci[3] = {(int)(c % nc[0]), (int)((c / nc[0]) % nc[1]), (int)(c / ((int64_t)nc[0] * nc[1]))};
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
+                    if (cx < 0 || cy < 0 || cz < 0 || cx >= nc[0] || cy >= nc[1] || cz >= nc[2]) continue;
+                    int64_t cell = ((int64_t)cz * nc[1] + cy) * nc[0] + cx;
+                    for (int64_t m = cs[cell]; m < cs[cell + 1]; m++) {
+                        int64_t j = cat[m];
+                        if (j == i) continue;
+                        double ddx = pos[j] - pos[i], ddy = pos[n + j] - pos[n + i], ddz = pos[2 * n + j] - pos[2 * n + i];
+                        if (ddx * ddx + ddy * ddy + ddz * ddz > rl2) continue;
+                        if (nk && excluded(keys, nk, (uint32_t)i, (uint32_t)j)) continue;
+                        if (used == *cap) {
+                            *cap = *cap * 2 + 1024;
+                            nb = (uint32_t *)realloc(nb, sizeof(uint32_t) * (size_t)*cap);
+                        }
+                        nb[used++] = (uint32_t)j;
+                    }
+                }
+    }
+    start[n] = used;
+    *nb_out = nb;
+    free(cs); free(cof); free(cat);
+}
+
+static double bonded_relax_forces(int64_t n, const double *p, const gs_sizes *S, const gs_out *o, double *F) {
     const double *x = p, *y = p + n, *z = p + 2 * n;
+    double e = 0.0;
+    /* 1-4 path pairs are excluded from the nonbonded list but interact
+     * through the scaled 1-4 term (LJ x 1/2); at serpentine U-turns they are
+     * lattice neighbours, so the relaxation must keep them apart too */
+    for (int64_t d = 0; d < S->n_diheds; d++) {
+        uint32_t i = o->dihed_i[d], j = o->dihed_l[d];
+        double dd[3] = {x[j] - x[i], y[j] - y[i], z[j] - z[i]};
+        double r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+        if (r2 == 0.0) continue;
+        double sg = 0.5 * (o->sigma[i] + o->sigma[j]), ep = sqrt(o->epsilon[i] * o->epsilon[j]);
+        double s2 = sg * sg / r2, s6 = s2 * s2 * s2;
+        double qq = COUL_K * o->charge[i] * o->charge[j] / 1.2;
+        double r = sqrt(r2);
+        double fr = 0.5 * 24.0 * ep * (2.0 * s6 * s6 - s6) / r2 + qq / (r2 * r);
+        e += 0.5 * 4.0 * ep * (s6 * s6 - s6) + qq / r;
+        for (int c = 0; c < 3; c++) { F[c * n + i] -= fr * dd[c]; F[c * n + j] += fr * dd[c]; }
+    }
     for (int64_t b = 0; b < S->n_bonds; b++) {
         uint32_t i = o->bond_i[b], j = o->bond_j[b];
         double d[3] = {x[j] - x[i], y[j] - y[i], z[j] - z[i]};
         double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
         if (r == 0) continue;
         double g = 2.0 * o->bond_k[b] * (r - o->bond_r0[b]) / r;
+        e += o->bond_k[b] * (r - o->bond_r0[b]) * (r - o->bond_r0[b]);
         for (int c = 0; c < 3; c++) { F[c * n + i] += g * d[c]; F[c * n + j] -= g * d[c]; }
     }
     for (int64_t a = 0; a < S->n_angles; a++) {
         uint32_t i = o->angle_i[a], j = o->angle_j[a], k = o->angle_k[a];
+        if (o->angle_kth[a] == 0.0) continue;
         double b1[3] = {x[i] - x[j], y[i] - y[j], z[i] - z[j]}, b2[3] = {x[k] - x[j], y[k] - y[j], z[k] - z[j]};
         double r1 = sqrt(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
         double r2 = sqrt(b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2]);
@@ -313,17 +412,20 @@ static void bonded_relax_forces(int64_t n, const double *p, const gs_sizes *S, c
         if (ct < -1) ct = -1;
         double st = sqrt(1 - ct * ct);
         if (st < 1e-3) st = 1e-3;
-        double g = 2.0 * o->angle_kth[a] * (acos(ct) - o->angle_th0[a]) / st;
+        double dth = acos(ct) - o->angle_th0[a];
+        e += o->angle_kth[a] * dth * dth;
+        double g = 2.0 * o->angle_kth[a] * dth / st;
         for (int c = 0; c < 3; c++) {
             double fi = g * (b2[c] / (r1 * r2) - ct * b1[c] / (r1 * r1));
             double fk = g * (b1[c] / (r1 * r2) - ct * b2[c] / (r2 * r2));
             F[c * n + i] += fi; F[c * n + k] += fk; F[c * n + j] -= fi + fk;
         }
     }
+    return e;
 }
 
-static double relax(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, int iters, int n_threads,
-                    double *max_before) {
+static double relax_stage(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, int iters, int n_threads,
+                          double rc, double rs, double ftol, double *max_before) {
     int64_t nk = S->n_excl;
     uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(nk > 0 ? nk : 1));
     for (int64_t e = 0; e < nk; e++) {
@@ -332,76 +434,86 @@ static double relax(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, 
         keys[e] = ((uint64_t)i << 32) | j;
     }
     qsort(keys, (size_t)nk, sizeof(uint64_t), cmp64);
-    double *F = (double *)malloc(sizeof(double) * 3 * (size_t)n);
-    int64_t *cell_of = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
-    int64_t *cell_atoms = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
-    double maxf = 0.0;
     if (n_threads < 1) n_threads = 1;
+    double *F = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *V = (double *)calloc(3 * (size_t)n, sizeof(double));
+    double *ref = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    int64_t *start = (int64_t *)malloc(sizeof(int64_t) * ((size_t)n + 1));
+    int64_t cap = n * 640 + 1024;
+    uint32_t *nb = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)cap);
+    double *eth = (double *)calloc((size_t)n_threads, sizeof(double));
+    nb_job *jobs = (nb_job *)malloc(sizeof(nb_job) * (size_t)n_threads);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)n_threads);
+    build_verlet(n, pos, keys, nk, &start, &nb, &cap, rc);
+    memcpy(ref, pos, sizeof(double) * 3 * (size_t)n);
+    const double dt_max = 0.1, f_inc = 1.1, f_dec = 0.5, a_start = 0.1, f_a = 0.99, max_step = 0.1;
+    double dt = 0.01, alpha = a_start, maxf = 0.0;
+    int n_pos = 0;
     for (int it = 0; it <= iters; it++) {
-        double lo[3], hi[3], w[3];
-        int nc[3];
-        for (int d = 0; d < 3; d++) {
-            lo[d] = INFINITY; hi[d] = -INFINITY;
-            for (int64_t i = 0; i < n; i++) { double v = pos[d * n + i]; if (v < lo[d]) lo[d] = v; if (v > hi[d]) hi[d] = v; }
-            nc[d] = (int)floor((hi[d] - lo[d]) / (RELAX_CUT * 1.001));
-            if (nc[d] < 1) nc[d] = 1;
-            w[d] = (hi[d] - lo[d]) / nc[d];
-            if (w[d] <= 0) w[d] = 1.0;
-        }
-        int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];
-        int64_t *cs = (int64_t *)calloc((size_t)ncell + 1, sizeof(int64_t));
+        /* rebuild the list once an atom moved half the skin */
+        double dmax = 0.0;
         for (int64_t i = 0; i < n; i++) {
-            int c3[3];
-            for (int d = 0; d < 3; d++) {
-                int c = (int)floor((pos[d * n + i] - lo[d]) / w[d]);
-                if (c < 0) c = 0;
-                if (c >= nc[d]) c = nc[d] - 1;
-                c3[d] = c;
-            }
-            cell_of[i] = ((int64_t)c3[2] * nc[1] + c3[1]) * nc[0] + c3[0];
-            cs[cell_of[i] + 1]++;
+            double dx = pos[i] - ref[i], dy = pos[n + i] - ref[n + i], dz = pos[2 * n + i] - ref[2 * n + i];
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > dmax) dmax = d2;
         }
-        for (int64_t c = 0; c < ncell; c++) cs[c + 1] += cs[c];
-        int64_t *cur = (int64_t *)malloc(sizeof(int64_t) * (size_t)ncell);
-        memcpy(cur, cs, sizeof(int64_t) * (size_t)ncell);
-        for (int64_t i = 0; i < n; i++) cell_atoms[cur[cell_of[i]]++] = i;
-        free(cur);
+        if (dmax > 0.25 * RELAX_SKIN * RELAX_SKIN) {
+            build_verlet(n, pos, keys, nk, &start, &nb, &cap, rc);
+            memcpy(ref, pos, sizeof(double) * 3 * (size_t)n);
+        }
         memset(F, 0, sizeof(double) * 3 * (size_t)n);
         bonded_relax_forces(n, pos, S, o, F);
-        lj_job *jobs = (lj_job *)malloc(sizeof(lj_job) * (size_t)n_threads);
-        pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)n_threads);
         int64_t chunk = (n + n_threads - 1) / n_threads;
         for (int t = 0; t < n_threads; t++) {
-            lj_job J = {n, pos, o->sigma, o->epsilon, cs, cell_atoms, cell_of, {nc[0], nc[1], nc[2]},
-                        {lo[0], lo[1], lo[2]}, {w[0], w[1], w[2]}, F, t * chunk, (t + 1) * chunk, keys, nk};
+            nb_job J = {n, rc, rs, pos, o->sigma, o->epsilon, o->charge, start, nb, F, eth, t * chunk, (t + 1) * chunk, t};
             if (J.a0 > n) J.a0 = n;
             if (J.a1 > n) J.a1 = n;
             jobs[t] = J;
-            if (t > 0) pthread_create(&th[t], NULL, lj_worker, &jobs[t]);
+            if (t > 0) pthread_create(&th[t], NULL, nb_worker, &jobs[t]);
         }
-        lj_worker(&jobs[0]);
+        nb_worker(&jobs[0]);
         for (int t = 1; t < n_threads; t++) pthread_join(th[t], NULL);
-        free(jobs); free(th); free(cs);
         maxf = 0.0;
+        double P = 0.0, fn = 0.0, vn = 0.0;
+        for (int64_t i = 0; i < 3 * n; i++) { P += F[i] * V[i]; fn += F[i] * F[i]; vn += V[i] * V[i]; }
         for (int64_t i = 0; i < n; i++) {
             double f2 = F[i] * F[i] + F[n + i] * F[n + i] + F[2 * n + i] * F[2 * n + i];
             if (f2 > maxf) maxf = f2;
         }
         maxf = sqrt(maxf);
         if (it == 0 && max_before) *max_before = maxf;
-        if (it == iters) break;
-        /* capped steepest descent: step along F, at most 0.05 A per atom */
-        const double alpha = 2e-4, cap = 0.05;
+        if (it == iters || maxf < ftol) break;
+        /* FIRE velocity mixing and time-step control */
+        if (P > 0.0) {
+            double s = fn > 0 ? alpha * sqrt(vn / fn) : 0.0;
+            for (int64_t i = 0; i < 3 * n; i++) V[i] = (1.0 - alpha) * V[i] + s * F[i];
+            if (++n_pos > 5) { dt = dt * f_inc < dt_max ? dt * f_inc : dt_max; alpha *= f_a; }
+        } else {
+            memset(V, 0, sizeof(double) * 3 * (size_t)n);
+            dt *= f_dec;
+            alpha = a_start;
+            n_pos = 0;
+        }
         for (int64_t i = 0; i < n; i++) {
-            double f[3] = {F[i], F[n + i], F[2 * n + i]};
-            double fm = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-            double s = alpha;
-            if (fm * s > cap) s = cap / fm;
-            for (int d = 0; d < 3; d++) pos[d * n + i] += s * f[d];
+            double d[3];
+            double d2 = 0.0;
+            for (int c = 0; c < 3; c++) { V[c * n + i] += dt * F[c * n + i]; d[c] = dt * V[c * n + i]; d2 += d[c] * d[c]; }
+            double sc = d2 > max_step * max_step ? max_step / sqrt(d2) : 1.0;
+            for (int c = 0; c < 3; c++) pos[c * n + i] += sc * d[c];
         }
     }
-    free(F); free(cell_of); free(cell_atoms); free(keys);
+    free(F); free(V); free(ref); free(start); free(nb); free(eth); free(jobs); free(th); free(keys);
     return maxf;
+}
+
+/* Two stages: most iterations on the cheap 6 A switched potential, then a
+ * fifth of them on the full potential (switch 8 -> 10 A). */
+static double relax(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, int iters, int n_threads,
+                    double *max_before) {
+    if (iters <= 0) return relax_stage(n, pos, S, o, 0, n_threads, 10.0, 8.0, 1.0, max_before);
+    int polish = iters / 5 > 0 ? iters / 5 : 1;
+    relax_stage(n, pos, S, o, iters - polish, n_threads, 6.0, 4.0, 0.5, max_before);
+    return relax_stage(n, pos, S, o, polish, n_threads, 10.0, 8.0, 1.0, NULL);
 }
 
 /* ------------------------------------------------------------ generate */
@@ -495,9 +607,16 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
         }
     }
     for (int64_t k = 0; k + 3 < nh; k++) {
-        o->dihed_i[nd] = (uint32_t)L.heavy[k]; o->dihed_j[nd] = (uint32_t)L.heavy[k + 1];
-        o->dihed_k[nd] = (uint32_t)L.heavy[k + 2]; o->dihed_l[nd] = (uint32_t)L.heavy[k + 3];
-        o->dihed_kphi[nd] = 1.0; o->dihed_n[nd] = 3; o->dihed_delta[nd] = 0.0; nd++;
+        const int64_t a0 = L.heavy[k], a1 = L.heavy[k + 1], a2 = L.heavy[k + 2], a3 = L.heavy[k + 3];
+        o->dihed_i[nd] = (uint32_t)a0; o->dihed_j[nd] = (uint32_t)a1;
+        o->dihed_k[nd] = (uint32_t)a2; o->dihed_l[nd] = (uint32_t)a3;
+        /* a torsion about a straight (180 deg) lattice angle is undefined and
+         * the cross-product forces diverge as the angle fluctuates through
+         * 180 deg: such quads stay in the topology with zero barrier */
+        const double t1 = lattice_angle(&ideal[3 * a0], &ideal[3 * a1], &ideal[3 * a2]);
+        const double t2 = lattice_angle(&ideal[3 * a1], &ideal[3 * a2], &ideal[3 * a3]);
+        const int straight = t1 > M_PI - 0.2 || t2 > M_PI - 0.2;
+        o->dihed_kphi[nd] = straight ? 0.0 : 1.0; o->dihed_n[nd] = 3; o->dihed_delta[nd] = 0.0; nd++;
     }
     for (int sep = 1; sep <= 3; sep++)
         for (int64_t k = 0; k + sep < nh; k++) {

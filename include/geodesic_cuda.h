@@ -150,7 +150,9 @@ int32_t gm_last_error(const gm_ctx *ctx, char *buf, int64_t len);
 
 /* ---- resident-state interface (benchmarks, batching) ------------------ */
 
-/* Uploads positions and velocities to the device state. */
+/* Uploads positions and velocities to the device state.  The neighbour list
+ * is kept (rebuilt later only if an atom moved more than half the skin), and
+ * the resident forces stay valid when the positions equal the resident ones. */
 int32_t gm_upload_state(gm_ctx *ctx, const double *px, const double *py, const double *pz,
                         const double *vx, const double *vy, const double *vz);
 /* Downloads positions and velocities from the device state. */
@@ -162,6 +164,16 @@ int32_t gm_run_resident(gm_ctx *ctx, double dt, uint64_t first_step, int64_t n_s
 int32_t gm_forces_resident(gm_ctx *ctx);
 /* Waits for the stream and reports device-side errors. */
 int32_t gm_synchronize(gm_ctx *ctx, gm_convergence *err);
+/* Average device time (ms, CUDA events on the context's stream) of one
+ * launch of: which = 0 the pair kernel, 1 the bonded kernel, 2 the list
+ * rebuild sequence, 3 one captured BAB step of length dt, 4 the pack kernel.
+ * Runs on the resident state; forces are recomputed afterwards. */
+int32_t gm_profile(gm_ctx *ctx, int32_t which, int32_t n_iter, double dt, double *avg_ms);
+/* Runs n_steps resident BAB steps, each bracketed by CUDA events; with
+ * flush_buf (a device buffer larger than L2) a memset of flush_bytes runs
+ * between steps, outside the bracketed time.  *total_ms = sum of step times. */
+int32_t gm_time_steps(gm_ctx *ctx, double dt, uint64_t first_step, int64_t n_steps, void *flush_buf,
+                      int64_t flush_bytes, double *total_ms);
 /* The context's cudaStream_t, for callers that time work on it. */
 void *gm_stream(gm_ctx *ctx);
 /* Counters: [0] pairs in the current list, [1] list rebuilds so far,

@@ -720,6 +720,24 @@ int64_t or_backend_build_neighbor_list(or_backend *b, double *px, double *py, do
     return b->n_pairs;
 }
 
+int64_t or_backend_set_pairs(or_backend *b, int64_t n_pairs, const uint32_t *pair_i, const uint32_t *pair_j,
+                             const double *px, const double *py, const double *pz) {
+    int64_t n = b->atoms.n;
+    if (n_pairs > b->cap) {
+        free(b->pair_i); free(b->pair_j);
+        b->cap = n_pairs;
+        b->pair_i = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
+        b->pair_j = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
+    }
+    memcpy(b->pair_i, pair_i, sizeof(uint32_t) * (size_t)n_pairs);
+    memcpy(b->pair_j, pair_j, sizeof(uint32_t) * (size_t)n_pairs);
+    b->n_pairs = n_pairs;
+    memcpy(b->ref, px, sizeof(double) * (size_t)n);
+    memcpy(b->ref + n, py, sizeof(double) * (size_t)n);
+    memcpy(b->ref + 2 * n, pz, sizeof(double) * (size_t)n);
+    return n_pairs;
+}
+
 int64_t or_backend_pairs(const or_backend *b, const uint32_t **pair_i, const uint32_t **pair_j) {
     *pair_i = b->pair_i;
     *pair_j = b->pair_j;

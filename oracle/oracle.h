@@ -150,6 +150,10 @@ void or_backend_free(or_backend *b);
 int32_t or_backend_n_threads(const or_backend *b);
 int64_t or_backend_build_neighbor_list(or_backend *b, double *px, double *py, double *pz);
 int64_t or_backend_pairs(const or_backend *b, const uint32_t **pair_i, const uint32_t **pair_j);
+/* Installs a pair list (and its build positions) without running the O(N^2)
+ * build; callers pass the reference's own pair set (e.g. from the cell path). */
+int64_t or_backend_set_pairs(or_backend *b, int64_t n_pairs, const uint32_t *pair_i, const uint32_t *pair_j,
+                             const double *px, const double *py, const double *pz);
 /* cpu_backend.rs:92-182: fills f* (reduced buffer) and returns the energy. */
 double or_backend_compute_forces(or_backend *b, const double *px, const double *py, const double *pz,
                                  double *fx, double *fy, double *fz);

@@ -113,6 +113,8 @@ def lib():
         L.or_backend_build_neighbor_list.argtypes = [C.c_void_p, _f64p, _f64p, _f64p]
         L.or_backend_pairs.restype = C.c_int64
         L.or_backend_pairs.argtypes = [C.c_void_p, P(_u32p), P(_u32p)]
+        L.or_backend_set_pairs.restype = C.c_int64
+        L.or_backend_set_pairs.argtypes = [C.c_void_p, C.c_int64, _u32p, _u32p, _f64p, _f64p, _f64p]
         L.or_backend_compute_forces.restype = C.c_double
         L.or_backend_compute_forces.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]
         L.or_backend_needs_rebuild.restype = C.c_int32
@@ -342,6 +344,12 @@ class CpuBackend:
         if cnt == 0:
             return np.zeros(0, np.uint32), np.zeros(0, np.uint32)
         return (np.ctypeslib.as_array(pi, shape=(cnt,)).copy(), np.ctypeslib.as_array(pj, shape=(cnt,)).copy())
+
+    def set_pairs(self, pair_i, pair_j, pos):
+        """Installs the given pair list (the reference's set) and build positions."""
+        pi, pj, p = _u32(pair_i), _u32(pair_j), _f64(pos)
+        lib().or_backend_set_pairs(self._h, len(pi), _p(pi, C.c_uint32), _p(pj, C.c_uint32),
+                                   *(_p(p[d], C.c_double) for d in range(3)))
 
     def compute_forces(self, pos):
         f = np.zeros((3, self.n))

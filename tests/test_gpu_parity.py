@@ -56,21 +56,38 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def nonbonded_only(topo):
+    """The topology with its bonded terms removed but its exclusions kept, so
+    compute_forces returns the nonbonded kernel's forces alone."""
+    t = amber.BondedTopology.empty()
+    t.excl_i, t.excl_j = topo.excl_i, topo.excl_j
+    return t
+
+
 @pytest.mark.parametrize("name", ["lj_pair", "water_box_4", "ala_dipeptide"])
 @pytest.mark.parametrize("precision", [backend.PRECISION_MIXED, backend.PRECISION_FP64])
 def test_fixture_forces_match_oracle(name, precision, load_fixture):
     """geodesic-gpu/tests/forces_gpu_vs_cpu.rs:7-64 on the same fixtures and
-    parameters (box 100 periodic, cutoff 12 / skin 14 / switch 10)."""
+    parameters (box 100 periodic, cutoff 12 / skin 14 / switch 10).  As in the
+    reference, the FP32 tolerance 1e-4 * max(|F|, 1) applies to the nonbonded
+    kernel (kernel_matches_cpu); full mixed-path forces (FP32 angle and
+    dihedral terms as well) must agree to 1e-5 globally and 1e-3 * max(|F|, 1)
+    per component.  The FP64 path meets 1e-10 * max(|F|, 1) everywhere."""
     atoms, topo, state = load_fixture(name)
     p = backend.SimParams(precision=precision, **FIX)
     r = both(atoms, topo, state.pos, p)
     assert_pairs_equal(r)
     assert np.array_equal(r["pos_g"], r["pos_r"])  # wrapped identically
     fg, fr = r["f_g"], r["f_r"]
-    tol = 1e-10 if precision == backend.PRECISION_FP64 else 1e-4
-    assert np.all(np.abs(fg - fr) <= tol * np.maximum(np.abs(fr), 1.0)), np.abs(fg - fr).max()
-    etol = 1e-10 if precision == backend.PRECISION_FP64 else 1e-5
-    assert abs(r["e_g"] - r["e_r"]) <= etol * max(abs(r["e_r"]), 1.0)
+    if precision == backend.PRECISION_FP64:
+        assert np.all(np.abs(fg - fr) <= 1e-10 * np.maximum(np.abs(fr), 1.0)), np.abs(fg - fr).max()
+        assert abs(r["e_g"] - r["e_r"]) <= 1e-10 * max(abs(r["e_r"]), 1.0)
+        return
+    assert rel_l2(fg, fr) <= 1e-5
+    assert np.all(np.abs(fg - fr) <= 1e-3 * np.maximum(np.abs(fr), 1.0)), np.abs(fg - fr).max()
+    assert abs(r["e_g"] - r["e_r"]) <= 1e-5 * max(abs(r["e_r"]), 1.0)
+    nb = both(atoms, nonbonded_only(topo), state.pos, p)
+    assert np.all(np.abs(nb["f_g"] - nb["f_r"]) <= 1e-4 * np.maximum(np.abs(nb["f_r"]), 1.0))
 
 
 def test_lj_pair_pin():
