@@ -822,7 +822,7 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     TRY(dalloc(c, &c->d_cell_start, (size_t)c->max_cells + 1));
     TRY(dalloc(c, &c->d_grid, 1));
     c->bbox_blocks = std::max(1, std::min(256, (n + 255) / 256));
-    TRY(dalloc(c, &c->d_bbox, 6 * (size_t)c->bbox_blocks));
+    TRY(dalloc(c, &c->d_bbox, 9 * (size_t)c->bbox_blocks));
     c->n_groups = (n + 31) / 32;
     TRY(dalloc(c, &c->d_count, (size_t)c->n_groups * 32));
     TRY(dalloc(c, &c->d_gmax, (size_t)c->n_groups));

@@ -64,7 +64,10 @@ pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__r
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 <= rc2 && r2 > 0.f) {
                     const float2 p = trow[__float_as_int(jh.w)];
-                    const float rinv = rsqrtf(r2);
+                    // rsqrtf plus one Newton step: the pair sums cancel to
+                    // small net forces, so the last ulps of 1/r matter
+                    float rinv = rsqrtf(r2);
+                    rinv = fmaf(0.5f * rinv, fmaf(-r2 * rinv, rinv, 1.0f), rinv);
                     const float rinv2 = rinv * rinv;
                     const float s2 = p.x * rinv2;
                     const float s6 = s2 * s2 * s2;
@@ -246,13 +249,19 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         const V3<T> b1 = diff<T>(a.pos, n, i, j), b2 = diff<T>(a.pos, n, kk, j);
         const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
         if (r1 != (T)0 && r2 != (T)0) {
-            T c = dot(b1, b2) / (r1 * r2);
-            c = c < (T)-1 ? (T)-1 : (c > (T)1 ? (T)1 : c);
-            T sn = sqrt((T)1 - c * c);
+            // theta - theta0 in FP64 in both paths: an FP32 acos is off by
+            // ~1e-7 rad, i.e. ~1e-5 kcal/mol/A at k = 50, which a structure
+            // near equilibrium cannot absorb
+            const V3<double> d1 = diff<double>(a.pos, n, i, j), d2 = diff<double>(a.pos, n, kk, j);
+            double c64 = dot(d1, d2) / sqrt(dot(d1, d1) * dot(d2, d2));
+            c64 = c64 < -1.0 ? -1.0 : (c64 > 1.0 ? 1.0 : c64);
+            const T c = (T)c64;
+            T sn = (T)sqrt(1.0 - c64 * c64);
             sn = sn > (T)1e-8 ? sn : (T)1e-8;
-            const T th = gm_acos(c);
-            const T k = (T)a.angle_kth[q], th0 = (T)a.angle_th0[q];
-            e = (double)(k * (th - th0) * (th - th0));
+            const double dth = acos(c64) - a.angle_th0[q];
+            const T k = (T)a.angle_kth[q];
+            e = a.angle_kth[q] * dth * dth;
+            const T th = (T)dth, th0 = (T)0;
             const T aa = (T)2 * k * (th - th0) / sn;
             const T ir12 = (T)1 / (r1 * r2), ir11 = (T)1 / (r1 * r1), ir22 = (T)1 / (r2 * r2);
             const V3<T> fi = {aa * (b2.x * ir12 - c * b1.x * ir11), aa * (b2.y * ir12 - c * b1.y * ir11),

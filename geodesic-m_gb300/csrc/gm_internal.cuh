@@ -113,7 +113,7 @@ struct ListArgs {
     DevStatus *status;
     double r_list, box[3];
     int periodic;
-    double *bbox_scratch;    // 6 * blocks
+    double *bbox_scratch;    // 9 * blocks (min, max, sum per dimension)
     int bbox_blocks;
 };
 

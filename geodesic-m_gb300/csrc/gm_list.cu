@@ -37,32 +37,38 @@ __global__ void wrap_kernel(int n, double *pos, double b0, double b1, double b2)
     pos[2 * n + i] = exact_wrap(pos[2 * n + i], b2);
 }
 
+// Per block: min x,y,z, max x,y,z and the sum x,y,z of the positions.
 __global__ void bbox_kernel(int n, const double *pos, double *partial) {
-    // per block: min x,y,z then max x,y,z
-    __shared__ double sm[6][256];
-    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    __shared__ double sm[9][256];
+    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX}, sum[3] = {0, 0, 0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         for (int d = 0; d < 3; d++) {
             double v = pos[d * n + i];
             mn[d] = fmin(mn[d], v);
             mx[d] = fmax(mx[d], v);
+            if (v == v) sum[d] += v;
         }
     }
-    for (int d = 0; d < 3; d++) { sm[d][threadIdx.x] = mn[d]; sm[3 + d][threadIdx.x] = mx[d]; }
+    for (int d = 0; d < 3; d++) {
+        sm[d][threadIdx.x] = mn[d];
+        sm[3 + d][threadIdx.x] = mx[d];
+        sm[6 + d][threadIdx.x] = sum[d];
+    }
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s)
             for (int d = 0; d < 3; d++) {
                 sm[d][threadIdx.x] = fmin(sm[d][threadIdx.x], sm[d][threadIdx.x + s]);
                 sm[3 + d][threadIdx.x] = fmax(sm[3 + d][threadIdx.x], sm[3 + d][threadIdx.x + s]);
+                sm[6 + d][threadIdx.x] += sm[6 + d][threadIdx.x + s];
             }
         __syncthreads();
     }
-    if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = sm[threadIdx.x][0];
+    if (threadIdx.x < 9) partial[blockIdx.x * 9 + threadIdx.x] = sm[threadIdx.x][0];
 }
 
 __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevStatus *st, double r_list,
-                            double b0, double b1, double b2, int periodic, int max_cells) {
+                            double b0, double b1, double b2, int periodic, int max_cells, int n_atoms) {
     if (threadIdx.x != 0) return;
     const double box[3] = {b0, b1, b2};
     const double wmin = r_list * 0.5 * (1.0 + 1e-5) + 1e-6;
@@ -81,23 +87,33 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
             lo[d] = -0.5 * box[d];
         }
     } else {
-        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX}, sum[3] = {0, 0, 0};
         for (int b = 0; b < blocks; b++)
             for (int d = 0; d < 3; d++) {
-                mn[d] = fmin(mn[d], partial[b * 6 + d]);
-                mx[d] = fmax(mx[d], partial[b * 6 + 3 + d]);
+                mn[d] = fmin(mn[d], partial[b * 9 + d]);
+                mx[d] = fmax(mx[d], partial[b * 9 + 3 + d]);
+                sum[d] += partial[b * 9 + 6 + d];
             }
+        // The grid covers a core cube around the mean position, at the finest
+        // cell width the allocation allows; atoms outside it (evaporated atoms
+        // of a droplet in vacuum) are clamped into the edge cells.  Clamping is
+        // 1-Lipschitz on cell indices, so the 5x5x5 stencil still finds every
+        // pair, and a few outliers no longer coarsen the whole grid.
+        const int per_dim = (int)floor(cbrt((double)max_cells));
         for (int d = 0; d < 3; d++) {
             double ext = mx[d] - mn[d];
-            if (!(ext == ext) || mx[d] < mn[d]) { ext = 0.0; mn[d] = mx[d] = 0.0; }
+            if (!(ext == ext) || mx[d] < mn[d]) { ext = 0.0; mn[d] = mx[d] = 0.0; sum[d] = 0.0; }
             // min-image of the reference folds pairs farther apart than box/2;
             // the cell search assumes it never does
             if (ext + r_list >= 0.5 * box[d]) atomicOr(&st->error, (unsigned)GM_DEV_EXTENT);
-            const double pad = 1e-3 * (1.0 + ext);
-            g->origin[d] = 0.5 * (mx[d] + mn[d]);
-            lo[d] = (mn[d] - g->origin[d]) - pad;
-            double span = ext + 2.0 * pad;
-            nc[d] = (int)floor(span / wmin);
+            const double mean = n_atoms > 0 ? sum[d] / n_atoms : 0.0;
+            const double half = 0.5 * per_dim * wmin;
+            double a = fmax(mn[d], mean - half), b = fmin(mx[d], mean + half);
+            if (!(b >= a)) { a = mn[d]; b = mx[d]; }
+            const double pad = 1e-3 * (1.0 + (b - a));
+            g->origin[d] = 0.5 * (a + b);
+            lo[d] = (a - g->origin[d]) - pad;
+            nc[d] = (int)floor((b - a + 2.0 * pad) / wmin);
             if (nc[d] < 1) nc[d] = 1;
         }
     }
@@ -380,7 +396,7 @@ void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s) {
 void gm_launch_grid(const ListArgs &a, cudaStream_t s) {
     if (!a.periodic && a.n > 0) bbox_kernel<<<a.bbox_blocks, 256, 0, s>>>(a.n, a.pos, a.bbox_scratch);
     grid_kernel<<<1, 32, 0, s>>>(a.bbox_scratch, a.periodic || a.n == 0 ? 0 : a.bbox_blocks, a.grid, a.status,
-                                 a.r_list, a.box[0], a.box[1], a.box[2], a.periodic, a.max_cells);
+                                 a.r_list, a.box[0], a.box[1], a.box[2], a.periodic, a.max_cells, a.n);
 }
 
 void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
