@@ -57,6 +57,7 @@ struct gm_ctx {
     int *d_perm = nullptr, *d_cell_of = nullptr, *d_cell_sorted = nullptr, *d_cell_count = nullptr,
         *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr;
     int max_cells = 0;
+    int *d_scan = nullptr;
     GridInfo *d_grid = nullptr;
     double *d_bbox = nullptr;
     int bbox_blocks = 0;
@@ -95,6 +96,7 @@ struct gm_ctx {
     int graph_cap = -1;
     long long launches_per_step = 0;
     bool forces_current = false;
+    bool use_graph = true;           // GM_GRAPH=0: direct launches (profilers)
     long long rebuild_base = 0;
     unsigned last_shake_T = 0, last_rattle_T = 0;
 };
@@ -197,6 +199,7 @@ ListArgs list_args(gm_ctx *c) {
     a.periodic = c->p.periodic;
     a.bbox_scratch = c->d_bbox;
     a.bbox_blocks = c->bbox_blocks;
+    a.scan_scratch = c->d_scan;
     return a;
 }
 
@@ -281,7 +284,9 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s) {
     gm_launch_bin(a, s);
     gm_launch_pack(a, c->fp64, s);
     gm_launch_build(a, s);
-    return (a.periodic ? 1 : 0) + (a.periodic ? 1 : 2) + 4 + 2;  // + 2 memsets
+    // wrap or bbox, grid, assign, 3 scan kernels, scatter, rank, pack, build
+    // (the two memsets are copy-engine work, not kernels)
+    return 10 + (a.periodic || a.n > 0 ? 1 : 0);
 }
 
 int seq_forces(gm_ctx *c, cudaStream_t s) {
@@ -530,6 +535,22 @@ int capture_graph(gm_ctx *c, double dt) {
     return GM_OK;
 }
 
+// The step without a graph: same kernels on the stream, the rebuild decision
+// read back on the host after each check (profilers cannot look inside
+// graphs that hold conditional nodes).
+int run_direct(gm_ctx *c, double dt, int64_t n_steps) {
+    for (int64_t k = 0; k < n_steps; k++) {
+        long long count = 0;
+        issue_step(c, c->stream, dt, 0ull, &count);
+        int rc = st_read(c);
+        if (rc) return rc;
+        if (c->h_status->rebuild && !c->h_status->error) count += seq_rebuild(c, c->stream);
+        issue_step_tail(c, c->stream, dt, &count);
+        c->launches += count;
+    }
+    return GM_OK;
+}
+
 int ensure_forces(gm_ctx *c) {
     // the first half-kick of a step needs forces at the current positions;
     // an existing list stays valid while no atom moved more than half the
@@ -638,6 +659,10 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     c->p = p;
     c->n = (int)atoms->n_atoms;
     c->fp64 = p.precision == GM_PRECISION_FP64;
+    {
+        const char *g = getenv("GM_GRAPH");
+        c->use_graph = !(g && g[0] == '0');
+    }
     const int n = c->n;
     auto bail = [&](int code) -> gm_ctx * {
         // no context survives to carry the message: report it on stderr
@@ -816,7 +841,10 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     TRY(dalloc(c, &c->d_cell_of, (size_t)n));
     TRY(dalloc(c, &c->d_cell_sorted, (size_t)n));
     TRY(dalloc(c, &c->d_tmp_atom, (size_t)n));
-    c->max_cells = std::max(2 * n, 4096);
+    // cell budget: a few cells per atom, at least 2^20 (the grid of a swollen
+    // droplet in vacuum stays fine-grained); 12 bytes per cell
+    c->max_cells = (int)std::min<long long>(std::max<long long>(8LL * n, 1LL << 20), 1LL << 27);
+    TRY(dalloc(c, &c->d_scan, (size_t)(c->max_cells + 1 + 1023) / 1024 + 1));
     TRY(dalloc(c, &c->d_cell_count, (size_t)c->max_cells));
     TRY(dalloc(c, &c->d_cell_cursor, (size_t)c->max_cells));
     TRY(dalloc(c, &c->d_cell_start, (size_t)c->max_cells + 1));
@@ -1079,7 +1107,7 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
     GM_CUDA(c, cudaSetDevice(c->device));
     int rc = ensure_forces(c);
     if (rc) return rc;
-    if (which == 3) {
+    if (which == 3 && c->use_graph) {
         rc = capture_graph(c, dt);
         if (rc) return rc;
     }
@@ -1095,7 +1123,10 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
             case 0: gm_launch_pair(fa, c->fp64, c->stream); break;
             case 1: gm_launch_bonded(fa, c->fp64, c->stream); break;
             case 2: seq_rebuild(c, c->stream); break;
-            case 3: cudaGraphLaunch(c->graph_exec, c->stream); break;
+            case 3:
+                if (c->use_graph) cudaGraphLaunch(c->graph_exec, c->stream);
+                else run_direct(c, dt, 1);
+                break;
             default: gm_launch_pack(la, c->fp64, c->stream); break;
         }
         cudaEventRecord(e1, c->stream);
@@ -1144,6 +1175,7 @@ int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_ste
     if (rc) return rc;
     rc = ensure_forces(c);
     if (rc) return rc;
+    if (!c->use_graph) return run_direct(c, dt, n_steps);
     rc = capture_graph(c, dt);
     if (rc) return rc;
     for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
@@ -1158,7 +1190,7 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
     int rc = reset_status(c);
     if (!rc) rc = set_step(c, first_step);
     if (!rc) rc = ensure_forces(c);
-    if (!rc) rc = capture_graph(c, dt);
+    if (!rc && c->use_graph) rc = capture_graph(c, dt);
     if (rc) return rc;
     std::vector<cudaEvent_t> ev((size_t)(2 * n_steps));
     for (auto &e : ev) GM_CUDA(c, cudaEventCreate(&e));
@@ -1166,13 +1198,18 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
         GM_CUDA(c, cudaMemsetAsync(flush_buf, 0, (size_t)flush_bytes, c->stream));
     for (int64_t k = 0; k < n_steps; k++) {
         GM_CUDA(c, cudaEventRecord(ev[(size_t)(2 * k)], c->stream));
-        GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        if (c->use_graph) {
+            GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        } else {
+            rc = run_direct(c, dt, 1);
+            if (rc) return rc;
+        }
         GM_CUDA(c, cudaEventRecord(ev[(size_t)(2 * k + 1)], c->stream));
         // evict the step's working set so every timed step starts from HBM
         if (flush_buf && flush_bytes > 0)
             GM_CUDA(c, cudaMemsetAsync(flush_buf, (int)((k + 1) & 0xff), (size_t)flush_bytes, c->stream));
     }
-    c->launches += c->launches_per_step * n_steps;
+    if (c->use_graph) c->launches += c->launches_per_step * n_steps;
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     double total = 0.0;
     for (int64_t k = 0; k < n_steps; k++) {

@@ -114,6 +114,7 @@ struct ListArgs {
     double r_list, box[3];
     int periodic;
     double *bbox_scratch;    // 9 * blocks (min, max, sum per dimension)
+    int *scan_scratch;       // one total per 1024 cells
     int bbox_blocks;
 };
 

@@ -160,41 +160,66 @@ __global__ void assign_kernel(int n, const double *pos, double *ref, const GridI
     atomicAdd(&cell_count[c], 1);
 }
 
-// Exclusive scan of cell_count[0..ncell) into cell_start[0..ncell] (one block).
-__global__ void scan_kernel(const GridInfo *g, const int *cell_count, int *cell_start, int max_cells) {
-    __shared__ int warp_sums[32];
-    __shared__ int carry;
-    const int ncell = min(g->ncell, max_cells);
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < ncell; base += blockDim.x) {
-        int i = base + threadIdx.x;
-        int v = i < ncell ? cell_count[i] : 0;
-        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        int x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) warp_sums[w] = x;
-        __syncthreads();
-        if (w == 0) {
-            int nw = blockDim.x >> 5;
-            int s = lane < nw ? warp_sums[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, s, o);
-                if (lane >= o) s += y;
-            }
-            warp_sums[lane] = s;
-        }
-        __syncthreads();
-        int excl = x - v + (w > 0 ? warp_sums[w - 1] : 0) + carry;
-        if (i < ncell) cell_start[i] = excl;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
-        __syncthreads();
+// Exclusive scan of cell_count[0..ncell) into cell_start[0..ncell], in three
+// launches: per-block scans of 1024 cells with block totals, a scan of the
+// totals in one block, then the block offsets added back.
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    if (threadIdx.x == 0) cell_start[ncell] = carry;
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        int t = lane < nw ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_sums[lane] = t;
+    }
+    __syncthreads();
+    const int excl = x - v + (w > 0 ? warp_sums[w - 1] : 0);
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void scan_local_kernel(const GridInfo *g, const int *cell_count, int *cell_start, int *block_sums,
+                                  int max_cells) {
+    __shared__ int warp_sums[32];
+    const int ncell = min(g->ncell, max_cells);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x >= ncell + 1) return;  // whole block idle (uniform)
+    const int v = i < ncell ? cell_count[i] : 0;
+    int total;
+    const int excl = block_exclusive_scan(v, warp_sums, total);
+    if (i <= ncell) cell_start[i] = excl;
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void scan_blocks_kernel(const GridInfo *g, int *block_sums, int max_cells) {
+    __shared__ int warp_sums[32];
+    const int ncell = min(g->ncell, max_cells);
+    const int nblocks = (ncell + 1 + 1023) / 1024;
+    int carry = 0;
+    for (int base = 0; base < nblocks; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < nblocks ? block_sums[i] : 0;
+        int total;
+        const int excl = block_exclusive_scan(v, warp_sums, total);
+        if (i < nblocks) block_sums[i] = excl + carry;
+        carry += total;
+    }
+}
+
+__global__ void scan_add_kernel(const GridInfo *g, int *cell_start, const int *block_sums, int max_cells) {
+    const int ncell = min(g->ncell, max_cells);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= ncell) cell_start[i] += block_sums[blockIdx.x];
 }
 
 __global__ void scatter_kernel(int n, const int *cell_of, const int *cell_start, int *cell_cursor, int *tmp_atom) {
@@ -405,7 +430,10 @@ void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
     const int nb = (a.n + 255) / 256;
     if (a.n > 0)
         assign_kernel<<<nb, 256, 0, s>>>(a.n, a.pos, a.ref, a.grid, a.cell_of, a.cell_count, a.max_cells, a.status);
-    scan_kernel<<<1, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start, a.max_cells);
+    const int scan_blocks = (a.max_cells + 1 + 1023) / 1024;
+    scan_local_kernel<<<scan_blocks, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start, a.scan_scratch, a.max_cells);
+    scan_blocks_kernel<<<1, 1024, 0, s>>>(a.grid, a.scan_scratch, a.max_cells);
+    scan_add_kernel<<<scan_blocks, 1024, 0, s>>>(a.grid, a.cell_start, a.scan_scratch, a.max_cells);
     if (a.n > 0) {
         scatter_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.cell_cursor, a.tmp_atom);
         rank_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.tmp_atom, a.perm, a.cell_sorted, a.status);
