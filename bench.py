@@ -170,7 +170,9 @@ def run_cuda(args, rank, world):
         return {"metric": METRIC, "value": round(world * ns_per_day(args.steps, sec), 3), "unit": "ns/day",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(1e3 * sec / args.steps, 5), "quick": True, "half_list_pairs": pairs,
-                "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"])}
+                "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"]),
+                "kernel_ms": {"pair": round(be.profile("pair", 3), 5), "rebuild": round(be.profile("rebuild", 2), 5)},
+                "split": be.counters().get("split")}
     # steady state: back-to-back steps, no flush (L2 keeps part of the list)
     t_bb = be.time_steps(DT_PS, min(args.steps, 2000), first_step=args.warmup + args.steps) / 1e3
     # roofline of the pair kernel: SURVEY algorithmic bytes 4 P + 52 N per launch

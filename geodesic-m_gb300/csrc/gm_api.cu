@@ -63,6 +63,7 @@ struct gm_ctx {
     int bbox_blocks = 0;
     // list
     int cap = 0, n_groups = 0;
+    int split = 1;                   // warps per group in the FP32 pair kernel
     int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr;
     bool built = false;
     // exclusions
@@ -208,6 +209,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.n = c->n;
     a.n_groups = c->n_groups;
     a.cap = c->cap;
+    a.split = c->fp64 ? 1 : c->split;
     a.hi = c->d_hi;
     a.lo = c->d_lo;
     a.pos64s = c->d_pos64s;
@@ -247,14 +249,15 @@ ForceArgs force_args(gm_ctx *c) {
     a.dihed_i = c->d_di; a.dihed_j = c->d_dj; a.dihed_k = c->d_dk; a.dihed_l = c->d_dl; a.dihed_kphi = c->d_dkphi;
     a.dihed_n = c->d_dn; a.dihed_delta = c->d_ddelta;
     a.bonded_blocks = c->bonded_blocks;
-    a.epart_bonded = c->d_epart + c->n_groups;
+    const int pair_parts = c->n_groups * a.split;
+    a.epart_bonded = c->d_epart + pair_parts;
     a.n14 = c->n14; a.p14_i = c->d_p14i; a.p14_j = c->d_p14j;
     a.scale14_lj = c->p.scale14_lj; a.scale14_coul = c->p.scale14_coul;
     a.sigma = c->d_sigma; a.epsilon = c->d_eps; a.charge64 = c->d_charge64;
     a.blocks14 = c->blocks14;
-    a.epart14 = c->d_epart + c->n_groups + c->bonded_blocks;
+    a.epart14 = c->d_epart + pair_parts + c->bonded_blocks;
     a.energy = c->d_energy;
-    a.n_epart_total = c->n_groups + c->bonded_blocks + c->blocks14;
+    a.n_epart_total = pair_parts + c->bonded_blocks + c->blocks14;
     return a;
 }
 
@@ -854,7 +857,14 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     c->n_groups = (n + 31) / 32;
     TRY(dalloc(c, &c->d_count, (size_t)c->n_groups * 32));
     TRY(dalloc(c, &c->d_gmax, (size_t)c->n_groups));
-    c->n_epart = c->n_groups + c->bonded_blocks + c->blocks14;
+    c->n_epart = c->n_groups * GM_MAX_SPLIT + c->bonded_blocks + c->blocks14;
+    {
+        // enough warps in flight to hide the gather latency: about 48 per SM
+        int dev_sms = 0;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
+        const int want = 48 * std::max(dev_sms, 1);
+        c->split = std::max(1, std::min(GM_MAX_SPLIT, (want + c->n_groups - 1) / std::max(c->n_groups, 1)));
+    }
     TRY(dalloc(c, &c->d_epart, (size_t)c->n_epart));
     TRY(dalloc(c, &c->d_energy, 1));
     TRY(dalloc(c, &c->d_kin_part, 256));
@@ -1264,7 +1274,7 @@ int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {
     if (rc) return rc;
     const DevStatus st = *c->h_status;
     int64_t v[8] = {0, (int64_t)st.n_rebuilds, c->cap, c->launches, (int64_t)st.shake_T, (int64_t)st.rattle_T,
-                    c->launches_per_step, 0};
+                    c->launches_per_step, c->split};
     if (c->built && n > 0) {
         // pairs in the current list (half of the symmetric entries)
         std::vector<int> count((size_t)c->n);

@@ -19,9 +19,14 @@ constexpr int kChunk = 32;
 constexpr float kCoulomb = 332.0522173f;
 constexpr double kCoulomb64 = 332.0522173;
 
+// Warp w works on group w / split and on the part w % split of the group's
+// list columns: entries [part * per, (part + 1) * per), per a multiple of the
+// 32-entry summation chunk.  The split raises the number of warps in flight
+// (a 50k-atom system has only 1,563 groups), and integer partial sums keep the
+// result independent of the order in which the parts land.
 template <bool PERIODIC, bool COULOMB>
 __global__ void __launch_bounds__(kPairWarps * 32)
-pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+pair_kernel_f32(int n, int cap, int split, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
                 const int *__restrict__ gmax, int ntypes, const float2 *__restrict__ tab, float rc2, float rsw,
                 float inv_wsw, float bx, float by, float bz, float ibx, float iby, float ibz,
@@ -30,7 +35,8 @@ pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__r
     for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab[t] = tab[t];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int group = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    const int wid = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    const int group = wid / split, part = wid - group * split;
     if (group * 32 >= n) return;
     const int s = group * 32 + lane;
     const bool valid = s < n;
@@ -40,59 +46,61 @@ pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__r
     const float2 *trow = s_tab + (valid ? __float_as_int(mh.w) : 0) * ntypes;
     const float qi = ml.w * kCoulomb;
     const int gm = gmax[group];
+    const int per = ((gm + split - 1) / split + kChunk - 1) / kChunk * kChunk;
+    const int e_begin = part * per, e_end = min(gm, e_begin + per);
     const int *L = list + (size_t)group * 32 * cap + lane;
+    const int self = valid ? s : 0;
     long long ax = 0, ay = 0, az = 0;
     double eacc = 0.0;
     unsigned int bad = 0;
-    for (int e0 = 0; e0 < gm; e0 += kChunk) {
+    for (int e0 = e_begin; e0 < e_end; e0 += kChunk) {
         float fx = 0.f, fy = 0.f, fz = 0.f, ev = 0.f;
-        const int e1 = min(e0 + kChunk, gm);
+        const int e1 = min(e0 + kChunk, e_end);
 #pragma unroll 4
         for (int e = e0; e < e1; e++) {
-            if (e < cnt) {
-                const int j = __ldg(L + (size_t)e * 32);
-                const float4 jh = __ldg(hi + j);
-                const float4 jl = __ldg(lo + j);
-                float dx = (jh.x - mh.x) + (jl.x - ml.x);
-                float dy = (jh.y - mh.y) + (jl.y - ml.y);
-                float dz = (jh.z - mh.z) + (jl.z - ml.z);
-                if (PERIODIC) {
-                    dx -= bx * rintf(dx * ibx);
-                    dy -= by * rintf(dy * iby);
-                    dz -= bz * rintf(dz * ibz);
+            // lanes past their own count gather their own atom: r2 == 0 drops it
+            const int j = e < cnt ? __ldg(L + (size_t)e * 32) : self;
+            const float4 jh = __ldg(hi + j);
+            const float4 jl = __ldg(lo + j);
+            float dx = (jh.x - mh.x) + (jl.x - ml.x);
+            float dy = (jh.y - mh.y) + (jl.y - ml.y);
+            float dz = (jh.z - mh.z) + (jl.z - ml.z);
+            if (PERIODIC) {
+                dx -= bx * rintf(dx * ibx);
+                dy -= by * rintf(dy * iby);
+                dz -= bz * rintf(dz * ibz);
+            }
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= rc2 && r2 > 0.f) {
+                const float2 p = trow[__float_as_int(jh.w)];
+                // rsqrtf plus one Newton step: the pair sums cancel to
+                // small net forces, so the last ulps of 1/r matter
+                float rinv = rsqrtf(r2);
+                rinv = fmaf(0.5f * rinv, fmaf(-r2 * rinv, rinv, 1.0f), rinv);
+                const float rinv2 = rinv * rinv;
+                const float s2 = p.x * rinv2;
+                const float s6 = s2 * s2 * s2;
+                const float s12 = s6 * s6;
+                float v = 4.f * p.y * (s12 - s6);
+                float fr = 24.f * p.y * (2.f * s12 - s6) * rinv2;  // F_r / r
+                if (COULOMB) {
+                    const float vc = qi * jl.w * rinv;
+                    v += vc;
+                    fr += vc * rinv2;
                 }
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 <= rc2 && r2 > 0.f) {
-                    const float2 p = trow[__float_as_int(jh.w)];
-                    // rsqrtf plus one Newton step: the pair sums cancel to
-                    // small net forces, so the last ulps of 1/r matter
-                    float rinv = rsqrtf(r2);
-                    rinv = fmaf(0.5f * rinv, fmaf(-r2 * rinv, rinv, 1.0f), rinv);
-                    const float rinv2 = rinv * rinv;
-                    const float s2 = p.x * rinv2;
-                    const float s6 = s2 * s2 * s2;
-                    const float s12 = s6 * s6;
-                    float v = 4.f * p.y * (s12 - s6);
-                    float fr = 24.f * p.y * (2.f * s12 - s6) * rinv2;  // F_r / r
-                    if (COULOMB) {
-                        const float vc = qi * jl.w * rinv;
-                        v += vc;
-                        fr += vc * rinv2;
-                    }
-                    const float r = r2 * rinv;
-                    if (r > rsw) {
-                        const float u = (r - rsw) * inv_wsw;
-                        const float u2 = u * u;
-                        const float sw = 1.f + u2 * u * (-10.f + u * (15.f - 6.f * u));
-                        const float dsw = -30.f * u2 * (1.f - u) * (1.f - u) * inv_wsw;
-                        fr = fr * sw - v * dsw * rinv;
-                        v *= sw;
-                    }
-                    fx -= fr * dx;
-                    fy -= fr * dy;
-                    fz -= fr * dz;
-                    ev += v;
+                const float r = r2 * rinv;
+                if (r > rsw) {
+                    const float u = (r - rsw) * inv_wsw;
+                    const float u2 = u * u;
+                    const float sw = 1.f + u2 * u * (-10.f + u * (15.f - 6.f * u));
+                    const float dsw = -30.f * u2 * (1.f - u) * (1.f - u) * inv_wsw;
+                    fr = fr * sw - v * dsw * rinv;
+                    v *= sw;
                 }
+                fx -= fr * dx;
+                fy -= fr * dy;
+                fz -= fr * dz;
+                ev += v;
             }
         }
         ax += gm_to_fix_checked(fx, bad);
@@ -100,14 +108,14 @@ pair_kernel_f32(int n, int cap, const float4 *__restrict__ hi, const float4 *__r
         az += gm_to_fix_checked(fz, bad);
         eacc += (double)ev;
     }
-    if (valid) {
+    if (valid && e_begin < e_end) {
         const int a = perm[s];
         gm_atomic_fix_add(force + a, ax);
         gm_atomic_fix_add(force + n + a, ay);
         gm_atomic_fix_add(force + 2 * n + a, az);
     }
     for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
-    if (lane == 0) epart[group] = 0.5 * eacc;
+    if (lane == 0) epart[wid] = 0.5 * eacc;
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
 }
@@ -381,10 +389,11 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.n == 0) return;
     const int blocks = (a.n_groups + kPairWarps - 1) / kPairWarps;
     if (!fp64) {
+        const int blocks32 = (a.n_groups * a.split + kPairWarps - 1) / kPairWarps;
         const size_t smem = sizeof(float2) * (size_t)a.ntypes * a.ntypes;
 #define GM_PAIR32(P, Q)                                                                                   \
-    pair_kernel_f32<P, Q><<<blocks, kPairWarps * 32, smem, s>>>(                                          \
-        a.n, a.cap, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, a.inv_wsw, \
+    pair_kernel_f32<P, Q><<<blocks32, kPairWarps * 32, smem, s>>>(                                        \
+        a.n, a.cap, a.split, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, a.inv_wsw, \
         a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status)
         if (a.periodic) { if (a.coulomb) GM_PAIR32(true, true); else GM_PAIR32(true, false); }
         else { if (a.coulomb) GM_PAIR32(false, true); else GM_PAIR32(false, false); }

@@ -29,6 +29,7 @@
 // in shared memory (64 x 64 x 8 B = 32 KB).
 #define GM_MAX_TYPES 64
 #define GM_WARP 32
+#define GM_MAX_SPLIT 16      // largest number of warps per 32-atom group
 
 // Device status bits (DevStatus::error).
 enum : unsigned int {
@@ -126,6 +127,7 @@ void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s);
 
 struct ForceArgs {
     int n, n_groups, cap;
+    int split;               // warps per 32-atom group in the FP32 pair kernel
     const float4 *hi, *lo;
     const double4 *pos64s;
     const int *type_sorted;  // FP64 mode
@@ -141,7 +143,7 @@ struct ForceArgs {
     double box64[3];
     int periodic;
     long long *force;
-    double *epart;           // per group
+    double *epart;           // per pair-kernel warp (n_groups * split), then bonded, then 1-4
     DevStatus *status;
     const double *pos;       // caller order FP64 (bonded)
     // bonded, caller order
@@ -157,7 +159,7 @@ struct ForceArgs {
     const double *sigma, *epsilon, *charge64;
     double *epart14; int blocks14;
     double *energy;          // total
-    int n_epart_total;       // epart has n_groups + bonded_blocks + blocks14 entries
+    int n_epart_total;       // n_groups * split + bonded_blocks + blocks14 entries
 };
 
 void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s);

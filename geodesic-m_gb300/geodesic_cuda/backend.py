@@ -349,4 +349,4 @@ class CudaBackend:
         out = (C.c_int64 * 8)()
         self._check(lib().gm_counters(self._h, out, 8))
         return dict(pairs=out[0], rebuilds=out[1], cap=out[2], launches=out[3], shake_iters=out[4],
-                    rattle_iters=out[5], launches_per_step=out[6])
+                    rattle_iters=out[5], launches_per_step=out[6], split=out[7])

@@ -178,7 +178,9 @@ int32_t gm_time_steps(gm_ctx *ctx, double dt, uint64_t first_step, int64_t n_ste
 void *gm_stream(gm_ctx *ctx);
 /* Counters: [0] pairs in the current list, [1] list rebuilds so far,
  * [2] list capacity per atom, [3] kernel launches issued so far,
- * [4] last SHAKE iteration count, [5] last RATTLE iteration count. */
+ * [4] last SHAKE iteration count, [5] last RATTLE iteration count,
+ * [6] kernel launches per captured step, [7] warps per 32-atom group in the
+ * FP32 pair kernel. */
 int32_t gm_counters(const gm_ctx *ctx, int64_t *out, int64_t n);
 
 #ifdef __cplusplus
