@@ -69,6 +69,26 @@ __global__ void bbox_kernel(int n, const double *pos, double *partial) {
 
 __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevStatus *st, double r_list,
                             double b0, double b1, double b2, int periodic, int max_cells, int n_atoms) {
+    // reduce the per-block bbox partials with the whole block first
+    __shared__ double red[9][256];
+    for (int v = 0; v < 9; v++) {
+        double acc = v < 3 ? DBL_MAX : (v < 6 ? -DBL_MAX : 0.0);
+        for (int b = threadIdx.x; b < blocks; b += blockDim.x) {
+            const double x = partial[b * 9 + v];
+            acc = v < 3 ? fmin(acc, x) : (v < 6 ? fmax(acc, x) : acc + x);
+        }
+        red[v][threadIdx.x] = acc;
+    }
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k)
+            for (int v = 0; v < 9; v++) {
+                const double x = red[v][threadIdx.x + k];
+                red[v][threadIdx.x] = v < 3 ? fmin(red[v][threadIdx.x], x)
+                                            : (v < 6 ? fmax(red[v][threadIdx.x], x) : red[v][threadIdx.x] + x);
+            }
+        __syncthreads();
+    }
     if (threadIdx.x != 0) return;
     const double box[3] = {b0, b1, b2};
     const double wmin = r_list * 0.5 * (1.0 + 1e-5) + 1e-6;
@@ -87,13 +107,8 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
             lo[d] = -0.5 * box[d];
         }
     } else {
-        double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX}, sum[3] = {0, 0, 0};
-        for (int b = 0; b < blocks; b++)
-            for (int d = 0; d < 3; d++) {
-                mn[d] = fmin(mn[d], partial[b * 9 + d]);
-                mx[d] = fmax(mx[d], partial[b * 9 + 3 + d]);
-                sum[d] += partial[b * 9 + 6 + d];
-            }
+        double mn[3], mx[3], sum[3];
+        for (int d = 0; d < 3; d++) { mn[d] = red[d][0]; mx[d] = red[3 + d][0]; sum[d] = red[6 + d][0]; }
         // The grid covers a core cube around the mean position, at the finest
         // cell width the allocation allows; atoms outside it (evaporated atoms
         // of a droplet in vacuum) are clamped into the edge cells.  Clamping is
@@ -325,78 +340,87 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
     const int ne = e1 - e0;
 #pragma unroll
     for (int k = 0; k < 8; k++) ex[k] = (k < ne) ? excl[e0 + k] : -1;
-    // group cell box
-    int cx = my_cell % g.nc[0], cy = (my_cell / g.nc[0]) % g.nc[1], cz = my_cell / (g.nc[0] * g.nc[1]);
-    int mn[3] = {valid ? cx : INT_MAX, valid ? cy : INT_MAX, valid ? cz : INT_MAX};
-    int mx[3] = {valid ? cx : INT_MIN, valid ? cy : INT_MIN, valid ? cz : INT_MIN};
-#pragma unroll
-    for (int d = 0; d < 3; d++)
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
-        }
-    Range rx = dim_range(mn[0], mx[0], g.nc[0], g.periodic, g.full[0]);
-    Range ry = dim_range(mn[1], mx[1], g.nc[1], g.periodic, g.full[1]);
-    Range rz = dim_range(mn[2], mx[2], g.nc[2], g.periodic, g.full[2]);
+    // Candidate regions, one per distinct cell row (cy, cz) among the lanes:
+    // a group of 32 sorted atoms usually lies in one row of cells, sometimes
+    // straddles the end of a row.  Sweeping each row's own 5 x 5 x (span + 4)
+    // box keeps the regions tight (one box over both rows would cover the
+    // whole row); a lane tests only the candidates of its own row's box, so
+    // it never meets a candidate twice.
+    const int cx = my_cell % g.nc[0], cy = (my_cell / g.nc[0]) % g.nc[1], cz = my_cell / (g.nc[0] * g.nc[1]);
+    const int row_id = valid ? cz * g.nc[1] + cy : -1;
     int *my_list = list + (size_t)group * 32 * cap + lane;
     int cnt = 0;
     const double bx[3] = {b0, b1, b2};
-    for (int zz = rz.lo; zz <= rz.hi; zz++) {
-        const int z = rz.wrap ? wrapi(zz, g.nc[2]) : zz;
-        for (int yy = ry.lo; yy <= ry.hi; yy++) {
-            const int y = ry.wrap ? wrapi(yy, g.nc[1]) : yy;
-            // the x extent as one or two runs of consecutive cells
-            int seg_lo[2], seg_hi[2], nseg;
-            if (!rx.wrap) { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
-            else if (rx.lo < 0) { seg_lo[0] = rx.lo + g.nc[0]; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi; nseg = 2; }
-            else if (rx.hi >= g.nc[0]) { seg_lo[0] = rx.lo; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi - g.nc[0]; nseg = 2; }
-            else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
-            for (int sg = 0; sg < nseg; sg++) {
-                const int row = (z * g.nc[1] + y) * g.nc[0];
-                const int a0 = cell_start[row + seg_lo[sg]], a1 = cell_start[row + seg_hi[sg] + 1];
-                for (int base = a0; base < a1; base += 32) {
-                    const int t = base + lane;
-                    __syncwarp();
-                    if (t < a1) {
-                        s_hi[wib][lane] = hi[t];
-                        s_lo[wib][lane] = lo[t];
-                        s_orig[wib][lane] = perm[t];
-                    }
-                    __syncwarp();
-                    const int m = min(32, a1 - base);
-                    for (int k = 0; k < m; k++) {
-                        const int j = base + k;
-                        if (!valid || j == s) continue;
-                        const float4 ch = s_hi[wib][k], cl = s_lo[wib][k];
-                        float dx = (ch.x - mh.x) + (cl.x - ml.x);
-                        float dy = (ch.y - mh.y) + (cl.y - ml.y);
-                        float dz = (ch.z - mh.z) + (cl.z - ml.z);
-                        if (g.periodic) {
-                            dx -= g.box[0] * rintf(dx * g.inv_box[0]);
-                            dy -= g.box[1] * rintf(dy * g.inv_box[1]);
-                            dz -= g.box[2] * rintf(dz * g.inv_box[2]);
+    unsigned remaining = __ballot_sync(0xffffffffu, valid);
+    while (remaining) {
+        const int leader = __ffs(remaining) - 1;
+        const int R = __shfl_sync(0xffffffffu, row_id, leader);
+        const bool mine = valid && row_id == R;
+        remaining &= ~__ballot_sync(0xffffffffu, mine);
+        const int xmin = __reduce_min_sync(0xffffffffu, mine ? cx : INT_MAX);
+        const int xmax = __reduce_max_sync(0xffffffffu, mine ? cx : INT_MIN);
+        const int yR = R % g.nc[1], zR = R / g.nc[1];
+        Range rx = dim_range(xmin, xmax, g.nc[0], g.periodic, g.full[0]);
+        Range ry = dim_range(yR, yR, g.nc[1], g.periodic, g.full[1]);
+        Range rz = dim_range(zR, zR, g.nc[2], g.periodic, g.full[2]);
+        for (int zz = rz.lo; zz <= rz.hi; zz++) {
+            const int z = rz.wrap ? wrapi(zz, g.nc[2]) : zz;
+            for (int yy = ry.lo; yy <= ry.hi; yy++) {
+                const int y = ry.wrap ? wrapi(yy, g.nc[1]) : yy;
+                // the x extent as one or two runs of consecutive cells
+                int seg_lo[2], seg_hi[2], nseg;
+                if (!rx.wrap) { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
+                else if (rx.lo < 0) { seg_lo[0] = rx.lo + g.nc[0]; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi; nseg = 2; }
+                else if (rx.hi >= g.nc[0]) { seg_lo[0] = rx.lo; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi - g.nc[0]; nseg = 2; }
+                else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
+                for (int sg = 0; sg < nseg; sg++) {
+                    const int row = (z * g.nc[1] + y) * g.nc[0];
+                    const int a0 = cell_start[row + seg_lo[sg]], a1 = cell_start[row + seg_hi[sg] + 1];
+                    for (int base = a0; base < a1; base += 32) {
+                        const int t = base + lane;
+                        __syncwarp();
+                        if (t < a1) {
+                            s_hi[wib][lane] = hi[t];
+                            s_lo[wib][lane] = lo[t];
+                            s_orig[wib][lane] = perm[t];
                         }
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        if (r2 > rl2_hi) continue;
-                        const int jo = s_orig[wib][k];
-                        bool in = r2 <= rl2_lo;
-                        if (!in) {
-                            // the reference's own FP64 decision
-                            double ex_ = exact_min_image(__dsub_rn(pos[jo], pos[my_orig]), bx[0]);
-                            double ey_ = exact_min_image(__dsub_rn(pos[n + jo], pos[n + my_orig]), bx[1]);
-                            double ez_ = exact_min_image(__dsub_rn(pos[2 * n + jo], pos[2 * n + my_orig]), bx[2]);
-                            double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
-                            in = rr <= rl2_64;
-                        }
-                        if (!in) continue;
-                        bool excluded = false;
+                        __syncwarp();
+                        if (!mine) continue;
+                        const int m = min(32, a1 - base);
+                        for (int k = 0; k < m; k++) {
+                            const int j = base + k;
+                            if (j == s) continue;
+                            const float4 ch = s_hi[wib][k], cl = s_lo[wib][k];
+                            float dx = (ch.x - mh.x) + (cl.x - ml.x);
+                            float dy = (ch.y - mh.y) + (cl.y - ml.y);
+                            float dz = (ch.z - mh.z) + (cl.z - ml.z);
+                            if (g.periodic) {
+                                dx -= g.box[0] * rintf(dx * g.inv_box[0]);
+                                dy -= g.box[1] * rintf(dy * g.inv_box[1]);
+                                dz -= g.box[2] * rintf(dz * g.inv_box[2]);
+                            }
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            if (r2 > rl2_hi) continue;
+                            const int jo = s_orig[wib][k];
+                            bool in = r2 <= rl2_lo;
+                            if (!in) {
+                                // the reference's own FP64 decision
+                                double ex_ = exact_min_image(__dsub_rn(pos[jo], pos[my_orig]), bx[0]);
+                                double ey_ = exact_min_image(__dsub_rn(pos[n + jo], pos[n + my_orig]), bx[1]);
+                                double ez_ = exact_min_image(__dsub_rn(pos[2 * n + jo], pos[2 * n + my_orig]), bx[2]);
+                                double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
+                                in = rr <= rl2_64;
+                            }
+                            if (!in) continue;
+                            bool excluded = false;
 #pragma unroll
-                        for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
-                        if (ne > 8)
-                            for (int q = e0 + 8; q < e1; q++) excluded |= (excl[q] == jo);
-                        if (excluded) continue;
-                        if (cnt < cap) my_list[(size_t)cnt * 32] = j;
-                        cnt++;
+                            for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
+                            if (ne > 8)
+                                for (int q = e0 + 8; q < e1; q++) excluded |= (excl[q] == jo);
+                            if (excluded) continue;
+                            if (cnt < cap) my_list[(size_t)cnt * 32] = j;
+                            cnt++;
+                        }
                     }
                 }
             }
@@ -420,7 +444,7 @@ void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s) {
 
 void gm_launch_grid(const ListArgs &a, cudaStream_t s) {
     if (!a.periodic && a.n > 0) bbox_kernel<<<a.bbox_blocks, 256, 0, s>>>(a.n, a.pos, a.bbox_scratch);
-    grid_kernel<<<1, 32, 0, s>>>(a.bbox_scratch, a.periodic || a.n == 0 ? 0 : a.bbox_blocks, a.grid, a.status,
+    grid_kernel<<<1, 256, 0, s>>>(a.bbox_scratch, a.periodic || a.n == 0 ? 0 : a.bbox_blocks, a.grid, a.status,
                                  a.r_list, a.box[0], a.box[1], a.box[2], a.periodic, a.max_cells, a.n);
 }
 
