@@ -148,13 +148,32 @@ def lib():
         L.gm_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_double, P(C.c_double)]
         L.gm_time_steps.argtypes = [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_void_p, C.c_int64,
                                     P(C.c_double)]
-        for f in ("gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
+        L.gm_build_pairs_static.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, P(GmParams), C.c_void_p,
+                                            C.c_void_p, C.c_int64, P(C.c_int64), C.c_void_p]
+        for f in ("gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
                   "gm_forces_resident", "gm_synchronize", "gm_counters", "gm_profile", "gm_time_steps"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
+
+
+def build_pairs_static(pos_ptr, n_atoms, excl_start_ptr, excl_ptr, params: SimParams, pair_i_ptr, pair_j_ptr,
+                       max_pairs, stream=None):
+    """gm_build_pairs_static: the half list of at most GM_STATIC_MAX_ATOMS
+    atoms from device buffers (integer device addresses), without allocating
+    device memory.  Returns the pair count; raises BackendError on failure
+    (status 7 with .n_pairs set when the count exceeds max_pairs)."""
+    cnt = C.c_int64()
+    prm = params.to_c()
+    rc = lib().gm_build_pairs_static(pos_ptr, int(n_atoms), excl_start_ptr, excl_ptr, C.byref(prm), pair_i_ptr,
+                                     pair_j_ptr, int(max_pairs), C.byref(cnt), stream)
+    if rc:
+        err = BackendError(rc, f"gm_build_pairs_static failed with status {rc}")
+        err.n_pairs = cnt.value
+        raise err
+    return cnt.value
 
 
 def _p(a, ct=C.c_double):

@@ -183,6 +183,43 @@ void *gm_stream(gm_ctx *ctx);
  * FP32 pair kernel. */
 int32_t gm_counters(const gm_ctx *ctx, int64_t *out, int64_t n);
 
+/* ---- allocation-free list build ---------------------------------------- */
+
+/* Largest system gm_build_pairs_static accepts, and the size of the one
+ * static device array (per device) that holds its scratch. */
+#define GM_STATIC_MAX_ATOMS 16384
+#define GM_STATIC_SCRATCH_BYTES (1280u * 1024u)
+
+/* No reference counterpart.  Builds the half neighbour list of a system of
+ * at most GM_STATIC_MAX_ATOMS atoms without allocating device memory: no
+ * context, no cudaMalloc/cudaFree, no allocating library call; the scratch
+ * is a static __device__ array of GM_STATIC_SCRATCH_BYTES.  It serves
+ * callers that cannot allocate when they need the list: a host engine whose
+ * device memory is held by its own pool, or a step running beside other
+ * streams, where cudaFree waits for the whole device.
+ *
+ * All pointers but params and n_pairs are DEVICE pointers on params->device
+ * (made current).  d_pos: x|y|z rows of n_atoms doubles, wrapped into the
+ * box in place when periodic (as gm_build_list does).  d_excl_start
+ * (n_atoms + 1) / d_excl: exclusions as CSR, both directions, each row
+ * ascending (both NULL for none).  The pairs (i < j, |r_ij| <= r_skin by the
+ * reference's FP64 test, excluded pairs left out) go to d_pair_i/d_pair_j,
+ * sorted by (i, then j): the same list gm_get_pairs returns.  *n_pairs
+ * (host) receives the count; with d_pair_i == NULL only the count is
+ * computed.  If the count exceeds max_pairs nothing is written and
+ * GM_ERR_LIST_OVERFLOW is returned.  n_atoms > GM_STATIC_MAX_ATOMS returns
+ * GM_ERR_UNSUPPORTED before any device call.  Runs on `stream` (a
+ * cudaStream_t; NULL = the default stream) and returns after it finished.
+ *
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress, which also loads the module there); make that first
+ * call before any stream capture.  All calls on one device share the one
+ * scratch array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const int32_t *d_excl_start, const int32_t *d_excl,
+                              const gm_params *params, uint32_t *d_pair_i, uint32_t *d_pair_j, int64_t max_pairs,
+                              int64_t *n_pairs, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
