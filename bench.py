@@ -37,6 +37,11 @@ METRIC = "ns/day & pairs/s at 50k atoms: mixed vs FP64 GPU path at ≤1e-5 rel f
 PHYS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
             scale14_lj=0.5, scale14_coul=1.0 / 1.2, max_constr_iter=100, constr_tol=1e-10)
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+# DRAM bytes (read + write) per launch of the FP32 pair kernel per half-list
+# pair, from one ncu capture of the 50k workload at its minimised start
+# (96,405,504 B for 10,067,070 pairs, profiles/pair_kernel_f32_50k_lattice.md);
+# traffic grows with the pair count, so the bench scales it to its own count
+PAIR_TRAFFIC_PER_PAIR = 96_405_504 / 10_067_070
 
 
 def ns_per_day(steps, seconds):
@@ -183,8 +188,10 @@ def run_cuda(args, rank, world):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_pair / 1e9
     # force / energy error of both device paths vs the FP64 oracle, at the
-    # minimised start (step 0) and at the thermalised state after the timed
-    # steps (net forces there are larger, so relative errors are smaller)
+    # generator's raw lattice (before minimisation), at the minimised start
+    # (step 0: net forces ~12x smaller than the individual terms, the hardest
+    # case for FP32 pair math) and at the thermalised state after the timed
+    # steps
     pos_end = np.ascontiguousarray(np.zeros((3, N_ATOMS)))
     vel_end = np.ascontiguousarray(np.zeros((3, N_ATOMS)))
     be.download_state(pos_end, vel_end)
@@ -193,7 +200,10 @@ def run_cuda(args, rank, world):
                             n_threads=0, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2)
     errs = {}
     fp64_nsday = None
-    for label, pos_k in (("step0", np.ascontiguousarray(state.pos)), (f"step{step_end}", pos_end)):
+    from geodesic_cuda import synth
+    raw = synth.generate(N_ATOMS, seed=SEED, temperature=300.0, relax_iters=0)[2].pos
+    for label, pos_k in (("generator_lattice", np.ascontiguousarray(raw)), ("step0", np.ascontiguousarray(state.pos)),
+                         (f"step{step_end}", pos_end)):
         pi_k, pj_k = oracle.neighbor_build(pos_k.copy(), atoms, topo, op, cells=True)
         ob = oracle.CpuBackend(atoms, topo, op)
         ob.set_pairs(pi_k, pj_k, pos_k)
@@ -252,7 +262,8 @@ def run_cuda(args, rank, world):
         "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
                       "list_rebuild": round(t_rebuild * 1e3, 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
+                     "peak_source": peak_kind,
                      "kernel": "pair_kernel_f32", "algorithmic_bytes": alg_bytes},
         "e2e": {"value": round(ns_per_day(n_e2e, t_e2e), 3), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
