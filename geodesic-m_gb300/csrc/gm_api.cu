@@ -84,6 +84,15 @@ struct gm_ctx {
         *d_cl_worst_idx = nullptr;
     double *d_cdsq = nullptr, *d_lam = nullptr, *d_rvec = nullptr, *d_cl_worst = nullptr;
     std::vector<int> h_ci, h_cj;
+    // constraint warm start (gm_mlp.cu)
+    bool ws_on = false, ws_model = false;
+    int ws_rec_stride = 0, ws_rec_cap = 0;
+    int *d_atom_cstart = nullptr, *d_atom_cref = nullptr;
+    float *d_ws_params = nullptr, *d_ws_norm = nullptr, *d_ws_m = nullptr, *d_ws_v = nullptr, *d_ws_feat = nullptr,
+          *d_rec_feat = nullptr, *d_rec_t = nullptr, *d_ws_partial = nullptr, *d_ws_out = nullptr;
+    double *d_ws_scale = nullptr, *d_ws_t1 = nullptr, *d_ws_lam0 = nullptr, *d_lam_sum = nullptr,
+           *d_ws_stats = nullptr;
+    int ws_partial_blocks = 0;
     // energy
     double *d_epart = nullptr, *d_energy = nullptr, *d_kin_part = nullptr, *d_ke = nullptr;
     int n_epart = 0;
@@ -275,7 +284,39 @@ ClusterArgs cluster_args(gm_ctx *c) {
     a.max_iter = c->p.max_constr_iter;
     a.tol = c->p.constr_tol;
     a.status = c->d_status;
+    a.lam_sum = (c->ws_on || c->ws_rec_stride > 0) ? c->d_lam_sum : nullptr;
+    a.lam0 = c->ws_on ? c->d_ws_lam0 : nullptr;
     return a;
+}
+
+// SHAKE with the warm start in between the preparation and the iterations
+// when a model is enabled, and the training record after it when recording
+// (resident steps only).  Returns the number of launches.
+long long issue_shake(gm_ctx *c, cudaStream_t s, bool resident) {
+    const ClusterArgs a = cluster_args(c);
+    long long k = 0;
+    gm_launch_shake_prepare(a, c->n, c->d_dref, s); k += 2;
+    const bool record = resident && c->ws_rec_stride > 0;
+    if (c->ws_on || record) {
+        WsFeatureArgs f{};
+        f.n_constr = c->n_constr; f.n_atoms = c->n;
+        f.constr_i = c->d_ci; f.constr_j = c->d_cj; f.constr_dsq = c->d_cdsq; f.inv_mass = c->d_inv_mass;
+        f.atom_cstart = c->d_atom_cstart; f.atom_cref = c->d_atom_cref; f.pos = c->d_pos; f.dref = c->d_dref;
+        f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1;
+        gm_launch_ws_features(f, s); k += 2;
+    }
+    if (c->ws_on) {
+        gm_launch_ws_infer(c->n_constr, c->d_ws_feat, c->d_ws_params, c->d_ws_norm, c->d_ws_scale, c->d_ws_t1,
+                           c->d_ws_lam0, nullptr, s);
+        k++;
+    }
+    k += gm_launch_shake_solve(a, c->n, c->d_pos, s);
+    if (record) {
+        gm_launch_ws_record(c->n_constr, c->d_ws_feat, c->d_lam_sum, c->d_ws_scale, c->d_ws_t1, c->d_rec_feat,
+                            c->d_rec_t, c->ws_rec_stride, c->ws_rec_cap, c->d_status, s);
+        k += 2;
+    }
+    return k;
 }
 
 // ---- kernel sequences (each counted for gm_counters[3]) -------------------
@@ -328,6 +369,10 @@ int reset_status(gm_ctx *c) {
     z.fail_step = ~0ull;
     z.n_rebuilds = c->h_status->n_rebuilds;
     z.step = c->h_status->step;
+    z.c_steps = c->h_status->c_steps;
+    z.shake_sum = c->h_status->shake_sum;
+    z.rattle_sum = c->h_status->rattle_sum;
+    z.rec_n = c->h_status->rec_n;
     *c->h_status = z;
     return st_write(c);
 }
@@ -481,7 +526,7 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
     gm_launch_half_kick(n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
     gm_launch_drift(n, c->d_pos, c->d_vel, c->d_dref, dt, !constrained, c->d_status, s); k++;
     if (constrained) {
-        gm_launch_shake(cluster_args(c), n, c->d_dref, c->d_pos, s); k += 4;
+        k += issue_shake(c, s, true);
         gm_launch_resync(n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, s); k++;
     }
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
@@ -632,6 +677,57 @@ void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int
 }  // namespace
 
 // ===================================================================== C ABI
+
+namespace {
+
+void drop_graph(gm_ctx *c) {
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+}
+
+int ws_alloc_model(gm_ctx *c) {
+    if (c->d_ws_params) return GM_OK;
+    int rc = dalloc(c, &c->d_ws_params, GM_WS_NPAR);
+    if (!rc) rc = dalloc(c, &c->d_ws_norm, GM_WS_NNORM);
+    if (!rc) rc = dalloc(c, &c->d_ws_m, GM_WS_NPAR);
+    if (!rc) rc = dalloc(c, &c->d_ws_v, GM_WS_NPAR);
+    if (!rc) rc = dalloc(c, &c->d_ws_out, GM_WS_NPAR + 1);
+    if (!rc) rc = dalloc(c, &c->d_ws_stats, 26 * 256);
+    return rc;
+}
+
+int ws_partial(gm_ctx *c, int blocks) {
+    if (blocks <= c->ws_partial_blocks) return GM_OK;
+    dfree(c, c->d_ws_partial);
+    c->d_ws_partial = nullptr;
+    c->ws_partial_blocks = 0;
+    int rc = dalloc(c, &c->d_ws_partial, (size_t)blocks * (GM_WS_NPAR + 1));
+    if (!rc) c->ws_partial_blocks = blocks;
+    return rc;
+}
+
+// Glorot-uniform weights from a splitmix64 stream, zero biases.
+void ws_init_params(uint64_t seed, std::vector<float> &P) {
+    P.assign(GM_WS_NPAR, 0.0f);
+    uint64_t z = seed;
+    auto next = [&z]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (double)(x >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
+    };
+    auto fill = [&](int off, int fan_in, int fan_out) {
+        const double a = std::sqrt(6.0 / (fan_in + fan_out));
+        for (int k = 0; k < fan_in * fan_out; k++) P[(size_t)(off + k)] = (float)((2.0 * next() - 1.0) * a);
+    };
+    fill(GM_WS_OFF_W1, GM_WS_IN, GM_WS_H);
+    fill(GM_WS_OFF_W2, GM_WS_H, GM_WS_H);
+    fill(GM_WS_OFF_W3, GM_WS_H, 1);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -821,6 +917,24 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
         TRY(dupload(c, &c->d_cl_acstart, acstart.data(), acstart.size()));
         TRY(dupload(c, &c->d_cl_acons, acons.data(), acons.size()));
         TRY(dalloc(c, &c->d_lam, (size_t)c->n_constr));
+        {
+            // per-atom constraints, ascending: k where the atom is i, -k-1 where it is j
+            std::vector<int> cs((size_t)n + 1, 0), cref(2 * (size_t)c->n_constr);
+            for (int k = 0; k < c->n_constr; k++) { cs[(size_t)c->h_ci[(size_t)k] + 1]++; cs[(size_t)c->h_cj[(size_t)k] + 1]++; }
+            for (int a = 0; a < n; a++) cs[(size_t)a + 1] += cs[(size_t)a];
+            std::vector<int> fill(cs.begin(), cs.end() - 1);
+            for (int k = 0; k < c->n_constr; k++) {
+                cref[(size_t)fill[(size_t)c->h_ci[(size_t)k]]++] = k;
+                cref[(size_t)fill[(size_t)c->h_cj[(size_t)k]]++] = -k - 1;
+            }
+            TRY(dupload(c, &c->d_atom_cstart, cs.data(), cs.size()));
+            TRY(dupload(c, &c->d_atom_cref, cref.data(), cref.size()));
+        }
+        TRY(dalloc(c, &c->d_lam_sum, (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_ws_lam0, (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_ws_scale, (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_ws_t1, (size_t)c->n_constr));
+        TRY(dalloc(c, &c->d_ws_feat, (size_t)GM_WS_IN * c->n_constr));
         TRY(dalloc(c, &c->d_rvec, 3 * (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_cl_iters, (size_t)c->n_clusters));
         TRY(dalloc(c, &c->d_cl_worst, (size_t)c->n_clusters));
@@ -988,9 +1102,9 @@ int32_t gm_geodesic_drift(gm_ctx *c, double *px, double *py, double *pz, double 
     gm_launch_drift(c->n, c->d_pos, c->d_vel, c->d_dref, dt, !constrained, c->d_status, c->stream);
     c->launches++;
     if (constrained) {
-        gm_launch_shake(cluster_args(c), c->n, c->d_dref, c->d_pos, c->stream);
+        c->launches += issue_shake(c, c->stream, false);
         gm_launch_resync(c->n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, c->stream);
-        c->launches += 5;
+        c->launches += 1;
     }
     rc = download3(c, c->d_pos, px, py, pz);
     if (!rc) rc = download3(c, c->d_vel, vx, vy, vz);
@@ -1273,8 +1387,9 @@ int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {
     int rc = st_read(c);
     if (rc) return rc;
     const DevStatus st = *c->h_status;
-    int64_t v[8] = {0, (int64_t)st.n_rebuilds, c->cap, c->launches, (int64_t)st.shake_T, (int64_t)st.rattle_T,
-                    c->launches_per_step, c->split};
+    int64_t v[12] = {0, (int64_t)st.n_rebuilds, c->cap, c->launches, (int64_t)st.shake_T, (int64_t)st.rattle_T,
+                     c->launches_per_step, c->split, (int64_t)st.c_steps, (int64_t)st.shake_sum,
+                     (int64_t)st.rattle_sum, (int64_t)st.rec_n};
     if (c->built && n > 0) {
         // pairs in the current list (half of the symmetric entries)
         std::vector<int> count((size_t)c->n);
@@ -1283,7 +1398,173 @@ int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {
         for (int x : count) s += x;
         v[0] = s / 2;
     }
-    for (int64_t k = 0; k < n && k < 8; k++) out[k] = v[k];
+    for (int64_t k = 0; k < n && k < 12; k++) out[k] = v[k];
+    return GM_OK;
+}
+
+/* ---- constraint warm start ------------------------------------------- */
+
+int32_t gm_ws_record(gm_ctx *c, int64_t cap_steps, int32_t stride) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!c->n_constr) return fail(c, GM_ERR_UNSUPPORTED, "the system has no constraints");
+    drop_graph(c);
+    if (cap_steps <= 0 || stride <= 0) {  // stop; the samples stay for training
+        c->ws_rec_stride = 0;
+        return GM_OK;
+    }
+    if ((double)cap_steps * c->n_constr * GM_WS_IN > 4e9) return fail(c, GM_ERR_INVALID_ARGUMENT, "record too large");
+    dfree(c, c->d_rec_feat);
+    dfree(c, c->d_rec_t);
+    c->d_rec_feat = c->d_rec_t = nullptr;
+    int rc = dalloc(c, &c->d_rec_feat, (size_t)cap_steps * c->n_constr * GM_WS_IN);
+    if (!rc) rc = dalloc(c, &c->d_rec_t, (size_t)cap_steps * c->n_constr);
+    if (rc) return rc;
+    rc = st_read(c);
+    if (rc) return rc;
+    c->h_status->rec_n = 0;
+    rc = st_write(c);
+    if (rc) return rc;
+    c->ws_rec_cap = (int)cap_steps;
+    c->ws_rec_stride = stride;
+    return GM_OK;
+}
+
+int32_t gm_ws_samples(gm_ctx *c, int64_t cap, float *feat, float *target, int64_t *n_samples) {
+    if (!c || !n_samples) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = st_read(c);
+    if (rc) return rc;
+    const int64_t n = c->d_rec_t ? (int64_t)c->h_status->rec_n * c->n_constr : 0;
+    *n_samples = n;
+    const int64_t m = std::min<int64_t>(n, cap);
+    if (m > 0 && feat) GM_CUDA(c, cudaMemcpy(feat, c->d_rec_feat, sizeof(float) * GM_WS_IN * m, cudaMemcpyDeviceToHost));
+    if (m > 0 && target) GM_CUDA(c, cudaMemcpy(target, c->d_rec_t, sizeof(float) * m, cudaMemcpyDeviceToHost));
+    return GM_OK;
+}
+
+int32_t gm_ws_train(gm_ctx *c, int64_t iters, int32_t blocks, double lr, uint64_t seed, double *final_loss) {
+    if (!c || iters < 0 || blocks <= 0) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = st_read(c);
+    if (rc) return rc;
+    const long long n = c->d_rec_t ? (long long)c->h_status->rec_n * c->n_constr : 0;
+    if (n <= 0) return fail(c, GM_ERR_NOT_BUILT, "no recorded warm-start samples");
+    if ((rc = ws_alloc_model(c)) || (rc = ws_partial(c, blocks))) return rc;
+    cudaStream_t s = c->stream;
+    gm_launch_ws_stats(n, c->d_rec_feat, c->d_rec_t, c->d_ws_stats, 256, c->d_ws_norm, s);
+    std::vector<float> P;
+    ws_init_params(seed, P);
+    GM_CUDA(c, cudaMemcpyAsync(c->d_ws_params, P.data(), sizeof(float) * P.size(), cudaMemcpyHostToDevice, s));
+    GM_CUDA(c, cudaMemsetAsync(c->d_ws_m, 0, sizeof(float) * GM_WS_NPAR, s));
+    GM_CUDA(c, cudaMemsetAsync(c->d_ws_v, 0, sizeof(float) * GM_WS_NPAR, s));
+    GM_CUDA(c, cudaMemsetAsync(c->d_ws_out, 0, sizeof(float) * (GM_WS_NPAR + 1), s));
+    for (int64_t it = 0; it < iters; it++) {
+        const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)it / (double)iters));  // cosine decay
+        gm_launch_ws_grad(n, c->d_rec_feat, c->d_rec_t, c->d_ws_norm, false, c->d_ws_params, blocks, seed,
+                          (long long)it, (long long)blocks * GM_WS_TILE, c->d_ws_partial, s);
+        gm_launch_ws_update(blocks, c->d_ws_partial, c->d_ws_params, c->d_ws_m, c->d_ws_v, (float)lr_t, 0.9f, 0.999f,
+                            1e-8f, (int)(it + 1), c->d_ws_out, s);
+    }
+    c->launches += 2 + 2 * iters;
+    GM_CUDA(c, cudaGetLastError());
+    float loss = 0.0f;
+    GM_CUDA(c, cudaMemcpyAsync(&loss, c->d_ws_out, sizeof(float), cudaMemcpyDeviceToHost, s));
+    GM_CUDA(c, cudaStreamSynchronize(s));
+    if (final_loss) *final_loss = (double)loss / ((double)blocks * GM_WS_TILE);
+    c->ws_model = true;
+    drop_graph(c);
+    return GM_OK;
+}
+
+int32_t gm_ws_enable(gm_ctx *c, int32_t on) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    if (on && !c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model (train or set one first)");
+    if (on && !c->n_constr) return fail(c, GM_ERR_UNSUPPORTED, "the system has no constraints");
+    c->ws_on = on != 0;
+    drop_graph(c);
+    return GM_OK;
+}
+
+int32_t gm_ws_params(gm_ctx *c, float *get_params, float *get_norm, const float *set_params, const float *set_norm) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = ws_alloc_model(c);
+    if (rc) return rc;
+    if (set_params) GM_CUDA(c, cudaMemcpy(c->d_ws_params, set_params, sizeof(float) * GM_WS_NPAR, cudaMemcpyHostToDevice));
+    if (set_norm) GM_CUDA(c, cudaMemcpy(c->d_ws_norm, set_norm, sizeof(float) * GM_WS_NNORM, cudaMemcpyHostToDevice));
+    if (set_params && set_norm) c->ws_model = true;
+    if ((get_params || get_norm) && !c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model");
+    if (get_params) GM_CUDA(c, cudaMemcpy(get_params, c->d_ws_params, sizeof(float) * GM_WS_NPAR, cudaMemcpyDeviceToHost));
+    if (get_norm) GM_CUDA(c, cudaMemcpy(get_norm, c->d_ws_norm, sizeof(float) * GM_WS_NNORM, cudaMemcpyDeviceToHost));
+    if (set_params || set_norm) drop_graph(c);
+    return GM_OK;
+}
+
+int32_t gm_ws_forward(gm_ctx *c, const float *x, int64_t m, float *y) {
+    if (!c || m < 0 || (m && (!x || !y))) return GM_ERR_INVALID_ARGUMENT;
+    if (!c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model");
+    if (!m) return GM_OK;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    float *dx = nullptr, *dy = nullptr, *dn = nullptr;
+    std::vector<float> ident(GM_WS_NNORM, 0.0f);
+    for (int f = 0; f < GM_WS_IN; f++) ident[(size_t)(GM_WS_IN + f)] = 1.0f;
+    ident[25] = 1.0f;
+    int rc = dupload(c, &dx, x, (size_t)m * GM_WS_IN);
+    if (!rc) rc = dalloc(c, &dy, (size_t)m);
+    if (!rc) rc = dupload(c, &dn, ident.data(), ident.size());
+    if (!rc) {
+        gm_launch_ws_infer((int)m, dx, c->d_ws_params, dn, nullptr, nullptr, nullptr, dy, c->stream);
+        c->launches++;
+        cudaError_t e = cudaMemcpyAsync(y, dy, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        rc = cuda_status(c, e, "gm_ws_forward");
+    }
+    dfree(c, dx);
+    dfree(c, dy);
+    dfree(c, dn);
+    return rc;
+}
+
+int32_t gm_ws_gradient(gm_ctx *c, const float *x, const float *t, int64_t m, float *grad, double *loss) {
+    if (!c || m <= 0 || !x || !t) return GM_ERR_INVALID_ARGUMENT;
+    if (!c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model");
+    GM_CUDA(c, cudaSetDevice(c->device));
+    const int blocks = (int)((m + GM_WS_TILE - 1) / GM_WS_TILE);
+    float *dx = nullptr, *dt = nullptr, *dp = nullptr, *dg = nullptr;
+    int rc = dupload(c, &dx, x, (size_t)m * GM_WS_IN);
+    if (!rc) rc = dupload(c, &dt, t, (size_t)m);
+    if (!rc) rc = dalloc(c, &dp, (size_t)blocks * (GM_WS_NPAR + 1));
+    if (!rc) rc = dalloc(c, &dg, (size_t)GM_WS_NPAR + 1);
+    if (!rc) {
+        gm_launch_ws_grad(m, dx, dt, nullptr, true, c->d_ws_params, blocks, 0, -1, m, dp, c->stream);
+        gm_launch_ws_update(blocks, dp, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f, 0, dg, c->stream);
+        c->launches += 2;
+        std::vector<float> h((size_t)GM_WS_NPAR + 1);
+        cudaError_t e = cudaMemcpyAsync(h.data(), dg, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        rc = cuda_status(c, e, "gm_ws_gradient");
+        if (!rc) {
+            if (grad) std::copy(h.begin(), h.begin() + GM_WS_NPAR, grad);
+            if (loss) *loss = (double)h[GM_WS_NPAR] / (double)m;
+        }
+    }
+    dfree(c, dx);
+    dfree(c, dt);
+    dfree(c, dp);
+    dfree(c, dg);
+    return rc;
+}
+
+int32_t gm_ws_last(gm_ctx *c, float *feat, double *lam0, double *lam_sum) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    if (!c->n_constr) return GM_OK;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    const size_t nc = (size_t)c->n_constr;
+    if (feat) GM_CUDA(c, cudaMemcpy(feat, c->d_ws_feat, sizeof(float) * GM_WS_IN * nc, cudaMemcpyDeviceToHost));
+    if (lam0) GM_CUDA(c, cudaMemcpy(lam0, c->d_ws_lam0, sizeof(double) * nc, cudaMemcpyDeviceToHost));
+    if (lam_sum) GM_CUDA(c, cudaMemcpy(lam_sum, c->d_lam_sum, sizeof(double) * nc, cudaMemcpyDeviceToHost));
     return GM_OK;
 }
 

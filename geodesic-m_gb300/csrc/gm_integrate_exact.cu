@@ -117,6 +117,7 @@ __device__ void shake_iteration(const ClusterArgs &c, int cl, const double *rvec
         const double denom = 2.0 * (inv_mi + inv_mj) * dot_new_old;
         const double lambda = denom == 0.0 ? 0.0 : diff / denom;
         c.lam[k] = lambda;
+        if (c.lam_sum) c.lam_sum[k] += lambda;  // the multiplier total, lam0 + sum of iterations
         const double la = fabs(lambda);
         if (la > max_lambda) { max_lambda = la; worst = k; }
     }
@@ -197,6 +198,35 @@ __global__ void shake_prepare(ClusterArgs c, const double *dref, int n_atoms) {
     c.rvec[k] = dref[i] - dref[j];
     c.rvec[c.n_constr + k] = dref[n_atoms + i] - dref[n_atoms + j];
     c.rvec[2 * c.n_constr + k] = dref[2 * n_atoms + i] - dref[2 * n_atoms + j];
+    if (c.lam_sum) c.lam_sum[k] = 0.0;
+}
+
+// Warm start: one displacement with the predicted multipliers lam0, by the
+// update of a Jacobi sweep (per-atom deltas over the atom's constraints in
+// ascending order from 0.0, then added), before the unchanged iterations.
+// The multiplier totals start from lam0.
+__global__ void warm_start_apply(ClusterArgs c, double *pos, int n_atoms) {
+    int cl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cl >= c.n_clusters || c.status->error) return;
+    const int nc = c.n_constr;
+    if (c.lam_sum)
+        for (int q = c.cl_cstart[cl]; q < c.cl_cstart[cl + 1]; q++) c.lam_sum[c.cl_cons[q]] = c.lam0[c.cl_cons[q]];
+    for (int q = c.cl_astart[cl]; q < c.cl_astart[cl + 1]; q++) {
+        const int a = c.cl_atoms[q];
+        const double inv_m = c.inv_mass[a];
+        double ddx = 0.0, ddy = 0.0, ddz = 0.0;
+        for (int r = c.cl_acstart[q]; r < c.cl_acstart[q + 1]; r++) {
+            const int ref = c.cl_acons[r];
+            const int k = ref >= 0 ? ref : -ref - 1;
+            const double w = c.lam0[k] * inv_m;
+            const double tx = w * c.rvec[k], ty = w * c.rvec[nc + k], tz = w * c.rvec[2 * nc + k];
+            if (ref < 0) { ddx -= tx; ddy -= ty; ddz -= tz; }
+            else { ddx += tx; ddy += ty; ddz += tz; }
+        }
+        pos[a] += ddx;
+        pos[n_atoms + a] += ddy;
+        pos[2 * n_atoms + a] += ddz;
+    }
 }
 
 template <bool RATTLE>
@@ -250,7 +280,13 @@ __global__ void reset_T(DevStatus *st, int rattle) {
 }
 
 __global__ void step_kernel(DevStatus *st) {
-    if (!st->error) st->step += 1;
+    if (st->error) return;
+    st->step += 1;
+    if (st->shake_T || st->rattle_T) {
+        st->c_steps += 1;
+        st->shake_sum += st->shake_T;
+        st->rattle_sum += st->rattle_T;
+    }
 }
 
 __global__ void kinetic_partial(int n, const double *vel, const double *mass, double *partial) {
@@ -319,13 +355,25 @@ void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq,
     check_kernel<<<blocks, 256, 0, s>>>(n, pos, ref, thr_sq, st, cond);
 }
 
-void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, double *pos, cudaStream_t s) {
+void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dref, cudaStream_t s) {
     if (c.n_clusters == 0) return;
     reset_T<<<1, 1, 0, s>>>(c.status, 0);
     shake_prepare<<<(c.n_constr + 255) / 256, 256, 0, s>>>(c, dref, n_atoms);
+}
+
+int gm_launch_shake_solve(const ClusterArgs &c, int n_atoms, double *pos, cudaStream_t s) {
+    if (c.n_clusters == 0) return 0;
     const int b = (c.n_clusters + 127) / 128;
+    int k = 0;
+    if (c.lam0) { warm_start_apply<<<b, 128, 0, s>>>(c, pos, n_atoms); k++; }
     cluster_phase1<false><<<b, 128, 0, s>>>(c, pos, nullptr, n_atoms);
     cluster_phase2<false><<<b, 128, 0, s>>>(c, pos, nullptr, n_atoms);
+    return k + 2;
+}
+
+void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, double *pos, cudaStream_t s) {
+    gm_launch_shake_prepare(c, n_atoms, dref, s);
+    gm_launch_shake_solve(c, n_atoms, pos, s);
 }
 
 void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s) {

@@ -54,6 +54,10 @@ struct DevStatus {
     unsigned long long n_rebuilds;
     unsigned long long step;       // current step of the resident loop
     unsigned long long fail_step;  // first step whose projection failed (init ~0)
+    unsigned long long c_steps;    // resident steps with constraints
+    unsigned long long shake_sum;  // sum of their SHAKE iteration counts
+    unsigned long long rattle_sum; // sum of their RATTLE iteration counts
+    unsigned int rec_n;            // warm-start samples recorded (in solves)
 };
 
 struct GridInfo {
@@ -177,6 +181,8 @@ struct ClusterArgs {
     const double *constr_dsq;
     const double *inv_mass;               // 1.0 / mass (caller order)
     double *lam;                          // per constraint scratch
+    double *lam_sum;                      // per constraint accumulated multiplier (nullptr: not kept)
+    const double *lam0;                   // per constraint warm-start multiplier (nullptr: cold start)
     double *rvec;                         // per constraint reference vector (3 x C)
     int *cl_iters;                        // per cluster iteration count
     double *cl_worst;                     // per cluster last max |lambda|
@@ -198,6 +204,11 @@ void gm_launch_resync(int n, const double *pos, double *vel, const double *dref,
 void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
                      unsigned long long cond_handle, int blocks, cudaStream_t s);
 void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, double *pos, cudaStream_t s);
+// the same solve in two halves, so the warm start can run in between:
+// prepare (reset T, reference vectors, multiplier sums) and the iterations
+// (warm-start displacement when c.lam0 is set, then both phases)
+void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dref, cudaStream_t s);
+int gm_launch_shake_solve(const ClusterArgs &c, int n_atoms, double *pos, cudaStream_t s);
 void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s);
 void gm_launch_step(DevStatus *st, cudaStream_t s);
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,
@@ -205,3 +216,55 @@ void gm_launch_kinetic(int n, const double *vel, const double *mass, double *par
 void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s);
 void gm_launch_differs(int n, const double *a, const double *b, unsigned int *flag, cudaStream_t s);
 int gm_check_blocks(int n);
+
+// ---- constraint warm start (gm_mlp.cu) -----------------------------------
+// A 12-64-64-1 SiLU network over per-constraint features predicts the
+// constraint's total SHAKE multiplier, as a correction to the first Jacobi
+// step (t = Lambda * 2 (1/m_i + 1/m_j) = t1 + network).  FP32 master parameters, laid out as
+// W1[12][64], b1[64], W2[64][64], b2[64], w3[64], b3; the matmul weights and
+// the activations are rounded to BF16, sums are FP32.  norm holds the
+// feature means[12], feature scales[12], target mean, target scale.
+constexpr int GM_WS_IN = 12, GM_WS_H = 64;
+constexpr int GM_WS_OFF_W1 = 0, GM_WS_OFF_B1 = 768, GM_WS_OFF_W2 = 832, GM_WS_OFF_B2 = 4928, GM_WS_OFF_W3 = 4992,
+              GM_WS_OFF_B3 = 5056, GM_WS_NPAR = 5057, GM_WS_NNORM = 26;
+constexpr int GM_WS_TILE = 128;  // samples per block of the training kernel
+
+// Features of constraint k = (i, j), d0^2 = dsq, r = ref_i - ref_j, d =
+// trial_i - trial_j, w = 1/m_i + 1/m_j:
+//  0 (d.d - d0^2) / d0^2   1 d.r / d0^2   2 d0   3 1/m_i   4 1/m_j
+//  5, 6 constraints on i, on j   7 t1 = (d.d - d0^2) / d.r (the first Jacobi
+//  step times 2 w)   8 c1 = sum over the other constraints l on a shared
+//  atom a of (1/m_a) / w_k cos(r_k, r_l) s_k s_l t1_l w_k / w_l (the first
+//  order coupling; s = +1 where a is the constraint's i, -1 where it is j)
+//  9 sum of the squared coupling coefficients   10 max |cos|   11 sum of t1_l
+struct WsFeatureArgs {
+    int n_constr, n_atoms;
+    const int *constr_i, *constr_j;
+    const double *constr_dsq, *inv_mass;
+    const int *atom_cstart, *atom_cref;  // per-atom constraints (CSR; ref k: atom is i, -k-1: atom is j)
+    const double *pos, *dref;    // trial and reference positions
+    float *feat;                 // [n_constr][12] raw features
+    double *scale;               // 2 (1/m_i + 1/m_j) per constraint
+    double *t1;                  // first Jacobi step of a cold solve, times scale
+};
+void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s);
+// lam0[k] = (t1[k] + y_k * t_scale + t_mean) / scale[k] from the raw features
+void gm_launch_ws_infer(int n, const float *feat, const float *params, const float *norm, const double *scale,
+                        const double *t1, double *lam0, float *y_out, cudaStream_t s);
+// records raw features and targets lam_sum * scale - t1 into slot rec_n when
+// step % stride == 0 (resident steps), then advances rec_n
+void gm_launch_ws_record(int n_constr, const float *feat, const double *lam_sum, const double *scale, const double *t1,
+                         float *rec_feat, float *rec_t, int stride, int cap_slots, DevStatus *st, cudaStream_t s);
+// feature/target statistics over n samples into norm (device, deterministic)
+void gm_launch_ws_stats(long long n, const float *feat, const float *t, double *partial, int blocks, float *norm,
+                        cudaStream_t s);
+// one forward/backward pass over a batch of blocks x 128 samples; sample b*128+s
+// is idx ? idx[...] : hash(seed, iter, .) % n.  Writes per-block gradients
+// and loss into partial[blocks][NPAR + 1]; rows past n_valid count nothing.
+void gm_launch_ws_grad(long long n, const float *feat, const float *t, const float *norm, bool standardized,
+                       const float *params, int blocks, unsigned long long seed, long long iter, long long n_valid,
+                       float *partial, cudaStream_t s);
+// fixed-order sum of the block gradients; Adam step when m != nullptr,
+// otherwise the summed gradient (and loss) go to grad_out
+void gm_launch_ws_update(int blocks, const float *partial, float *params, float *m, float *v, float lr, float b1,
+                         float b2, float eps, int t, float *grad_out, cudaStream_t s);

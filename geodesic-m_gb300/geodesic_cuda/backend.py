@@ -150,7 +150,17 @@ def lib():
                                     P(C.c_double)]
         L.gm_build_pairs_static.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, P(GmParams), C.c_void_p,
                                             C.c_void_p, C.c_int64, P(C.c_int64), C.c_void_p]
-        for f in ("gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
+        _f32p = P(C.c_float)
+        L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
+        L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
+        L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
+        L.gm_ws_enable.argtypes = [C.c_void_p, C.c_int32]
+        L.gm_ws_params.argtypes = [C.c_void_p, _f32p, _f32p, _f32p, _f32p]
+        L.gm_ws_forward.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p]
+        L.gm_ws_gradient.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int64, _f32p, P(C.c_double)]
+        L.gm_ws_last.argtypes = [C.c_void_p, _f32p, _f64p, _f64p]
+        for f in ("gm_ws_record", "gm_ws_samples", "gm_ws_train", "gm_ws_enable", "gm_ws_params", "gm_ws_forward",
+                  "gm_ws_gradient", "gm_ws_last", "gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
                   "gm_forces_resident", "gm_synchronize", "gm_counters", "gm_profile", "gm_time_steps"):
@@ -365,7 +375,66 @@ class CudaBackend:
         return int(lib().gm_stream(self._h) or 0)
 
     def counters(self) -> dict:
-        out = (C.c_int64 * 8)()
-        self._check(lib().gm_counters(self._h, out, 8))
+        out = (C.c_int64 * 12)()
+        self._check(lib().gm_counters(self._h, out, 12))
         return dict(pairs=out[0], rebuilds=out[1], cap=out[2], launches=out[3], shake_iters=out[4],
-                    rattle_iters=out[5], launches_per_step=out[6], split=out[7])
+                    rattle_iters=out[5], launches_per_step=out[6], split=out[7], constrained_steps=out[8],
+                    shake_iter_sum=out[9], rattle_iter_sum=out[10], ws_records=out[11])
+
+    # ------------------------------------------- constraint warm start
+    WS_NPAR, WS_NNORM = 5057, 26
+
+    def ws_record(self, cap_steps, stride=1):
+        """Record (features, multiplier target) of every stride-th resident solve."""
+        self._check(lib().gm_ws_record(self._h, int(cap_steps), int(stride)))
+
+    def ws_samples(self):
+        n = C.c_int64()
+        self._check(lib().gm_ws_samples(self._h, 0, None, None, C.byref(n)))
+        f = np.zeros((max(n.value, 1), 12), np.float32)
+        t = np.zeros(max(n.value, 1), np.float32)
+        self._check(lib().gm_ws_samples(self._h, n.value, _p(f, C.c_float), _p(t, C.c_float), C.byref(n)))
+        return f[:n.value], t[:n.value]
+
+    def ws_train(self, iters, blocks=64, lr=3e-3, seed=1):
+        """Train the warm-start network on the recorded samples; returns the last batch loss."""
+        loss = C.c_double()
+        self._check(lib().gm_ws_train(self._h, int(iters), int(blocks), float(lr), int(seed), C.byref(loss)))
+        return loss.value
+
+    def ws_enable(self, on=True):
+        self._check(lib().gm_ws_enable(self._h, 1 if on else 0))
+
+    def ws_params(self, params=None, norm=None):
+        """Sets the parameters/norm when given; returns the current ones."""
+        sp = None if params is None else np.ascontiguousarray(params, np.float32)
+        sn = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        if sp is not None or sn is not None:
+            self._check(lib().gm_ws_params(self._h, None, None, None if sp is None else _p(sp, C.c_float),
+                                           None if sn is None else _p(sn, C.c_float)))
+        gp = np.zeros(self.WS_NPAR, np.float32)
+        gn = np.zeros(self.WS_NNORM, np.float32)
+        self._check(lib().gm_ws_params(self._h, _p(gp, C.c_float), _p(gn, C.c_float), None, None))
+        return gp, gn
+
+    def ws_forward(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(len(x), np.float32)
+        self._check(lib().gm_ws_forward(self._h, _p(x, C.c_float), len(x), _p(y, C.c_float)))
+        return y
+
+    def ws_gradient(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(self.WS_NPAR, np.float32)
+        loss = C.c_double()
+        self._check(lib().gm_ws_gradient(self._h, _p(x, C.c_float), _p(t, C.c_float), len(x), _p(g, C.c_float),
+                                         C.byref(loss)))
+        return g, loss.value
+
+    def ws_last(self, n_constr):
+        f = np.zeros((max(n_constr, 1), 12), np.float32)
+        l0 = np.zeros(max(n_constr, 1))
+        ls = np.zeros(max(n_constr, 1))
+        self._check(lib().gm_ws_last(self._h, _p(f, C.c_float), _p(l0), _p(ls)))
+        return f[:n_constr], l0[:n_constr], ls[:n_constr]

@@ -17,10 +17,15 @@
  * Maxwell-Boltzmann at the requested temperature, zero net momentum.
  *
  * Optional hydrogens (h_fraction > 0): that fraction of lattice sites become
- * H atoms (mass 1.008, sigma 1.2 A, epsilon 0.02, name "H"), each bonded to a
- * random lattice-adjacent heavy atom at 1.09 A (k = 340); the heavy atoms
- * keep the serpentine chain.  H atoms get H-X-Y angles (k = 35) and the
- * matching 1-2/1-3 exclusions.
+ * H atoms (mass 1.008; AMBER aliphatic-H Lennard-Jones, sigma 2.65 A,
+ * epsilon 0.0157 kcal/mol; charges U[-0.1, 0.1] e, so that oppositely
+ * charged H pairs cannot collapse onto each other; name "H"), each bonded
+ * to a random lattice-adjacent heavy atom at 1.09 A (k = 340); the heavy
+ * atoms keep the serpentine chain.  H atoms get H-X-Y angles to the
+ * parent's chain neighbours and H-X-H angles to the parent's other H atoms
+ * (k = 35) and the matching 1-2/1-3 exclusions.  The minimiser keeps the H bonds rigid
+ * at 1.09 A and the velocities get no H-parent component along the bond,
+ * so the MD run (H bonds constrained) starts on the constraint manifold.
  *
  * Pre-relaxation: FIRE minimisation in FP64 of bonds, angles, the scaled 1-4
  * pairs (LJ x 1/2, Coulomb x 1/1.2) and LJ + Coulomb with the quintic switch
@@ -205,14 +210,18 @@ int gs_sizes_for(const gs_request *q, gs_sizes *out) {
     int64_t h_angles = 0;
     int64_t *pos_in_chain = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
     for (int64_t k = 0; k < nh; k++) pos_in_chain[L.heavy[k]] = k;
+    int64_t *nh_of = (int64_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(int64_t));
     for (int64_t a = 0; a < n; a++) {
         if (!L.is_h[a]) continue;
         int64_t k = pos_in_chain[L.h_parent[a]];
         h_angles += (k > 0) + (k + 1 < nh);
+        /* and one H-X-H angle per pair of H atoms sharing the parent */
+        h_angles += nh_of[L.h_parent[a]]++;
     }
+    free(nh_of);
     out->n_angles = (nh > 1 ? nh - 2 : 0) + h_angles;
     out->n_diheds = nh > 2 ? nh - 3 : 0;
-    /* exclusions: chain 1-2, 1-3, 1-4; H: parent (1-2) + H-Y (1-3) */
+    /* exclusions: chain 1-2, 1-3, 1-4; H: parent (1-2) + H-Y and H-H (1-3) */
     out->n_excl = (nh > 0 ? nh - 1 : 0) + (nh > 1 ? nh - 2 : 0) + (nh > 2 ? nh - 3 : 0) + nH + h_angles;
     out->n_types = NTYPES + (nH > 0);
     free(pos_in_chain);
@@ -424,8 +433,46 @@ static double bonded_relax_forces(int64_t n, const double *p, const gs_sizes *S,
     return e;
 }
 
+/* Rigid H bonds inside the minimiser: the force on an H along its bond is
+ * carried by the bond to the parent, and the H is put back at 1.09 A after
+ * every move, so the minimum is taken on the constraint manifold (the MD run
+ * then starts without a perpendicular load the constraints cannot take). */
+static void rigid_h_forces(int64_t n, const double *pos, const int64_t *hp, double *F, double *V) {
+    for (int64_t a = 0; a < n; a++) {
+        const int64_t b = hp[a];
+        if (b < 0) continue;
+        double u[3], len = 0.0;
+        for (int k = 0; k < 3; k++) { u[k] = pos[k * n + a] - pos[k * n + b]; len += u[k] * u[k]; }
+        len = sqrt(len);
+        if (!(len > 0.0)) continue;
+        double fu = 0.0, vr = 0.0;
+        for (int k = 0; k < 3; k++) {
+            u[k] /= len;
+            fu += F[k * n + a] * u[k];
+            vr += (V[k * n + a] - V[k * n + b]) * u[k];
+        }
+        for (int k = 0; k < 3; k++) {
+            F[k * n + a] -= fu * u[k];
+            F[k * n + b] += fu * u[k];
+            V[k * n + a] -= vr * u[k];
+        }
+    }
+}
+
+static void rigid_h_snap(int64_t n, double *pos, const int64_t *hp) {
+    for (int64_t a = 0; a < n; a++) {
+        const int64_t b = hp[a];
+        if (b < 0) continue;
+        double d[3], len = 0.0;
+        for (int k = 0; k < 3; k++) { d[k] = pos[k * n + a] - pos[k * n + b]; len += d[k] * d[k]; }
+        len = sqrt(len);
+        if (len > 0.0)
+            for (int k = 0; k < 3; k++) pos[k * n + a] = pos[k * n + b] + 1.09 * d[k] / len;
+    }
+}
+
 static double relax_stage(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, int iters, int n_threads,
-                          double rc, double rs, double ftol, double *max_before) {
+                          double rc, double rs, double ftol, double *max_before, const int64_t *hp) {
     int64_t nk = S->n_excl;
     uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(nk > 0 ? nk : 1));
     for (int64_t e = 0; e < nk; e++) {
@@ -473,6 +520,7 @@ static double relax_stage(int64_t n, double *pos, const gs_sizes *S, const gs_ou
         }
         nb_worker(&jobs[0]);
         for (int t = 1; t < n_threads; t++) pthread_join(th[t], NULL);
+        if (hp) rigid_h_forces(n, pos, hp, F, V);
         maxf = 0.0;
         double P = 0.0, fn = 0.0, vn = 0.0;
         for (int64_t i = 0; i < 3 * n; i++) { P += F[i] * V[i]; fn += F[i] * F[i]; vn += V[i] * V[i]; }
@@ -501,6 +549,7 @@ static double relax_stage(int64_t n, double *pos, const gs_sizes *S, const gs_ou
             double sc = d2 > max_step * max_step ? max_step / sqrt(d2) : 1.0;
             for (int c = 0; c < 3; c++) pos[c * n + i] += sc * d[c];
         }
+        if (hp) rigid_h_snap(n, pos, hp);
     }
     free(F); free(V); free(ref); free(start); free(nb); free(eth); free(jobs); free(th); free(keys);
     return maxf;
@@ -509,11 +558,12 @@ static double relax_stage(int64_t n, double *pos, const gs_sizes *S, const gs_ou
 /* Two stages: most iterations on the cheap 6 A switched potential, then a
  * fifth of them on the full potential (switch 8 -> 10 A). */
 static double relax(int64_t n, double *pos, const gs_sizes *S, const gs_out *o, int iters, int n_threads,
-                    double *max_before) {
-    if (iters <= 0) return relax_stage(n, pos, S, o, 0, n_threads, 10.0, 8.0, 1.0, max_before);
+                    double *max_before, const int64_t *hp) {
+    if (hp) rigid_h_snap(n, pos, hp);
+    if (iters <= 0) return relax_stage(n, pos, S, o, 0, n_threads, 10.0, 8.0, 1.0, max_before, hp);
     int polish = iters / 5 > 0 ? iters / 5 : 1;
-    relax_stage(n, pos, S, o, iters - polish, n_threads, 6.0, 4.0, 0.5, max_before);
-    return relax_stage(n, pos, S, o, polish, n_threads, 10.0, 8.0, 1.0, NULL);
+    relax_stage(n, pos, S, o, iters - polish, n_threads, 6.0, 4.0, 0.5, max_before, hp);
+    return relax_stage(n, pos, S, o, polish, n_threads, 10.0, 8.0, 1.0, NULL, hp);
 }
 
 /* ------------------------------------------------------------ generate */
@@ -531,7 +581,7 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
         teps[t] = 0.02 + 0.18 * uni(&r);
         tmass[t] = 12.0 + 4.0 * uni(&r);
     }
-    tsig[NTYPES] = 1.2; teps[NTYPES] = 0.02; tmass[NTYPES] = 1.008;
+    tsig[NTYPES] = 2.65; teps[NTYPES] = 0.0157; tmass[NTYPES] = 1.008;
     double qsum = 0.0;
     int c[3];
     double *x = o->pos, *y = o->pos + n, *z = o->pos + 2 * n;
@@ -544,7 +594,7 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
         o->epsilon[p] = teps[s];
         o->mass[p] = tmass[s];
         o->element[p] = L.is_h[p] ? 0 : 1;
-        o->charge[p] = -0.5 + uni(&r);
+        o->charge[p] = L.is_h[p] ? 0.2 * (uni(&r) - 0.5) : -0.5 + uni(&r);
         qsum += o->charge[p];
         path_site(p, side, c);
         x[p] = c[0] * SPACING + (uni(&r) * 0.6 - 0.3);
@@ -605,6 +655,17 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
             o->angle_kth[na] = degenerate ? 0.0 : 35.0; o->angle_th0[na] = th; na++;
             o->excl_i[ne] = (uint32_t)(a < yv ? a : yv); o->excl_j[ne] = (uint32_t)(a < yv ? yv : a); ne++;
         }
+        /* H-X-H with every earlier H of the same parent (as a force field's
+         * H-C-H angles): keeps the H atoms of one parent apart and excludes
+         * their 1-3 pair */
+        for (int64_t e = 0; e < a; e++) {
+            if (!L.is_h[e] || L.h_parent[e] != b) continue;
+            o->angle_i[na] = (uint32_t)e; o->angle_j[na] = (uint32_t)b; o->angle_k[na] = (uint32_t)a;
+            double th = lattice_angle(&ideal[3 * e], &ideal[3 * b], &ideal[3 * a]);
+            int degenerate = th < 0.2 || th > M_PI - 0.2;
+            o->angle_kth[na] = degenerate ? 0.0 : 35.0; o->angle_th0[na] = th; na++;
+            o->excl_i[ne] = (uint32_t)e; o->excl_j[ne] = (uint32_t)a; ne++;
+        }
     }
     for (int64_t k = 0; k + 3 < nh; k++) {
         const int64_t a0 = L.heavy[k], a1 = L.heavy[k + 1], a2 = L.heavy[k + 2], a3 = L.heavy[k + 3];
@@ -632,7 +693,16 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
     free(ideal);
     if (nb != S->n_bonds || na != S->n_angles || nd != S->n_diheds || ne != S->n_excl) { free_layout(&L); return -1; }
     /* relaxation */
-    o->max_force_after = relax(n, o->pos, S, o, q->relax_iters, q->n_threads, &o->max_force_before);
+    /* with hydrogens the H bonds are rigid in the minimiser (they become
+     * constraints in the MD run), so the start lies on the constraint
+     * manifold without a load the constraints cannot take */
+    int64_t *hp = NULL;
+    if (q->h_fraction > 0.0) {
+        hp = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+        for (int64_t a = 0; a < n; a++) hp[a] = L.is_h[a] ? L.h_parent[a] : -1;
+    }
+    o->max_force_after = relax(n, o->pos, S, o, q->relax_iters, q->n_threads, &o->max_force_before, hp);
+    free(hp);
     /* Maxwell-Boltzmann velocities, zero net momentum */
     rng_t rv = {q->seed ^ 0x56454C4Full};
     const double kB = 0.0019872041; /* kcal/mol/K */
@@ -645,6 +715,19 @@ int gs_generate(const gs_request *q, const gs_sizes *S, gs_out *o) {
     if (n > 0 && q->temperature > 0)
         for (int64_t p = 0; p < n; p++)
             for (int d = 0; d < 3; d++) o->vel[d * n + p] -= pm[d] / mt;
+    /* and on its tangent space: no H-parent relative velocity along the bond
+     * (only the H velocity changes, so H atoms sharing a parent stay
+     * independent) */
+    for (int64_t a = 0; a < n; a++) {
+        if (!L.is_h[a]) continue;
+        const int64_t b = L.h_parent[a];
+        double u[3], len = 0.0, vr = 0.0;
+        for (int k = 0; k < 3; k++) { u[k] = o->pos[k * n + a] - o->pos[k * n + b]; len += u[k] * u[k]; }
+        len = sqrt(len);
+        if (!(len > 0.0)) continue;
+        for (int k = 0; k < 3; k++) { u[k] /= len; vr += (o->vel[k * n + a] - o->vel[k * n + b]) * u[k]; }
+        for (int k = 0; k < 3; k++) o->vel[k * n + a] -= vr * u[k];
+    }
     free_layout(&L);
     return 0;
 }

@@ -180,8 +180,54 @@ void *gm_stream(gm_ctx *ctx);
  * [2] list capacity per atom, [3] kernel launches issued so far,
  * [4] last SHAKE iteration count, [5] last RATTLE iteration count,
  * [6] kernel launches per captured step, [7] warps per 32-atom group in the
- * FP32 pair kernel. */
+ * FP32 pair kernel, [8] resident steps with constraints, [9] / [10] the sum
+ * of their SHAKE / RATTLE iteration counts, [11] warm-start solves recorded. */
 int32_t gm_counters(const gm_ctx *ctx, int64_t *out, int64_t n);
+
+/* ---- constraint warm start (no reference counterpart) ------------------
+ *
+ * A 12-64-64-1 SiLU network (BF16 matmul weights and activations, FP32
+ * sums) predicts each constraint's total SHAKE multiplier Lambda (the sum of
+ * the Jacobi lambdas of constraint.rs:62-152) from 12 rotation-invariant
+ * features of the constraint and of the constraints sharing its atoms: with
+ * r = r_ref, d = r_trial, (d.d - d0^2)/d0^2, d.r/d0^2, d0, 1/m_i, 1/m_j, the
+ * constraint counts on i and j, t1 (below), the first-order coupling
+ * sum_l (1/m_a)/w cos(r_k, r_l) s_k s_l t1_l w_k/w_l over the constraints l
+ * sharing an atom a (s = +1 at the constraint's i, -1 at its j, w =
+ * 1/m_i + 1/m_j), the sum of the squared coupling coefficients, the largest
+ * |cos| and the sum of the neighbours' t1.  With the warm start on, each
+ * SHAKE solve first moves the atoms once with the predicted multipliers (the
+ * Jacobi update formula) and then runs the unchanged iteration to the same
+ * tolerance, so the result meets the same convergence test.  Parameters:
+ * 5057 FP32 values (W1[12][64], b1[64], W2[64][64], b2[64], w3[64], b3);
+ * norm: 26 FP32 values (feature means[12], scales[12], target mean, scale).
+ * The network output is the standardised correction t - t1, where t =
+ * Lambda * 2 (1/m_i + 1/m_j) and t1 = (|r_trial|^2 - d0^2) / (r_trial .
+ * r_ref) is the first Jacobi step of a cold solve. */
+
+/* Records (raw features, target t - t1) of every constraint at every stride-th
+ * resident step (gm_run_resident / gm_time_steps / gm_steps), up to
+ * cap_steps solves; cap_steps = 0 stops recording and keeps the samples. */
+int32_t gm_ws_record(gm_ctx *ctx, int64_t cap_steps, int32_t stride);
+/* Copies up to cap recorded samples (feat: [cap][12], target: [cap]). */
+int32_t gm_ws_samples(gm_ctx *ctx, int64_t cap, float *feat, float *target, int64_t *n_samples);
+/* Trains the network on the GPU from a seeded Glorot start: feature and
+ * target statistics over the recorded samples, then iters Adam steps
+ * (cosine-decayed lr) on batches of blocks x 128 samples drawn by a seeded
+ * hash.  *final_loss: mean squared error of the last batch (standardised). */
+int32_t gm_ws_train(gm_ctx *ctx, int64_t iters, int32_t blocks, double lr, uint64_t seed, double *final_loss);
+/* Uses (1) or stops using (0) the network as the SHAKE warm start. */
+int32_t gm_ws_enable(gm_ctx *ctx, int32_t on);
+/* Gets and/or sets the parameters (5057) and norm (26); NULL skips. */
+int32_t gm_ws_params(gm_ctx *ctx, float *get_params, float *get_norm, const float *set_params, const float *set_norm);
+/* Network output for m standardised inputs x[m][12] (host). */
+int32_t gm_ws_forward(gm_ctx *ctx, const float *x, int64_t m, float *y);
+/* Gradient (5057) of the mean squared error over m standardised samples
+ * (x[m][12], t[m]) by the training kernels, and the loss. */
+int32_t gm_ws_gradient(gm_ctx *ctx, const float *x, const float *t, int64_t m, float *grad, double *loss);
+/* Raw features ([C][12]), predicted multipliers and multiplier totals of the
+ * last solve that computed them (NULL skips). */
+int32_t gm_ws_last(gm_ctx *ctx, float *feat, double *lam0, double *lam_sum);
 
 /* ---- allocation-free list build ---------------------------------------- */
 

@@ -311,6 +311,18 @@ def drift_and_constrain(pos, vel, topo, atoms, dt, max_iter, tol, step=0):
     return int(it)
 
 
+def drift_and_constrain_ws(pos, vel, topo, atoms, dt, max_iter, tol, lam0, step=0):
+    """integrator.rs:32-71 with the SHAKE warm start of constraint_solve
+    (lam0: predicted multipliers applied once before the iterations).  The
+    same operations as or_drift_and_constrain.  Returns (iterations, summed
+    multipliers)."""
+    ref = pos.copy()
+    pos += dt * vel
+    it, lam = constraint_solve(topo, atoms, ref, pos, max_iter, tol, step, lam0=lam0, want_lambda=True)
+    vel[...] = (pos - ref) / dt
+    return it, lam
+
+
 def kinetic_energy(vel, mass) -> float:
     m = _f64(mass)
     v = _f64(vel)
