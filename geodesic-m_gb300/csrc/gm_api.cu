@@ -56,7 +56,14 @@ struct gm_ctx {
     int *d_type_sorted = nullptr;
     int *d_perm = nullptr, *d_cell_of = nullptr, *d_cell_sorted = nullptr, *d_cell_count = nullptr,
         *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr;
-    int max_cells = 0;
+    long long total_cells = 0;     // cell budget of all systems
+    // systems of a batch (one for a plain context)
+    int n_sys = 1, n_slots = 0, scan_blocks = 0, max_sys_atoms = 0;
+    std::vector<int> h_atom_off;
+    int *d_sys_atom_off = nullptr, *d_sys_slot_off = nullptr, *d_sys_cell_off = nullptr, *d_atom_sys = nullptr,
+        *d_group_sys = nullptr;
+    unsigned int *d_sys_flag = nullptr;
+    long long *d_e_sys = nullptr;  // per-system energies (batches)
     int *d_scan = nullptr;
     GridInfo *d_grid = nullptr;
     double *d_bbox = nullptr;
@@ -178,6 +185,8 @@ bool finite3(const double *x, const double *y, const double *z, int n) {
 ListArgs list_args(gm_ctx *c) {
     ListArgs a{};
     a.n = c->n;
+    a.n_slots = c->n_slots;
+    a.n_sys = c->n_sys;
     a.cap = c->cap;
     a.pos = c->d_pos;
     a.hi = c->d_hi;
@@ -191,7 +200,6 @@ ListArgs list_args(gm_ctx *c) {
     a.cell_start = c->d_cell_start;
     a.cell_cursor = c->d_cell_cursor;
     a.tmp_atom = c->d_tmp_atom;
-    a.max_cells = c->max_cells;
     a.type = c->d_type;
     a.charge = c->d_charge;
     a.charge64 = c->d_charge64;
@@ -210,6 +218,14 @@ ListArgs list_args(gm_ctx *c) {
     a.bbox_scratch = c->d_bbox;
     a.bbox_blocks = c->bbox_blocks;
     a.scan_scratch = c->d_scan;
+    a.scan_blocks = c->scan_blocks;
+    a.max_sys_atoms = c->max_sys_atoms;
+    a.sys_atom_off = c->d_sys_atom_off;
+    a.sys_slot_off = c->d_sys_slot_off;
+    a.sys_cell_off = c->d_sys_cell_off;
+    a.atom_sys = c->d_atom_sys;
+    a.group_sys = c->d_group_sys;
+    a.sys_flag = c->d_sys_flag;
     return a;
 }
 
@@ -217,6 +233,10 @@ ForceArgs force_args(gm_ctx *c) {
     ForceArgs a{};
     a.n = c->n;
     a.n_groups = c->n_groups;
+    a.n_slots = c->n_slots;
+    a.group_sys = c->d_group_sys;
+    a.atom_sys = c->d_atom_sys;
+    a.e_sys = c->n_sys > 1 ? c->d_e_sys : nullptr;
     a.cap = c->cap;
     a.split = c->fp64 ? 1 : c->split;
     a.hi = c->d_hi;
@@ -321,20 +341,25 @@ long long issue_shake(gm_ctx *c, cudaStream_t s, bool resident) {
 
 // ---- kernel sequences (each counted for gm_counters[3]) -------------------
 
-int seq_rebuild(gm_ctx *c, cudaStream_t s) {
+// The list rebuild of every system (all) or of the systems the rebuild check
+// flagged; the flags are cleared at the end.
+int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
     ListArgs a = list_args(c);
+    if (all) gm_launch_flags(a, true, s);
     gm_launch_wrap(a, c->d_pos, s);
     gm_launch_grid(a, s);
     gm_launch_bin(a, s);
     gm_launch_pack(a, c->fp64, s);
     gm_launch_build(a, s);
-    // wrap or bbox, grid, assign, 3 scan kernels, scatter, rank, pack, build
-    // (the two memsets are copy-engine work, not kernels)
-    return 10 + (a.periodic || a.n > 0 ? 1 : 0);
+    gm_launch_flags(a, false, s);
+    // [flags], wrap or bbox, grid, clear cells, assign, 3 scan kernels,
+    // scatter, rank, pack, build, clear flags
+    return (all ? 1 : 0) + 12 + (a.periodic || a.n > 0 ? 1 : 0);
 }
 
 int seq_forces(gm_ctx *c, cudaStream_t s) {
     ListArgs la = list_args(c);
+    if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);
     gm_launch_pack(la, c->fp64, s);
     ForceArgs fa = force_args(c);
     gm_launch_bonded(fa, c->fp64, s);
@@ -459,30 +484,37 @@ int ensure_list_buffers(gm_ctx *c, int cap) {
 }
 
 int estimate_cap(gm_ctx *c, const double *px, const double *py, const double *pz) {
-    double vol;
-    if (c->p.periodic) vol = c->p.box[0] * c->p.box[1] * c->p.box[2];
-    else {
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        const double *P[3] = {px, py, pz};
-        for (int i = 0; i < c->n; i++)
-            for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], P[d][i]); hi[d] = std::max(hi[d], P[d][i]); }
-        vol = 1.0;
-        for (int d = 0; d < 3; d++) vol *= std::max(hi[d] - lo[d], 2.0);
-    }
-    const double rho = c->n / std::max(vol, 1.0);
+    // densest system: its atoms over its bounding box (or the periodic box)
+    double est = 32.0;
     const double rl = c->p.r_skin;
-    double est = 1.35 * (4.0 / 3.0) * M_PI * rl * rl * rl * rho + 48.0;
-    est = std::min(est, (double)c->n + 32.0);
+    for (int sy = 0; sy < c->n_sys; sy++) {
+        const int a0 = c->h_atom_off[(size_t)sy], a1 = c->h_atom_off[(size_t)sy + 1];
+        double vol;
+        if (c->p.periodic) vol = c->p.box[0] * c->p.box[1] * c->p.box[2];
+        else {
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            const double *P[3] = {px, py, pz};
+            for (int i = a0; i < a1; i++)
+                for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], P[d][i]); hi[d] = std::max(hi[d], P[d][i]); }
+            vol = 1.0;
+            for (int d = 0; d < 3; d++) vol *= std::max(hi[d] - lo[d], 2.0);
+        }
+        const double rho = (a1 - a0) / std::max(vol, 1.0);
+        double e = 1.35 * (4.0 / 3.0) * M_PI * rl * rl * rl * rho + 48.0;
+        e = std::min(e, (double)(a1 - a0) + 32.0);
+        est = std::max(est, e);
+    }
     int cap = ((int)std::ceil(est) + 31) / 32 * 32;
     return std::max(cap, 32);
 }
 
-int do_build(gm_ctx *c) {
-    // list build on the resident positions, growing the capacity on overflow
+int do_build(gm_ctx *c, bool all = true) {
+    // list build on the resident positions (every system, or the flagged
+    // ones), growing the capacity on overflow (then rebuilding every system)
     for (int attempt = 0; attempt < 6; attempt++) {
         int rc = reset_status(c);
         if (rc) return rc;
-        c->launches += seq_rebuild(c, c->stream);
+        c->launches += seq_rebuild(c, c->stream, all || attempt > 0);
         rc = check_status(c, nullptr);
         if (rc == GM_ERR_LIST_OVERFLOW) {
             int newcap = ((int)(c->cap * 1.5) + 31) / 32 * 32;
@@ -530,7 +562,9 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
         gm_launch_resync(n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, s); k++;
     }
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
-    gm_launch_check(n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, cond, gm_check_blocks(n), s); k++;
+    gm_launch_check(n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, cond, gm_check_blocks(n), c->d_atom_sys,
+                    c->d_sys_flag, s);
+    k++;
     *count += k;
     return GM_OK;
 }
@@ -570,7 +604,7 @@ int capture_graph(gm_ctx *c, double dt) {
     GM_CUDA(c, cudaGraphAddNode(&cnode, capg, deps, edges, ndeps, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     GM_CUDA(c, cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    seq_rebuild(c, c->side);
+    seq_rebuild(c, c->side, false);
     GM_CUDA(c, cudaStreamEndCapture(c->side, &body));
     GM_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
     issue_step_tail(c, c->stream, dt, &count);
@@ -592,7 +626,7 @@ int run_direct(gm_ctx *c, double dt, int64_t n_steps) {
         issue_step(c, c->stream, dt, 0ull, &count);
         int rc = st_read(c);
         if (rc) return rc;
-        if (c->h_status->rebuild && !c->h_status->error) count += seq_rebuild(c, c->stream);
+        if (c->h_status->rebuild && !c->h_status->error) count += seq_rebuild(c, c->stream, false);
         issue_step_tail(c, c->stream, dt, &count);
         c->launches += count;
     }
@@ -612,13 +646,14 @@ int ensure_forces(gm_ctx *c) {
         if (rc) return rc;
         const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;
         gm_launch_check(c->n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, 0ull, gm_check_blocks(c->n),
+                        c->d_atom_sys, c->d_sys_flag,
                         c->stream);
         c->launches++;
         rc = st_read(c);
         if (rc) return rc;
         if (c->h_status->error & GM_DEV_NONFINITE_POS) return fail(c, GM_ERR_NONFINITE, "non-finite position");
         if (c->h_status->rebuild) {
-            rc = do_build(c);
+            rc = do_build(c, false);  // the flagged systems
             if (rc) return rc;
         }
     }
@@ -729,16 +764,116 @@ void ws_init_params(uint64_t seed, std::vector<float> &P) {
 
 }  // namespace
 
+namespace {
+
+// Systems of a batch merged into one context: atom arrays concatenated,
+// topology indices shifted by each system's first atom.
+struct Merged {
+    std::vector<int> atom_off;
+    std::vector<double> sigma, eps, mass, charge;
+    std::vector<uint8_t> element;
+    std::vector<uint32_t> bi, bj, ai, aj, ak, di, dj, dk, dl, dn, ci, cj, ei, ej;
+    std::vector<double> bk, br0, akth, ath0, dkphi, ddelta, cdsq;
+    bool has_element = false;
+    gm_atoms A{};
+    gm_topology T{};
+};
+
+// Returns false when a system's arrays or indices are invalid.
+bool merge_systems(int n_sys, const gm_atoms *atoms, const gm_topology *topos, Merged &m) {
+    m.atom_off.assign(1, 0);
+    for (int s = 0; s < n_sys; s++) {
+        const gm_atoms &a = atoms[s];
+        if (a.n_atoms < 0 || (a.n_atoms > 0 && (!a.sigma || !a.epsilon || !a.mass))) return false;
+        if ((long long)m.atom_off.back() + a.n_atoms > INT32_MAX / 2) return false;
+        m.atom_off.push_back(m.atom_off.back() + (int)a.n_atoms);
+        if (a.element) m.has_element = true;
+    }
+    for (int s = 0; s < n_sys; s++) {
+        const gm_atoms &a = atoms[s];
+        const gm_topology &t = topos[s];
+        const uint32_t n = (uint32_t)a.n_atoms, off = (uint32_t)m.atom_off[(size_t)s];
+        for (int64_t i = 0; i < a.n_atoms; i++) {
+            m.sigma.push_back(a.sigma[i]);
+            m.eps.push_back(a.epsilon[i]);
+            m.mass.push_back(a.mass[i]);
+            m.charge.push_back(a.charge ? a.charge[i] : 0.0);
+            m.element.push_back(a.element ? a.element[i] : (uint8_t)1);
+        }
+        auto idx = [&](const uint32_t *src, int64_t cnt, std::vector<uint32_t> &dst) {
+            if (cnt > 0 && !src) return false;
+            for (int64_t k = 0; k < cnt; k++) {
+                if (src[k] >= n) return false;
+                dst.push_back(src[k] + off);
+            }
+            return true;
+        };
+        auto val = [](const double *src, int64_t cnt, std::vector<double> &dst) {
+            if (cnt > 0 && !src) return false;
+            dst.insert(dst.end(), src, src + cnt);
+            return true;
+        };
+        if (t.n_bonds < 0 || t.n_angles < 0 || t.n_diheds < 0 || t.n_constr < 0 || t.n_excl < 0) return false;
+        if (!idx(t.bond_i, t.n_bonds, m.bi) || !idx(t.bond_j, t.n_bonds, m.bj) || !val(t.bond_k, t.n_bonds, m.bk) ||
+            !val(t.bond_r0, t.n_bonds, m.br0) || !idx(t.angle_i, t.n_angles, m.ai) ||
+            !idx(t.angle_j, t.n_angles, m.aj) || !idx(t.angle_k, t.n_angles, m.ak) ||
+            !val(t.angle_kth, t.n_angles, m.akth) || !val(t.angle_th0, t.n_angles, m.ath0) ||
+            !idx(t.dihed_i, t.n_diheds, m.di) || !idx(t.dihed_j, t.n_diheds, m.dj) ||
+            !idx(t.dihed_k, t.n_diheds, m.dk) || !idx(t.dihed_l, t.n_diheds, m.dl) ||
+            !val(t.dihed_kphi, t.n_diheds, m.dkphi) || !val(t.dihed_delta, t.n_diheds, m.ddelta) ||
+            !idx(t.constr_i, t.n_constr, m.ci) || !idx(t.constr_j, t.n_constr, m.cj) ||
+            !val(t.constr_dsq, t.n_constr, m.cdsq) || !idx(t.excl_i, t.n_excl, m.ei) || !idx(t.excl_j, t.n_excl, m.ej))
+            return false;
+        if (t.n_diheds > 0 && !t.dihed_n) return false;
+        m.dn.insert(m.dn.end(), t.dihed_n, t.dihed_n + t.n_diheds);  // a multiplicity, not an index
+    }
+    const int64_t n = m.atom_off.back();
+    m.A = gm_atoms{n, m.sigma.data(), m.eps.data(), m.mass.data(), m.charge.data(),
+                   m.has_element ? m.element.data() : nullptr};
+    gm_topology &T = m.T;
+    T.n_bonds = (int64_t)m.bi.size(); T.bond_i = m.bi.data(); T.bond_j = m.bj.data(); T.bond_k = m.bk.data();
+    T.bond_r0 = m.br0.data();
+    T.n_angles = (int64_t)m.ai.size(); T.angle_i = m.ai.data(); T.angle_j = m.aj.data(); T.angle_k = m.ak.data();
+    T.angle_kth = m.akth.data(); T.angle_th0 = m.ath0.data();
+    T.n_diheds = (int64_t)m.di.size(); T.dihed_i = m.di.data(); T.dihed_j = m.dj.data(); T.dihed_k = m.dk.data();
+    T.dihed_l = m.dl.data(); T.dihed_kphi = m.dkphi.data(); T.dihed_n = m.dn.data(); T.dihed_delta = m.ddelta.data();
+    T.n_constr = (int64_t)m.ci.size(); T.constr_i = m.ci.data(); T.constr_j = m.cj.data(); T.constr_dsq = m.cdsq.data();
+    T.n_excl = (int64_t)m.ei.size(); T.excl_i = m.ei.data(); T.excl_j = m.ej.data();
+    return true;
+}
+
+gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys_topos, const gm_params *params,
+                    int32_t *status);
+
+}  // namespace
+
 extern "C" {
 
 gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *params, int32_t *status) {
+    return create_impl(1, atoms, t, params, status);
+}
+
+gm_ctx *gm_create_ensemble(int32_t n_systems, const gm_atoms *atoms, const gm_topology *topos, const gm_params *params,
+                           int32_t *status) {
+    return create_impl(n_systems, atoms, topos, params, status);
+}
+
+}  // extern "C"
+
+namespace {
+
+gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys_topos, const gm_params *params,
+                    int32_t *status) {
     int32_t dummy;
     if (!status) status = &dummy;
     *status = GM_OK;
-    if (!atoms || !t || !params || atoms->n_atoms < 0 || atoms->n_atoms > INT32_MAX / 2) {
+    Merged mg;
+    if (n_sys < 1 || !sys_atoms || !sys_topos || !params || !merge_systems(n_sys, sys_atoms, sys_topos, mg)) {
         *status = GM_ERR_INVALID_ARGUMENT;
         return nullptr;
     }
+    const gm_atoms *atoms = &mg.A;
+    const gm_topology *t = &mg.T;
     const gm_params &p = *params;
     // config.rs:213-248 validation
     if (!(p.r_switch < p.r_cutoff && p.r_cutoff < p.r_skin) || !(p.box[0] > 0 && p.box[1] > 0 && p.box[2] > 0) ||
@@ -777,35 +912,46 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
     int rc;
 #define TRY(x) do { rc = (x); if (rc) return bail(rc); } while (0)
-    // ---- atoms: deduplicate (sigma, epsilon) into types
-    std::map<std::pair<double, double>, int> types;
+    // ---- atoms: deduplicate (sigma, epsilon) into types, per system (the
+    // systems of a batch never interact, so each has its own type table)
+    c->n_sys = n_sys;
+    c->h_atom_off = mg.atom_off;
     std::vector<int> type((size_t)n);
-    std::vector<double> tsig, teps;
-    for (int i = 0; i < n; i++) {
-        auto key = std::make_pair(atoms->sigma[i], atoms->epsilon[i]);
-        auto it = types.find(key);
-        if (it == types.end()) {
-            it = types.emplace(key, (int)tsig.size()).first;
-            tsig.push_back(key.first);
-            teps.push_back(key.second);
+    std::vector<std::vector<double>> tsig((size_t)n_sys), teps((size_t)n_sys);
+    for (int sy = 0; sy < n_sys; sy++) {
+        std::map<std::pair<double, double>, int> types;
+        for (int i = mg.atom_off[(size_t)sy]; i < mg.atom_off[(size_t)sy + 1]; i++) {
+            auto key = std::make_pair(atoms->sigma[i], atoms->epsilon[i]);
+            auto it = types.find(key);
+            if (it == types.end()) {
+                it = types.emplace(key, (int)tsig[(size_t)sy].size()).first;
+                tsig[(size_t)sy].push_back(key.first);
+                teps[(size_t)sy].push_back(key.second);
+            }
+            type[(size_t)i] = it->second;
         }
-        type[(size_t)i] = it->second;
+        c->ntypes = std::max(c->ntypes, std::max((int)tsig[(size_t)sy].size(), 1));
     }
-    c->ntypes = std::max((int)tsig.size(), 1);
     if (c->ntypes > GM_MAX_TYPES) {
-        fail(c, GM_ERR_UNSUPPORTED, "%d distinct (sigma, epsilon) pairs; at most %d are supported", c->ntypes, GM_MAX_TYPES);
+        fail(c, GM_ERR_UNSUPPORTED, "%d distinct (sigma, epsilon) pairs in a system; at most %d are supported",
+             c->ntypes, GM_MAX_TYPES);
         return bail(GM_ERR_UNSUPPORTED);
     }
-    std::vector<float2> tab32((size_t)c->ntypes * c->ntypes);
-    std::vector<double2> tab64((size_t)c->ntypes * c->ntypes);
-    for (int a = 0; a < (int)tsig.size(); a++)
-        for (int b = 0; b < (int)tsig.size(); b++) {
-            // nonbonded.rs:46-47 Lorentz-Berthelot, evaluated as the reference does
-            const double sg = 0.5 * (tsig[(size_t)a] + tsig[(size_t)b]);
-            const double ep = std::sqrt(teps[(size_t)a] * teps[(size_t)b]);
-            tab64[(size_t)a * c->ntypes + b] = make_double2(sg, ep);
-            tab32[(size_t)a * c->ntypes + b] = make_float2((float)(sg * sg), (float)ep);
-        }
+    const size_t T2 = (size_t)c->ntypes * c->ntypes;
+    std::vector<float2> tab32(T2 * (size_t)n_sys, make_float2(0.f, 0.f));
+    std::vector<double2> tab64(T2 * (size_t)n_sys, make_double2(0.0, 0.0));
+    for (int sy = 0; sy < n_sys; sy++) {
+        const auto &sg_ = tsig[(size_t)sy];
+        const auto &ep_ = teps[(size_t)sy];
+        for (size_t a = 0; a < sg_.size(); a++)
+            for (size_t b = 0; b < sg_.size(); b++) {
+                // nonbonded.rs:46-47 Lorentz-Berthelot, evaluated as the reference does
+                const double sg = 0.5 * (sg_[a] + sg_[b]);
+                const double ep = std::sqrt(ep_[a] * ep_[b]);
+                tab64[T2 * (size_t)sy + a * (size_t)c->ntypes + b] = make_double2(sg, ep);
+                tab32[T2 * (size_t)sy + a * (size_t)c->ntypes + b] = make_float2((float)(sg * sg), (float)ep);
+            }
+    }
     std::vector<double> inv_mass((size_t)n), charge64((size_t)n);
     std::vector<float> charge((size_t)n);
     for (int i = 0; i < n; i++) {
@@ -948,29 +1094,77 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     TRY(dalloc(c, &c->d_fout, 3 * (size_t)n));
     TRY(dalloc(c, &c->d_host_f, 3 * (size_t)n));
     TRY(dalloc(c, &c->d_force, 3 * (size_t)n));
-    TRY(dalloc(c, &c->d_hi, (size_t)n));
-    TRY(dalloc(c, &c->d_lo, (size_t)n));
-    if (c->fp64) {
-        TRY(dalloc(c, &c->d_pos64s, (size_t)n));
-        TRY(dalloc(c, &c->d_type_sorted, (size_t)n));
+    // ---- systems: 32-aligned slot ranges, cell budgets, lookup tables
+    {
+        std::vector<int> slot_off(1, 0), cell_off(1, 0), atom_sys((size_t)n), group_sys;
+        long long full_cells = 0;
+        for (int sy = 0; sy < n_sys; sy++) {
+            const long long ns = mg.atom_off[(size_t)sy + 1] - mg.atom_off[(size_t)sy];
+            full_cells += std::min<long long>(std::max<long long>(8LL * ns, 1LL << 20), 1LL << 27) + 1;
+        }
+        const bool small_budget = full_cells > (1LL << 30);
+        for (int sy = 0; sy < n_sys; sy++) {
+            const int ns = mg.atom_off[(size_t)sy + 1] - mg.atom_off[(size_t)sy];
+            c->max_sys_atoms = std::max(c->max_sys_atoms, ns);
+            for (int i = mg.atom_off[(size_t)sy]; i < mg.atom_off[(size_t)sy + 1]; i++) atom_sys[(size_t)i] = sy;
+            const int padded = (ns + 31) / 32 * 32;
+            for (int g = 0; g < padded / 32; g++) group_sys.push_back(sy);
+            slot_off.push_back(slot_off.back() + padded);
+            // cell budget: a few cells per atom, at least 2^20 (the grid of a
+            // swollen droplet in vacuum stays fine-grained); 12 bytes per cell.
+            // A batch gives each system the budget it has alone (so its grid,
+            // sorted order and sums are the same) while the total stays below
+            // 2^30 cells, else 8 cells per atom.
+            const long long cells = small_budget ? std::max<long long>(8LL * ns, 1LL << 15)
+                                                 : std::min<long long>(std::max<long long>(8LL * ns, 1LL << 20), 1LL << 27);
+            if ((long long)cell_off.back() + cells + 1 > INT32_MAX) {
+                fail(c, GM_ERR_UNSUPPORTED, "cell budget of the batch exceeds 2^31");
+                return bail(GM_ERR_UNSUPPORTED);
+            }
+            cell_off.push_back(cell_off.back() + (int)cells + 1);
+            c->scan_blocks = std::max(c->scan_blocks, (int)((cells + 1 + 1023) / 1024));
+        }
+        c->n_slots = slot_off.back();
+        c->total_cells = cell_off.back();
+        TRY(dupload(c, &c->d_sys_atom_off, mg.atom_off.data(), mg.atom_off.size()));
+        TRY(dupload(c, &c->d_sys_slot_off, slot_off.data(), slot_off.size()));
+        TRY(dupload(c, &c->d_sys_cell_off, cell_off.data(), cell_off.size()));
+        TRY(dupload(c, &c->d_atom_sys, atom_sys.data(), atom_sys.size()));
+        TRY(dupload(c, &c->d_group_sys, group_sys.data(), group_sys.size()));
+        TRY(dalloc(c, &c->d_sys_flag, (size_t)n_sys));
+        TRY(dalloc(c, &c->d_e_sys, (size_t)n_sys));
+        cudaMemset(c->d_sys_flag, 0, sizeof(unsigned int) * (size_t)n_sys);
+        cudaMemset(c->d_e_sys, 0, sizeof(long long) * (size_t)n_sys);
     }
-    TRY(dalloc(c, &c->d_perm, (size_t)n));
+    const size_t ns_ = (size_t)c->n_slots;
+    TRY(dalloc(c, &c->d_hi, ns_));
+    TRY(dalloc(c, &c->d_lo, ns_));
+    cudaMemset(c->d_hi, 0, sizeof(float4) * ns_);
+    cudaMemset(c->d_lo, 0, sizeof(float4) * ns_);
+    if (c->fp64) {
+        TRY(dalloc(c, &c->d_pos64s, ns_));
+        TRY(dalloc(c, &c->d_type_sorted, ns_));
+        cudaMemset(c->d_pos64s, 0, sizeof(double4) * ns_);
+        cudaMemset(c->d_type_sorted, 0, sizeof(int) * ns_);
+    }
+    TRY(dalloc(c, &c->d_perm, ns_));
+    cudaMemset(c->d_perm, 0xFF, sizeof(int) * ns_);  // -1: padding until a build fills the slot
     TRY(dalloc(c, &c->d_cell_of, (size_t)n));
-    TRY(dalloc(c, &c->d_cell_sorted, (size_t)n));
-    TRY(dalloc(c, &c->d_tmp_atom, (size_t)n));
-    // cell budget: a few cells per atom, at least 2^20 (the grid of a swollen
-    // droplet in vacuum stays fine-grained); 12 bytes per cell
-    c->max_cells = (int)std::min<long long>(std::max<long long>(8LL * n, 1LL << 20), 1LL << 27);
-    TRY(dalloc(c, &c->d_scan, (size_t)(c->max_cells + 1 + 1023) / 1024 + 1));
-    TRY(dalloc(c, &c->d_cell_count, (size_t)c->max_cells));
-    TRY(dalloc(c, &c->d_cell_cursor, (size_t)c->max_cells));
-    TRY(dalloc(c, &c->d_cell_start, (size_t)c->max_cells + 1));
-    TRY(dalloc(c, &c->d_grid, 1));
-    c->bbox_blocks = std::max(1, std::min(256, (n + 255) / 256));
-    TRY(dalloc(c, &c->d_bbox, 9 * (size_t)c->bbox_blocks));
-    c->n_groups = (n + 31) / 32;
-    TRY(dalloc(c, &c->d_count, (size_t)c->n_groups * 32));
+    TRY(dalloc(c, &c->d_cell_sorted, ns_));
+    TRY(dalloc(c, &c->d_tmp_atom, ns_));
+    TRY(dalloc(c, &c->d_scan, (size_t)c->scan_blocks * n_sys));
+    TRY(dalloc(c, &c->d_cell_count, (size_t)c->total_cells));
+    TRY(dalloc(c, &c->d_cell_cursor, (size_t)c->total_cells));
+    TRY(dalloc(c, &c->d_cell_start, (size_t)c->total_cells));
+    TRY(dalloc(c, &c->d_grid, (size_t)n_sys));
+    cudaMemset(c->d_grid, 0, sizeof(GridInfo) * (size_t)n_sys);
+    c->bbox_blocks = std::max(1, std::min(256, (c->max_sys_atoms + 255) / 256));
+    TRY(dalloc(c, &c->d_bbox, 9 * (size_t)c->bbox_blocks * n_sys));
+    c->n_groups = c->n_slots / 32;
+    TRY(dalloc(c, &c->d_count, ns_));
+    cudaMemset(c->d_count, 0, sizeof(int) * ns_);  // padding slots keep count 0
     TRY(dalloc(c, &c->d_gmax, (size_t)c->n_groups));
+    cudaMemset(c->d_gmax, 0, sizeof(int) * (size_t)c->n_groups);
     c->n_epart = c->n_groups * GM_MAX_SPLIT + c->bonded_blocks + c->blocks14;
     {
         // enough warps in flight to hide the gather latency: about 48 per SM
@@ -998,6 +1192,10 @@ gm_ctx *gm_create(const gm_atoms *atoms, const gm_topology *t, const gm_params *
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(GM_ERR_DEVICE);
     return c;
 }
+
+}  // namespace
+
+extern "C" {
 
 int32_t gm_destroy(gm_ctx *c) {
     if (!c) return GM_OK;
@@ -1080,11 +1278,14 @@ int32_t gm_needs_rebuild(gm_ctx *c, const double *px, const double *py, const do
     rc = reset_status(c);
     if (rc) return rc;
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;
-    gm_launch_check(c->n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, 0ull, gm_check_blocks(c->n), c->stream);
-    c->launches++;
+    gm_launch_check(c->n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, 0ull, gm_check_blocks(c->n),
+                    c->d_atom_sys, c->d_sys_flag, c->stream);
     rc = st_read(c);
     if (rc) return rc;
     *result = c->h_status->rebuild ? 1 : 0;
+    gm_launch_flags(list_args(c), false, c->stream);  // a query: leave no system marked
+    c->launches += 2;
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
     return GM_OK;
 }
 
@@ -1162,16 +1363,17 @@ int32_t gm_get_pairs(gm_ctx *c, int64_t cap, uint32_t *pair_i, uint32_t *pair_j,
     if (!c || !n_pairs) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
     if (!c->built) return fail(c, GM_ERR_NOT_BUILT, "no neighbour list");
-    const int n = c->n;
-    std::vector<int> perm((size_t)n), count((size_t)c->n_groups * 32), list((size_t)c->n_groups * 32 * c->cap);
+    const int ns = c->n_slots;
+    std::vector<int> perm((size_t)ns), count((size_t)ns), list((size_t)ns * c->cap);
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (n) {
-        GM_CUDA(c, cudaMemcpy(perm.data(), c->d_perm, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
-        GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+    if (ns) {
+        GM_CUDA(c, cudaMemcpy(perm.data(), c->d_perm, sizeof(int) * (size_t)ns, cudaMemcpyDeviceToHost));
+        GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)ns, cudaMemcpyDeviceToHost));
         GM_CUDA(c, cudaMemcpy(list.data(), c->d_list, sizeof(int) * list.size(), cudaMemcpyDeviceToHost));
     }
     std::vector<uint64_t> keys;
-    for (int s = 0; s < n; s++) {
+    for (int s = 0; s < ns; s++) {
+        if (perm[(size_t)s] < 0) continue;  // padding slot
         const int g = s / 32, l = s % 32;
         for (int e = 0; e < count[(size_t)s]; e++) {
             const int j = list[(size_t)g * 32 * c->cap + (size_t)e * 32 + l];
@@ -1246,7 +1448,7 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
         switch (which) {
             case 0: gm_launch_pair(fa, c->fp64, c->stream); break;
             case 1: gm_launch_bonded(fa, c->fp64, c->stream); break;
-            case 2: seq_rebuild(c, c->stream); break;
+            case 2: seq_rebuild(c, c->stream, true); break;
             case 3:
                 if (c->use_graph) cudaGraphLaunch(c->graph_exec, c->stream);
                 else run_direct(c, dt, 1);
@@ -1392,8 +1594,9 @@ int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {
                      (int64_t)st.rattle_sum, (int64_t)st.rec_n};
     if (c->built && n > 0) {
         // pairs in the current list (half of the symmetric entries)
-        std::vector<int> count((size_t)c->n);
-        if (c->n) GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)c->n, cudaMemcpyDeviceToHost));
+        std::vector<int> count((size_t)c->n_slots);
+        if (c->n_slots)
+            GM_CUDA(c, cudaMemcpy(count.data(), c->d_count, sizeof(int) * (size_t)c->n_slots, cudaMemcpyDeviceToHost));
         long long s = 0;
         for (int x : count) s += x;
         v[0] = s / 2;
@@ -1565,6 +1768,48 @@ int32_t gm_ws_last(gm_ctx *c, float *feat, double *lam0, double *lam_sum) {
     if (feat) GM_CUDA(c, cudaMemcpy(feat, c->d_ws_feat, sizeof(float) * GM_WS_IN * nc, cudaMemcpyDeviceToHost));
     if (lam0) GM_CUDA(c, cudaMemcpy(lam0, c->d_ws_lam0, sizeof(double) * nc, cudaMemcpyDeviceToHost));
     if (lam_sum) GM_CUDA(c, cudaMemcpy(lam_sum, c->d_lam_sum, sizeof(double) * nc, cudaMemcpyDeviceToHost));
+    return GM_OK;
+}
+
+/* ---- batches of independent systems ----------------------------------- */
+
+int32_t gm_ensemble_info(const gm_ctx *c, int64_t *atom_offsets) {
+    if (!c || !atom_offsets) return GM_ERR_INVALID_ARGUMENT;
+    for (int sy = 0; sy <= c->n_sys; sy++) atom_offsets[sy] = c->h_atom_off[(size_t)sy];
+    return GM_OK;
+}
+
+int32_t gm_ensemble_energies(gm_ctx *c, double *e_pot, double *e_kin) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (e_pot) {
+        if (!c->forces_current) return fail(c, GM_ERR_NOT_BUILT, "no forces evaluated at the current positions");
+        if (c->n_sys == 1) {
+            GM_CUDA(c, cudaMemcpy(e_pot, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<long long> q((size_t)c->n_sys);
+            GM_CUDA(c, cudaMemcpy(q.data(), c->d_e_sys, sizeof(long long) * q.size(), cudaMemcpyDeviceToHost));
+            for (int sy = 0; sy < c->n_sys; sy++) e_pot[sy] = (double)q[(size_t)sy] / GM_EFIX_SCALE;
+        }
+    }
+    if (e_kin) {
+        // lib.rs:68-77 per system, in atom order
+        const size_t n = (size_t)c->n;
+        std::vector<double> v(3 * n), m(n);
+        if (n) {
+            GM_CUDA(c, cudaMemcpy(v.data(), c->d_vel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost));
+            GM_CUDA(c, cudaMemcpy(m.data(), c->d_mass, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        }
+        for (int sy = 0; sy < c->n_sys; sy++) {
+            double sum = 0.0;
+            for (int i = c->h_atom_off[(size_t)sy]; i < c->h_atom_off[(size_t)sy + 1]; i++) {
+                const double vx = v[(size_t)i], vy = v[n + (size_t)i], vz = v[2 * n + (size_t)i];
+                sum += m[(size_t)i] * (vx * vx + vy * vy + vz * vz);
+            }
+            e_kin[sy] = 0.5 * sum * (1.0 / (20.455 * 20.455));
+        }
+    }
     return GM_OK;
 }
 

@@ -24,26 +24,33 @@ constexpr double kCoulomb64 = 332.0522173;
 // 32-entry summation chunk.  The split raises the number of warps in flight
 // (a 50k-atom system has only 1,563 groups), and integer partial sums keep the
 // result independent of the order in which the parts land.
-template <bool PERIODIC, bool COULOMB>
+// BATCH: systems of a batch have their own type tables ([system][type][type],
+// read through L1); a single system keeps its table in shared memory.
+template <bool PERIODIC, bool COULOMB, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32)
-pair_kernel_f32(int n, int cap, int split, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
                 const int *__restrict__ gmax, int ntypes, const float2 *__restrict__ tab, float rc2, float rsw,
                 float inv_wsw, float bx, float by, float bz, float ibx, float iby, float ibz,
-                long long *__restrict__ force, double *__restrict__ epart, DevStatus *st) {
+                long long *__restrict__ force, double *__restrict__ epart, DevStatus *st,
+                const int *__restrict__ group_sys, long long *e_sys) {
     extern __shared__ float2 s_tab[];
-    for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab[t] = tab[t];
-    __syncthreads();
+    if (!BATCH) {
+        for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab[t] = tab[t];
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
     const int group = wid / split, part = wid - group * split;
-    if (group * 32 >= n) return;
+    if (group * 32 >= n_slots) return;
     const int s = group * 32 + lane;
-    const bool valid = s < n;
+    const int atom = perm[s];  // -1 on a padding slot
+    const bool valid = atom >= 0;
     float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
     int cnt = 0;
     if (valid) { mh = hi[s]; ml = lo[s]; cnt = count[s]; }
-    const float2 *trow = s_tab + (valid ? __float_as_int(mh.w) : 0) * ntypes;
+    const float2 *trow = (BATCH ? tab + (size_t)group_sys[group] * ntypes * ntypes : s_tab) +
+                         (valid ? __float_as_int(mh.w) : 0) * ntypes;
     const float qi = ml.w * kCoulomb;
     const int gm = gmax[group];
     const int per = ((gm + split - 1) / split + kChunk - 1) / kChunk * kChunk;
@@ -72,7 +79,7 @@ pair_kernel_f32(int n, int cap, int split, const float4 *__restrict__ hi, const 
             }
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 <= rc2 && r2 > 0.f) {
-                const float2 p = trow[__float_as_int(jh.w)];
+                const float2 p = BATCH ? __ldg(trow + __float_as_int(jh.w)) : trow[__float_as_int(jh.w)];
                 // rsqrtf plus one Newton step: the pair sums cancel to
                 // small net forces, so the last ulps of 1/r matter
                 float rinv = rsqrtf(r2);
@@ -109,36 +116,39 @@ pair_kernel_f32(int n, int cap, int split, const float4 *__restrict__ hi, const 
         eacc += (double)ev;
     }
     if (valid && e_begin < e_end) {
-        const int a = perm[s];
-        gm_atomic_fix_add(force + a, ax);
-        gm_atomic_fix_add(force + n + a, ay);
-        gm_atomic_fix_add(force + 2 * n + a, az);
+        gm_atomic_fix_add(force + atom, ax);
+        gm_atomic_fix_add(force + n + atom, ay);
+        gm_atomic_fix_add(force + 2 * n + atom, az);
     }
     for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
     if (lane == 0) epart[wid] = 0.5 * eacc;
+    if (e_sys && lane == 0) gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
 }
 
-template <bool PERIODIC, bool COULOMB>
+template <bool PERIODIC, bool COULOMB, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32)
-pair_kernel_f64(int n, int cap, const double4 *__restrict__ p64, const int *__restrict__ type_s,
+pair_kernel_f64(int n, int n_slots, int cap, const double4 *__restrict__ p64, const int *__restrict__ type_s,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
                 const int *__restrict__ gmax, int ntypes, const double2 *__restrict__ tab, double rc2, double rsw,
                 double rc, double bx, double by, double bz, long long *__restrict__ force,
-                double *__restrict__ epart, DevStatus *st) {
+                double *__restrict__ epart, DevStatus *st, const int *__restrict__ group_sys, long long *e_sys) {
     extern __shared__ double2 s_tab64[];
-    for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab64[t] = tab[t];
-    __syncthreads();
+    if (!BATCH) {
+        for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab64[t] = tab[t];
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int group = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
-    if (group * 32 >= n) return;
+    if (group * 32 >= n_slots) return;
     const int s = group * 32 + lane;
-    const bool valid = s < n;
+    const int atom = perm[s];  // -1 on a padding slot
+    const bool valid = atom >= 0;
     double4 mi = make_double4(0, 0, 0, 0);
     int cnt = 0, ti = 0;
     if (valid) { mi = p64[s]; cnt = count[s]; ti = type_s[s]; }
-    const double2 *trow = s_tab64 + ti * ntypes;
+    const double2 *trow = (BATCH ? tab + (size_t)group_sys[group] * ntypes * ntypes : s_tab64) + ti * ntypes;
     const double qi = mi.w * kCoulomb64;
     const int gm = gmax[group];
     const int *L = list + (size_t)group * 32 * cap + lane;
@@ -187,13 +197,13 @@ pair_kernel_f64(int n, int cap, const double4 *__restrict__ p64, const int *__re
     }
     unsigned int bad = 0;
     if (valid) {
-        const int a = perm[s];
-        gm_atomic_fix_add(force + a, gm_to_fix_checked(fx, bad));
-        gm_atomic_fix_add(force + n + a, gm_to_fix_checked(fy, bad));
-        gm_atomic_fix_add(force + 2 * n + a, gm_to_fix_checked(fz, bad));
+        gm_atomic_fix_add(force + atom, gm_to_fix_checked(fx, bad));
+        gm_atomic_fix_add(force + n + atom, gm_to_fix_checked(fy, bad));
+        gm_atomic_fix_add(force + 2 * n + atom, gm_to_fix_checked(fz, bad));
     }
     for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
     if (lane == 0) epart[group] = 0.5 * eacc;
+    if (e_sys && lane == 0) gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
 }
@@ -233,12 +243,14 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
     const int n = a.n;
     double e = 0.0;
     unsigned bad = 0;
+    int first = -1;  // an atom of the term: its system owns the energy
     if (t < a.n_bonds) {
         // force/bonded.rs:5-40, V = k (r - r0)^2.  FP64 in both paths: a bond
         // stretched across a wrapped periodic boundary carries forces ~1e5
         // kcal/mol/A whose FP32 rounding would swamp small net forces (the
         // reference's GPU backend also keeps bonded terms in FP64).
         const int i = a.bond_i[t], j = a.bond_j[t];
+        first = i;
         const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
         const double k = a.bond_k[t], r0 = a.bond_r0[t];
         const double r2 = dx * dx + dy * dy + dz * dz;
@@ -254,6 +266,7 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         // force/bonded.rs:44-102, V = k (theta - theta0)^2
         const int q = t - a.n_bonds;
         const int i = a.angle_i[q], j = a.angle_j[q], kk = a.angle_k[q];
+        first = i;
         const V3<T> b1 = diff<T>(a.pos, n, i, j), b2 = diff<T>(a.pos, n, kk, j);
         const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
         if (r1 != (T)0 && r2 != (T)0) {
@@ -284,6 +297,7 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         // force/bonded.rs:112-164, V = k [1 + cos(n phi - delta)]
         const int q = t - a.n_bonds - a.n_angles;
         const int i = a.dihed_i[q], j = a.dihed_j[q], k = a.dihed_k[q], l = a.dihed_l[q];
+        first = i;
         const V3<T> b1 = diff<T>(a.pos, n, j, i), b2 = diff<T>(a.pos, n, k, j), b3 = diff<T>(a.pos, n, l, k);
         const V3<T> m = cross(b1, b2), nv = cross(b2, b3);
         const T m2 = dot(m, m), n2 = dot(nv, nv), b2l = sqrt(dot(b2, b2));
@@ -316,6 +330,7 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         __syncthreads();
     }
     if (threadIdx.x == 0) a.epart_bonded[blockIdx.x] = se[0];
+    if (a.e_sys) gm_add_sys_energy(a.e_sys, first >= 0 ? a.atom_sys[first] : -1, e);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
 }
@@ -327,8 +342,10 @@ __global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
     const int n = a.n;
     double e = 0.0;
     unsigned bad = 0;
+    int first = -1;
     if (t < a.n14) {
         const int i = a.p14_i[t], j = a.p14_j[t];
+        first = i;
         const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 > 0.0) {
@@ -359,6 +376,7 @@ __global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
         __syncthreads();
     }
     if (threadIdx.x == 0) a.epart14[blockIdx.x] = se[0];
+    if (a.e_sys) gm_add_sys_energy(a.e_sys, first >= 0 ? a.atom_sys[first] : -1, e);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
 }
@@ -388,24 +406,31 @@ int gm_bonded_blocks(int nb, int na, int nd) {
 void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.n == 0) return;
     const int blocks = (a.n_groups + kPairWarps - 1) / kPairWarps;
+    const bool batch = a.e_sys != nullptr;
     if (!fp64) {
         const int blocks32 = (a.n_groups * a.split + kPairWarps - 1) / kPairWarps;
-        const size_t smem = sizeof(float2) * (size_t)a.ntypes * a.ntypes;
-#define GM_PAIR32(P, Q)                                                                                   \
-    pair_kernel_f32<P, Q><<<blocks32, kPairWarps * 32, smem, s>>>(                                        \
-        a.n, a.cap, a.split, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, a.inv_wsw, \
-        a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status)
-        if (a.periodic) { if (a.coulomb) GM_PAIR32(true, true); else GM_PAIR32(true, false); }
-        else { if (a.coulomb) GM_PAIR32(false, true); else GM_PAIR32(false, false); }
+        const size_t smem = batch ? 0 : sizeof(float2) * (size_t)a.ntypes * a.ntypes;
+#define GM_PAIR32(P, Q, B)                                                                                   \
+    pair_kernel_f32<P, Q, B><<<blocks32, kPairWarps * 32, smem, s>>>(                                        \
+        a.n, a.n_slots, a.cap, a.split, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, \
+        a.inv_wsw, a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status, \
+        a.group_sys, a.e_sys)
+#define GM_PAIR32B(P, Q) { if (batch) GM_PAIR32(P, Q, true); else GM_PAIR32(P, Q, false); }
+        if (a.periodic) { if (a.coulomb) GM_PAIR32B(true, true) else GM_PAIR32B(true, false) }
+        else { if (a.coulomb) GM_PAIR32B(false, true) else GM_PAIR32B(false, false) }
+#undef GM_PAIR32B
 #undef GM_PAIR32
     } else {
-        const size_t smem = sizeof(double2) * (size_t)a.ntypes * a.ntypes;
-#define GM_PAIR64(P, Q)                                                                                        \
-    pair_kernel_f64<P, Q><<<blocks, kPairWarps * 32, smem, s>>>(                                               \
-        a.n, a.cap, a.pos64s, a.type_sorted, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab64, a.rc2_64,     \
-        a.rsw_64, a.rc_64, a.box64[0], a.box64[1], a.box64[2], a.force, a.epart, a.status)
-        if (a.periodic) { if (a.coulomb) GM_PAIR64(true, true); else GM_PAIR64(true, false); }
-        else { if (a.coulomb) GM_PAIR64(false, true); else GM_PAIR64(false, false); }
+        const size_t smem = batch ? 0 : sizeof(double2) * (size_t)a.ntypes * a.ntypes;
+#define GM_PAIR64(P, Q, B)                                                                                        \
+    pair_kernel_f64<P, Q, B><<<blocks, kPairWarps * 32, smem, s>>>(                                               \
+        a.n, a.n_slots, a.cap, a.pos64s, a.type_sorted, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab64,     \
+        a.rc2_64, a.rsw_64, a.rc_64, a.box64[0], a.box64[1], a.box64[2], a.force, a.epart, a.status, a.group_sys, \
+        a.e_sys)
+#define GM_PAIR64B(P, Q) { if (batch) GM_PAIR64(P, Q, true); else GM_PAIR64(P, Q, false); }
+        if (a.periodic) { if (a.coulomb) GM_PAIR64B(true, true) else GM_PAIR64B(true, false) }
+        else { if (a.coulomb) GM_PAIR64B(false, true) else GM_PAIR64B(false, false) }
+#undef GM_PAIR64B
 #undef GM_PAIR64
     }
 }

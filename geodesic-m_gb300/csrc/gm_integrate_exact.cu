@@ -67,8 +67,9 @@ __global__ void resync_kernel(int n, const double *pos, double *vel, const doubl
 }
 
 __global__ void check_kernel(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
-                             unsigned long long cond) {
-    // neighbor.rs:60-72 plus the run loop's finite-position guard (lib.rs:94-107)
+                             unsigned long long cond, const int *atom_sys, unsigned int *sys_flag) {
+    // neighbor.rs:60-72 plus the run loop's finite-position guard (lib.rs:94-107);
+    // the atom's system is marked for the rebuild
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int need = 0, bad = 0;
     if (i < n) {
@@ -76,6 +77,7 @@ __global__ void check_kernel(int n, const double *pos, const double *ref, double
         bad = !(isfinite(x) && isfinite(y) && isfinite(z));
         const double dx = x - ref[i], dy = y - ref[n + i], dz = z - ref[2 * n + i];
         need = dx * dx + dy * dy + dz * dz > thr_sq;
+        if (need) sys_flag[atom_sys[i]] = 1u;
     }
     need = __syncthreads_or(need);
     bad = __syncthreads_or(bad);
@@ -351,8 +353,8 @@ void gm_launch_resync(int n, const double *pos, double *vel, const double *dref,
 void gm_launch_step(DevStatus *st, cudaStream_t s) { step_kernel<<<1, 1, 0, s>>>(st); }
 
 void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
-                     unsigned long long cond, int blocks, cudaStream_t s) {
-    check_kernel<<<blocks, 256, 0, s>>>(n, pos, ref, thr_sq, st, cond);
+                     unsigned long long cond, int blocks, const int *atom_sys, unsigned int *sys_flag, cudaStream_t s) {
+    check_kernel<<<blocks, 256, 0, s>>>(n, pos, ref, thr_sq, st, cond, atom_sys, sys_flag);
 }
 
 void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dref, cudaStream_t s) {

@@ -91,38 +91,64 @@ __device__ __forceinline__ void gm_atomic_fix_add(long long *p, long long v) {
     atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
 }
 
+// Per-system energies of a batch: int64 fixed point at 2^-32 kcal/mol, so the
+// sum is independent of the order contributions arrive in.
+constexpr double GM_EFIX_SCALE = 4294967296.0;
+
+// Adds each lane's energy e to its system sy (sy < 0: nothing); one atomic
+// per warp when the warp's lanes share a system.  All 32 lanes must call.
+__device__ __forceinline__ void gm_add_sys_energy(long long *e_sys, int sy, double e) {
+    const long long q = sy >= 0 ? __double2ll_rn(e * GM_EFIX_SCALE) : 0ll;
+    const int s0 = __shfl_sync(0xffffffffu, sy, 0);
+    if (__all_sync(0xffffffffu, sy == s0 || sy < 0) && s0 >= 0) {
+        long long t = q;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((threadIdx.x & 31) == 0) gm_atomic_fix_add(e_sys + s0, t);
+    } else if (sy >= 0 && q != 0) {
+        gm_atomic_fix_add(e_sys + sy, q);
+    }
+}
+
 // ------------------------------------------------------- launcher exports
 
 struct ListArgs {
-    int n;
+    int n;                   // atoms, all systems
+    int n_slots;             // sorted slots: each system's atoms padded to a multiple of 32
+    int n_sys;               // systems in the context
     int cap;                 // list entries per atom
-    const double *pos;       // FP64 x|y|z, caller order
-    float4 *hi, *lo;         // sorted
-    double4 *pos64s;         // sorted FP64 copy (FP64 mode) or nullptr
-    int *type_sorted;        // sorted types (FP64 mode)
-    int *perm;               // sorted -> caller
-    int *cell_of;            // caller order
-    int *cell_sorted;        // sorted
-    int *cell_count, *cell_start, *cell_cursor;
-    int *tmp_slot;           // caller -> unsorted slot
-    int *tmp_atom;           // unsorted slot -> caller
-    int max_cells;
+    const double *pos;       // FP64 x|y|z rows of n atoms, caller order
+    float4 *hi, *lo;         // per slot
+    double4 *pos64s;         // per slot FP64 copy (FP64 mode) or nullptr
+    int *type_sorted;        // per slot types (FP64 mode)
+    int *perm;               // slot -> atom (global index), -1 on padding slots
+    int *cell_of;            // atom -> cell of its system
+    int *cell_sorted;        // slot -> cell of its system
+    int *cell_count, *cell_start, *cell_cursor;  // system s at sys_cell_off[s] (cell_start: ncell + 1 entries)
+    int *tmp_atom;           // slot -> atom of the system, before the in-cell rank
     const int *type;         // caller order
     const float *charge;     // caller order
     const double *charge64;  // caller order (FP64 mode)
     const int *excl_start, *excl;   // caller-order CSR (both directions, sorted)
     int *list, *count, *gmax;
-    double *ref;             // FP64 x|y|z copy at the build
+    double *ref;             // FP64 x|y|z copy at each system's build
     long long *force;        // zeroed with the pack
-    GridInfo *grid;
+    GridInfo *grid;          // one per system
     DevStatus *status;
     double r_list, box[3];
     int periodic;
-    double *bbox_scratch;    // 9 * blocks (min, max, sum per dimension)
-    int *scan_scratch;       // one total per 1024 cells
-    int bbox_blocks;
+    double *bbox_scratch;    // [n_sys][bbox_blocks][9] (min, max, sum per dimension)
+    int *scan_scratch;       // [n_sys][scan_blocks]: one total per 1024 cells
+    int bbox_blocks, scan_blocks, max_sys_atoms;
+    // systems: atoms [sys_atom_off[s], +1), slots [sys_slot_off[s], +1) (32-aligned),
+    // cells [sys_cell_off[s], +1) (the system's cell budget + 1)
+    const int *sys_atom_off, *sys_slot_off, *sys_cell_off;
+    const int *atom_sys;     // atom -> system
+    const int *group_sys;    // 32-slot group -> system
+    unsigned int *sys_flag;  // 1: rebuild the system's list at the next rebuild
 };
 
+// set (every system) or clear the rebuild flags; clearing also clears status->rebuild
+void gm_launch_flags(const ListArgs &a, bool set, cudaStream_t s);
 void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s);
 void gm_launch_grid(const ListArgs &a, cudaStream_t s);
 void gm_launch_bin(const ListArgs &a, cudaStream_t s);
@@ -131,6 +157,9 @@ void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s);
 
 struct ForceArgs {
     int n, n_groups, cap;
+    int n_slots;             // n_groups * 32 (each system padded to whole groups)
+    const int *group_sys, *atom_sys;
+    long long *e_sys;        // per-system potential energy, fixed point 2^-32 kcal/mol (batches), or nullptr
     int split;               // warps per 32-atom group in the FP32 pair kernel
     const float4 *hi, *lo;
     const double4 *pos64s;
@@ -202,7 +231,8 @@ void gm_launch_drift(int n, double *pos, double *vel, double *dref, double dt, b
 void gm_launch_resync(int n, const double *pos, double *vel, const double *dref, double dt, const DevStatus *st,
                       cudaStream_t s);
 void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
-                     unsigned long long cond_handle, int blocks, cudaStream_t s);
+                     unsigned long long cond_handle, int blocks, const int *atom_sys, unsigned int *sys_flag,
+                     cudaStream_t s);
 void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, double *pos, cudaStream_t s);
 // the same solve in two halves, so the warm start can run in between:
 // prepare (reset T, reference vectors, multiplier sums) and the iterations

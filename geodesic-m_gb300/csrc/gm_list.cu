@@ -1,17 +1,25 @@
-// gm_list.cu — Verlet list build on the device (neighbor.rs:8-55 semantics).
+// gm_list.cu — Verlet list build on the device (neighbor.rs:8-55 semantics),
+// for one system or a batch of independent systems in one context.
 //
 // Pipeline at each rebuild (all on the context's stream, no host sync):
 //   wrap (periodic only) -> bbox partials -> grid setup -> cell assignment +
 //   counting-sort histogram -> scan -> scatter -> in-cell rank by caller
 //   index (deterministic order) -> pack -> list build.
-// The list build gives each warp 32 consecutive cell-sorted atoms; the warp
-// streams every candidate in the union of their 5x5x5 half-cell stencils
-// through shared memory and each lane tests it against its own atom.  The
+// Every kernel runs over all systems at once (blockIdx.y = system) and skips
+// the systems whose rebuild flag is clear, so a batch rebuilds only the
+// systems that need it.  Each system owns a range of atoms, a 32-aligned
+// range of sorted slots (padding slots have perm = -1 and no list), a range
+// of cells and its own grid; perm and the list entries hold global indices.
+// The list build gives each warp 32 consecutive cell-sorted atoms of one
+// system; the warp streams the candidates of each cell row its atoms occupy
+// through shared memory and each lane tests them against its own atom.  The
 // test runs in FP32 on hi+lo coordinates; candidates within `margin` of the
 // list radius are re-decided with the reference's exact FP64 expression
 // (min-image, then dx*dx + dy*dy + dz*dz, no fused multiply-add), so the pair
 // set equals the reference's bit for bit.
+#include <algorithm>
 #include <cfloat>
+#include <climits>
 
 #include "gm_internal.cuh"
 
@@ -29,21 +37,57 @@ __device__ __forceinline__ double exact_wrap(double x, double L) {
     return __dsub_rn(x, __dmul_rn(L, floor(__ddiv_rn(x, L))));
 }
 
-__global__ void wrap_kernel(int n, double *pos, double b0, double b1, double b2) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    pos[i] = exact_wrap(pos[i], b0);
-    pos[n + i] = exact_wrap(pos[n + i], b1);
-    pos[2 * n + i] = exact_wrap(pos[2 * n + i], b2);
+// Atom range of system blockIdx.y, or false when it keeps its list.
+__device__ __forceinline__ bool sys_atoms(const ListArgs &a, int &a0, int &a1) {
+    const int s = blockIdx.y;
+    if (!a.sys_flag[s]) return false;
+    a0 = a.sys_atom_off[s];
+    a1 = a.sys_atom_off[s + 1];
+    return true;
 }
 
-// Per block: min x,y,z, max x,y,z and the sum x,y,z of the positions.
-__global__ void bbox_kernel(int n, const double *pos, double *partial) {
+__global__ void set_flags_kernel(ListArgs a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.n_sys) a.sys_flag[s] = 1u;
+}
+
+__global__ void clear_flags_kernel(ListArgs a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.n_sys) a.sys_flag[s] = 0u;
+    if (s == 0) a.status->rebuild = 0u;
+}
+
+__global__ void wrap_kernel(ListArgs a, double *pos) {
+    int a0, a1;
+    if (!sys_atoms(a, a0, a1)) return;
+    const int n = a.n;
+    for (int i = a0 + blockIdx.x * blockDim.x + threadIdx.x; i < a1; i += gridDim.x * blockDim.x) {
+        pos[i] = exact_wrap(pos[i], a.box[0]);
+        pos[n + i] = exact_wrap(pos[n + i], a.box[1]);
+        pos[2 * n + i] = exact_wrap(pos[2 * n + i], a.box[2]);
+    }
+}
+
+// Partial-sum blocks of a system's bbox: as many as a context holding only
+// that system uses, so a system's grid (and its FP32 copies) come out the
+// same alone or in a batch.
+__device__ __forceinline__ int bbox_blocks_of(int n_atoms, int cap) {
+    const int b = (n_atoms + 255) / 256;
+    return b < 1 ? 1 : (b > cap ? cap : b);
+}
+
+// Per block and system: min x,y,z, max x,y,z and the sum x,y,z.
+__global__ void bbox_kernel(ListArgs a) {
     __shared__ double sm[9][256];
     double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX}, sum[3] = {0, 0, 0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int a0, a1;
+    if (!sys_atoms(a, a0, a1)) return;  // uniform per block
+    const int nb = bbox_blocks_of(a1 - a0, 256);
+    if ((int)blockIdx.x >= nb) return;
+    const int n = a.n;
+    for (int i = a0 + blockIdx.x * blockDim.x + threadIdx.x; i < a1; i += nb * blockDim.x) {
         for (int d = 0; d < 3; d++) {
-            double v = pos[d * n + i];
+            double v = a.pos[d * n + i];
             mn[d] = fmin(mn[d], v);
             mx[d] = fmax(mx[d], v);
             if (v == v) sum[d] += v;
@@ -64,16 +108,20 @@ __global__ void bbox_kernel(int n, const double *pos, double *partial) {
             }
         __syncthreads();
     }
-    if (threadIdx.x < 9) partial[blockIdx.x * 9 + threadIdx.x] = sm[threadIdx.x][0];
+    if (threadIdx.x < 9)
+        a.bbox_scratch[((size_t)blockIdx.y * a.bbox_blocks + blockIdx.x) * 9 + threadIdx.x] = sm[threadIdx.x][0];
 }
 
-__global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevStatus *st, double r_list,
-                            double b0, double b1, double b2, int periodic, int max_cells, int n_atoms) {
-    // reduce the per-block bbox partials with the whole block first
+// One block per system: reduce its bbox partials, then lay out its grid.
+__global__ void grid_kernel(ListArgs a, int blocks) {
+    const int sys = blockIdx.x;
+    if (!a.sys_flag[sys]) return;
     __shared__ double red[9][256];
+    const double *partial = a.bbox_scratch + (size_t)sys * blocks * 9;
+    const int nb = a.periodic ? 0 : bbox_blocks_of(a.sys_atom_off[sys + 1] - a.sys_atom_off[sys], 256);
     for (int v = 0; v < 9; v++) {
         double acc = v < 3 ? DBL_MAX : (v < 6 ? -DBL_MAX : 0.0);
-        for (int b = threadIdx.x; b < blocks; b += blockDim.x) {
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
             const double x = partial[b * 9 + v];
             acc = v < 3 ? fmin(acc, x) : (v < 6 ? fmax(acc, x) : acc + x);
         }
@@ -90,16 +138,19 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
-    const double box[3] = {b0, b1, b2};
-    const double wmin = r_list * 0.5 * (1.0 + 1e-5) + 1e-6;
+    GridInfo *g = a.grid + sys;
+    const int n_atoms = a.sys_atom_off[sys + 1] - a.sys_atom_off[sys];
+    const int max_cells = a.sys_cell_off[sys + 1] - a.sys_cell_off[sys] - 1;
+    const double box[3] = {a.box[0], a.box[1], a.box[2]};
+    const double wmin = a.r_list * 0.5 * (1.0 + 1e-5) + 1e-6;
     int nc[3];
     double w[3], lo[3];
-    g->periodic = periodic;
+    g->periodic = a.periodic;
     for (int d = 0; d < 3; d++) {
         g->box[d] = (float)box[d];
         g->inv_box[d] = (float)(1.0 / box[d]);
     }
-    if (periodic) {
+    if (a.periodic) {
         for (int d = 0; d < 3; d++) {
             nc[d] = (int)floor(box[d] / wmin);
             if (nc[d] < 1) nc[d] = 1;
@@ -120,15 +171,15 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
             if (!(ext == ext) || mx[d] < mn[d]) { ext = 0.0; mn[d] = mx[d] = 0.0; sum[d] = 0.0; }
             // min-image of the reference folds pairs farther apart than box/2;
             // the cell search assumes it never does
-            if (ext + r_list >= 0.5 * box[d]) atomicOr(&st->error, (unsigned)GM_DEV_EXTENT);
+            if (ext + a.r_list >= 0.5 * box[d]) atomicOr(&a.status->error, (unsigned)GM_DEV_EXTENT);
             const double mean = n_atoms > 0 ? sum[d] / n_atoms : 0.0;
             const double half = 0.5 * per_dim * wmin;
-            double a = fmax(mn[d], mean - half), b = fmin(mx[d], mean + half);
-            if (!(b >= a)) { a = mn[d]; b = mx[d]; }
-            const double pad = 1e-3 * (1.0 + (b - a));
-            g->origin[d] = 0.5 * (a + b);
-            lo[d] = (a - g->origin[d]) - pad;
-            nc[d] = (int)floor((b - a + 2.0 * pad) / wmin);
+            double lo_c = fmax(mn[d], mean - half), hi_c = fmin(mx[d], mean + half);
+            if (!(hi_c >= lo_c)) { lo_c = mn[d]; hi_c = mx[d]; }
+            const double pad = 1e-3 * (1.0 + (hi_c - lo_c));
+            g->origin[d] = 0.5 * (lo_c + hi_c);
+            lo[d] = (lo_c - g->origin[d]) - pad;
+            nc[d] = (int)floor((hi_c - lo_c + 2.0 * pad) / wmin);
             if (nc[d] < 1) nc[d] = 1;
         }
     }
@@ -138,16 +189,28 @@ __global__ void grid_kernel(const double *partial, int blocks, GridInfo *g, DevS
         for (int d = 0; d < 3; d++) nc[d] = nc[d] > 1 ? (nc[d] * 3) / 4 : 1;
     }
     for (int d = 0; d < 3; d++) {
-        double span = periodic ? box[d] : -2.0 * lo[d];
+        double span = a.periodic ? box[d] : -2.0 * lo[d];
         w[d] = span / nc[d];
         g->nc[d] = nc[d];
         g->lo[d] = (float)lo[d];
         g->inv_w[d] = (float)(1.0 / w[d]);
-        g->full[d] = periodic && nc[d] < 5;
+        g->full[d] = a.periodic && nc[d] < 5;
     }
     g->ncell = nc[0] * nc[1] * nc[2];  // <= max_cells by construction
-    st->rebuild = 0;
-    st->n_rebuilds += 1;
+    atomicAdd(&a.status->n_rebuilds, 1ull);
+}
+
+// Clears the cells the system's new grid uses (the only ones assign and the
+// scan touch), after the grid is laid out.
+__global__ void clear_cells_kernel(ListArgs a) {
+    const int s = blockIdx.y;
+    if (!a.sys_flag[s]) return;
+    const int c0 = a.sys_cell_off[s];
+    const int c1 = c0 + min(a.grid[s].ncell, a.sys_cell_off[s + 1] - c0 - 1);
+    for (int c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += gridDim.x * blockDim.x) {
+        a.cell_count[c] = 0;
+        a.cell_cursor[c] = 0;
+    }
 }
 
 __device__ __forceinline__ int cell_coord(float h, float lo, float inv_w, int nc) {
@@ -156,28 +219,33 @@ __device__ __forceinline__ int cell_coord(float h, float lo, float inv_w, int nc
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-__global__ void assign_kernel(int n, const double *pos, double *ref, const GridInfo *g, int *cell_of,
-                              int *cell_count, int max_cells, DevStatus *st) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c3[3];
-    for (int d = 0; d < 3; d++) {
-        double x = pos[d * n + i];
-        ref[d * n + i] = x;  // NeighborList::ref_{x,y,z} (neighbor.rs:48-50)
-        c3[d] = cell_coord((float)(x - g->origin[d]), g->lo[d], g->inv_w[d], g->nc[d]);
+__global__ void assign_kernel(ListArgs a) {
+    int a0, a1;
+    if (!sys_atoms(a, a0, a1)) return;
+    const GridInfo *g = a.grid + blockIdx.y;
+    const int coff = a.sys_cell_off[blockIdx.y];
+    const int max_cells = a.sys_cell_off[blockIdx.y + 1] - coff - 1;
+    const int n = a.n;
+    for (int i = a0 + blockIdx.x * blockDim.x + threadIdx.x; i < a1; i += gridDim.x * blockDim.x) {
+        int c3[3];
+        for (int d = 0; d < 3; d++) {
+            double x = a.pos[d * n + i];
+            a.ref[d * n + i] = x;  // NeighborList::ref_{x,y,z} (neighbor.rs:48-50)
+            c3[d] = cell_coord((float)(x - g->origin[d]), g->lo[d], g->inv_w[d], g->nc[d]);
+        }
+        int c = (c3[2] * g->nc[1] + c3[1]) * g->nc[0] + c3[0];
+        if (c < 0 || c >= max_cells) {
+            atomicOr(&a.status->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+            c = 0;
+        }
+        a.cell_of[i] = c;
+        atomicAdd(&a.cell_count[coff + c], 1);
     }
-    int c = (c3[2] * g->nc[1] + c3[1]) * g->nc[0] + c3[0];
-    if (c < 0 || c >= max_cells) {
-        atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
-        c = 0;
-    }
-    cell_of[i] = c;
-    atomicAdd(&cell_count[c], 1);
 }
 
-// Exclusive scan of cell_count[0..ncell) into cell_start[0..ncell], in three
-// launches: per-block scans of 1024 cells with block totals, a scan of the
-// totals in one block, then the block offsets added back.
+// Exclusive scan of each system's cell counts into its cell_start[0..ncell],
+// in three launches: per-block scans of 1024 cells with block totals, a scan
+// of the totals per system, then the block offsets added back.
 __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int x = v;
@@ -203,90 +271,109 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &
     return excl;
 }
 
-__global__ void scan_local_kernel(const GridInfo *g, const int *cell_count, int *cell_start, int *block_sums,
-                                  int max_cells) {
-    __shared__ int warp_sums[32];
-    const int ncell = min(g->ncell, max_cells);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x * blockDim.x >= ncell + 1) return;  // whole block idle (uniform)
-    const int v = i < ncell ? cell_count[i] : 0;
-    int total;
-    const int excl = block_exclusive_scan(v, warp_sums, total);
-    if (i <= ncell) cell_start[i] = excl;
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+__device__ __forceinline__ int sys_ncell(const ListArgs &a, int s) {
+    const int max_cells = a.sys_cell_off[s + 1] - a.sys_cell_off[s] - 1;
+    return min(a.grid[s].ncell, max_cells);
 }
 
-__global__ void scan_blocks_kernel(const GridInfo *g, int *block_sums, int max_cells) {
+__global__ void scan_local_kernel(ListArgs a) {
     __shared__ int warp_sums[32];
-    const int ncell = min(g->ncell, max_cells);
-    const int nblocks = (ncell + 1 + 1023) / 1024;
+    const int s = blockIdx.y;
+    if (!a.sys_flag[s]) return;
+    const int ncell = sys_ncell(a, s), coff = a.sys_cell_off[s];
+    if (blockIdx.x * blockDim.x >= ncell + 1) return;  // whole block idle (uniform)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = i < ncell ? a.cell_count[coff + i] : 0;
+    int total;
+    const int excl = block_exclusive_scan(v, warp_sums, total);
+    if (i <= ncell) a.cell_start[coff + i] = excl;
+    if (threadIdx.x == 0) a.scan_scratch[(size_t)s * a.scan_blocks + blockIdx.x] = total;
+}
+
+__global__ void scan_blocks_kernel(ListArgs a) {
+    __shared__ int warp_sums[32];
+    const int s = blockIdx.x;
+    if (!a.sys_flag[s]) return;
+    int *sums = a.scan_scratch + (size_t)s * a.scan_blocks;
+    const int nblocks = (sys_ncell(a, s) + 1 + 1023) / 1024;
     int carry = 0;
     for (int base = 0; base < nblocks; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        const int v = i < nblocks ? block_sums[i] : 0;
+        const int v = i < nblocks ? sums[i] : 0;
         int total;
         const int excl = block_exclusive_scan(v, warp_sums, total);
-        if (i < nblocks) block_sums[i] = excl + carry;
+        if (i < nblocks) sums[i] = excl + carry;
         carry += total;
     }
 }
 
-__global__ void scan_add_kernel(const GridInfo *g, int *cell_start, const int *block_sums, int max_cells) {
-    const int ncell = min(g->ncell, max_cells);
+__global__ void scan_add_kernel(ListArgs a) {
+    const int s = blockIdx.y;
+    if (!a.sys_flag[s]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= ncell) cell_start[i] += block_sums[blockIdx.x];
+    if (i <= sys_ncell(a, s))
+        a.cell_start[a.sys_cell_off[s] + i] += a.scan_scratch[(size_t)s * a.scan_blocks + blockIdx.x];
 }
 
-__global__ void scatter_kernel(int n, const int *cell_of, const int *cell_start, int *cell_cursor, int *tmp_atom) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c = cell_of[i];
-    int slot = cell_start[c] + atomicAdd(&cell_cursor[c], 1);
-    tmp_atom[slot] = i;
+__global__ void scatter_kernel(ListArgs a) {
+    int a0, a1;
+    if (!sys_atoms(a, a0, a1)) return;
+    const int coff = a.sys_cell_off[blockIdx.y], soff = a.sys_slot_off[blockIdx.y];
+    for (int i = a0 + blockIdx.x * blockDim.x + threadIdx.x; i < a1; i += gridDim.x * blockDim.x) {
+        const int c = a.cell_of[i];
+        const int slot = a.cell_start[coff + c] + atomicAdd(&a.cell_cursor[coff + c], 1);
+        a.tmp_atom[soff + slot] = i - a0;
+    }
 }
 
 // Within a cell, atoms are ordered by caller index: the rank of an atom is
 // the number of cell members with a smaller index.  Independent of the
 // atomic order of the scatter, so the sorted layout is deterministic.
-__global__ void rank_kernel(int n, const int *cell_of, const int *cell_start, const int *tmp_atom, int *perm,
-                            int *cell_sorted, DevStatus *st) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int a = tmp_atom[k];
-    int c = cell_of[a];
-    int s0 = cell_start[c], s1 = cell_start[c + 1];
-    if (s1 - s0 > 65536) {
-        // no physical system packs this many atoms into one half cell; keep
-        // the quadratic rank bounded and report it
-        atomicOr(&st->error, (unsigned)GM_DEV_CELL_OVERFLOW);
-        perm[k] = a;
-        cell_sorted[k] = c;
-        return;
+__global__ void rank_kernel(ListArgs a) {
+    int a0, a1;
+    if (!sys_atoms(a, a0, a1)) return;
+    const int coff = a.sys_cell_off[blockIdx.y], soff = a.sys_slot_off[blockIdx.y];
+    const int ns = a1 - a0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
+        const int at = a.tmp_atom[soff + k];
+        const int c = a.cell_of[a0 + at];
+        const int s0 = a.cell_start[coff + c], s1 = a.cell_start[coff + c + 1];
+        if (s1 - s0 > 65536) {
+            // no physical system packs this many atoms into one half cell; keep
+            // the quadratic rank bounded and report it
+            atomicOr(&a.status->error, (unsigned)GM_DEV_CELL_OVERFLOW);
+            a.perm[soff + k] = a0 + at;
+            a.cell_sorted[soff + k] = c;
+            continue;
+        }
+        int rank = 0;
+        for (int m = s0; m < s1; m++) rank += a.tmp_atom[soff + m] < at;
+        a.perm[soff + s0 + rank] = a0 + at;
+        a.cell_sorted[soff + s0 + rank] = c;
     }
-    int rank = 0;
-    for (int m = s0; m < s1; m++) rank += tmp_atom[m] < a;
-    perm[s0 + rank] = a;
-    cell_sorted[s0 + rank] = c;
 }
 
-__global__ void pack_kernel(int n, const double *pos, const int *perm, const int *type, const float *charge,
-                            const GridInfo *g, float4 *hi, float4 *lo, double4 *pos64s, int *type_sorted,
-                            const double *charge64, long long *force) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    int a = perm[s];
-    double x = pos[a], y = pos[n + a], z = pos[2 * n + a];
-    double dx = x - g->origin[0], dy = y - g->origin[1], dz = z - g->origin[2];
-    float hx = (float)dx, hy = (float)dy, hz = (float)dz;
-    hi[s] = make_float4(hx, hy, hz, __int_as_float(type[a]));
-    lo[s] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), charge[a]);
-    if (pos64s) {
-        pos64s[s] = make_double4(x, y, z, charge64[a]);
-        type_sorted[s] = type[a];
+// Every slot of every system, every force evaluation: the FP32 hi/lo copies
+// relative to the system's grid origin, and the force accumulators cleared.
+__global__ void pack_kernel(ListArgs a, bool fp64) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_slots) return;
+    const int at = a.perm[s];
+    if (at < 0) return;  // padding slot
+    const int n = a.n;
+    const GridInfo *g = a.grid + a.atom_sys[at];
+    const double x = a.pos[at], y = a.pos[n + at], z = a.pos[2 * n + at];
+    const double dx = x - g->origin[0], dy = y - g->origin[1], dz = z - g->origin[2];
+    const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+    a.hi[s] = make_float4(hx, hy, hz, __int_as_float(a.type[at]));
+    a.lo[s] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), a.charge[at]);
+    if (fp64) {
+        a.pos64s[s] = make_double4(x, y, z, a.charge64[at]);
+        a.type_sorted[s] = a.type[at];
     }
-    force[a] = 0;
-    force[n + a] = 0;
-    force[2 * n + a] = 0;
+    a.force[at] = 0;
+    a.force[n + at] = 0;
+    a.force[2 * n + at] = 0;
 }
 
 struct Range { int lo, hi, nc, wrap; };
@@ -311,35 +398,38 @@ __device__ __forceinline__ Range dim_range(int mn, int mx, int nc, int periodic,
 __device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c >= nc ? c - nc : c); }
 
 __global__ void __launch_bounds__(kBuildWarps * 32)
-build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-             const int *__restrict__ perm, const int *__restrict__ cell_sorted, const int *__restrict__ cell_start,
-             const GridInfo *__restrict__ gp, const double *__restrict__ pos, const int *__restrict__ excl_start,
-             const int *__restrict__ excl, int *__restrict__ list, int *__restrict__ count, int *__restrict__ gmax,
-             DevStatus *st, float rl2_lo, float rl2_hi, double rl2_64, double b0, double b1, double b2) {
+build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     __shared__ float4 s_hi[kBuildWarps][32];
     __shared__ float4 s_lo[kBuildWarps][32];
     __shared__ int s_orig[kBuildWarps][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int group = blockIdx.x * kBuildWarps + wib;
+    if (group * 32 >= a.n_slots) return;
+    const int sys = a.group_sys[group];
+    if (!a.sys_flag[sys]) return;  // warp-uniform: the system keeps its list
+    const int soff = a.sys_slot_off[sys], coff = a.sys_cell_off[sys];
+    const int ns = a.sys_atom_off[sys + 1] - a.sys_atom_off[sys];
     const int s = group * 32 + lane;
-    if (group * 32 >= n) return;
-    const bool valid = s < n;
-    const GridInfo g = *gp;
+    const bool valid = s - soff < ns;
+    const GridInfo g = a.grid[sys];
+    const int n = a.n;
+    const int cap = a.cap;
+    const int *__restrict__ cell_start = a.cell_start + coff;
     float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
     int my_orig = -1, my_cell = 0;
     if (valid) {
-        mh = hi[s];
-        ml = lo[s];
-        my_orig = perm[s];
-        my_cell = cell_sorted[s];
+        mh = a.hi[s];
+        ml = a.lo[s];
+        my_orig = a.perm[s];
+        my_cell = a.cell_sorted[s];
     }
     // own exclusions (caller indices, ascending); up to 8 kept in registers
     int e0 = 0, e1 = 0;
     int ex[8];
-    if (valid) { e0 = excl_start[my_orig]; e1 = excl_start[my_orig + 1]; }
+    if (valid) { e0 = a.excl_start[my_orig]; e1 = a.excl_start[my_orig + 1]; }
     const int ne = e1 - e0;
 #pragma unroll
-    for (int k = 0; k < 8; k++) ex[k] = (k < ne) ? excl[e0 + k] : -1;
+    for (int k = 0; k < 8; k++) ex[k] = (k < ne) ? a.excl[e0 + k] : -1;
     // Candidate regions, one per distinct cell row (cy, cz) among the lanes:
     // a group of 32 sorted atoms usually lies in one row of cells, sometimes
     // straddles the end of a row.  Sweeping each row's own 5 x 5 x (span + 4)
@@ -348,9 +438,9 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
     // it never meets a candidate twice.
     const int cx = my_cell % g.nc[0], cy = (my_cell / g.nc[0]) % g.nc[1], cz = my_cell / (g.nc[0] * g.nc[1]);
     const int row_id = valid ? cz * g.nc[1] + cy : -1;
-    int *my_list = list + (size_t)group * 32 * cap + lane;
+    int *my_list = a.list + (size_t)group * 32 * cap + lane;
     int cnt = 0;
-    const double bx[3] = {b0, b1, b2};
+    const double bx[3] = {a.box[0], a.box[1], a.box[2]};
     unsigned remaining = __ballot_sync(0xffffffffu, valid);
     while (remaining) {
         const int leader = __ffs(remaining) - 1;
@@ -375,18 +465,19 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
                 else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
                 for (int sg = 0; sg < nseg; sg++) {
                     const int row = (z * g.nc[1] + y) * g.nc[0];
-                    const int a0 = cell_start[row + seg_lo[sg]], a1 = cell_start[row + seg_hi[sg] + 1];
-                    for (int base = a0; base < a1; base += 32) {
+                    // the system's slots, made global
+                    const int b0 = soff + cell_start[row + seg_lo[sg]], b1 = soff + cell_start[row + seg_hi[sg] + 1];
+                    for (int base = b0; base < b1; base += 32) {
                         const int t = base + lane;
                         __syncwarp();
-                        if (t < a1) {
-                            s_hi[wib][lane] = hi[t];
-                            s_lo[wib][lane] = lo[t];
-                            s_orig[wib][lane] = perm[t];
+                        if (t < b1) {
+                            s_hi[wib][lane] = a.hi[t];
+                            s_lo[wib][lane] = a.lo[t];
+                            s_orig[wib][lane] = a.perm[t];
                         }
                         __syncwarp();
                         if (!mine) continue;
-                        const int m = min(32, a1 - base);
+                        const int m = min(32, b1 - base);
                         for (int k = 0; k < m; k++) {
                             const int j = base + k;
                             if (j == s) continue;
@@ -405,9 +496,9 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
                             bool in = r2 <= rl2_lo;
                             if (!in) {
                                 // the reference's own FP64 decision
-                                double ex_ = exact_min_image(__dsub_rn(pos[jo], pos[my_orig]), bx[0]);
-                                double ey_ = exact_min_image(__dsub_rn(pos[n + jo], pos[n + my_orig]), bx[1]);
-                                double ez_ = exact_min_image(__dsub_rn(pos[2 * n + jo], pos[2 * n + my_orig]), bx[2]);
+                                double ex_ = exact_min_image(__dsub_rn(a.pos[jo], a.pos[my_orig]), bx[0]);
+                                double ey_ = exact_min_image(__dsub_rn(a.pos[n + jo], a.pos[n + my_orig]), bx[1]);
+                                double ez_ = exact_min_image(__dsub_rn(a.pos[2 * n + jo], a.pos[2 * n + my_orig]), bx[2]);
                                 double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
                                 in = rr <= rl2_64;
                             }
@@ -416,7 +507,7 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
 #pragma unroll
                             for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
                             if (ne > 8)
-                                for (int q = e0 + 8; q < e1; q++) excluded |= (excl[q] == jo);
+                                for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
                             if (excluded) continue;
                             if (cnt < cap) my_list[(size_t)cnt * 32] = j;
                             cnt++;
@@ -427,55 +518,60 @@ build_kernel(int n, int cap, const float4 *__restrict__ hi, const float4 *__rest
         }
     }
     if (valid) {
-        count[s] = cnt < cap ? cnt : cap;
-        if (cnt > cap) atomicOr(&st->error, (unsigned)GM_DEV_LIST_OVERFLOW);
+        a.count[s] = cnt < cap ? cnt : cap;
+        if (cnt > cap) atomicOr(&a.status->error, (unsigned)GM_DEV_LIST_OVERFLOW);
     }
     int c = valid ? (cnt < cap ? cnt : cap) : 0;
     for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
-    if (lane == 0) gmax[group] = c;
+    if (lane == 0) a.gmax[group] = c;
+}
+
+// Per-system launch shape: x covers the largest system, y the systems.
+dim3 sys_grid(const ListArgs &a, int per_block, int cap_blocks) {
+    int bx = (a.max_sys_atoms + per_block - 1) / per_block;
+    bx = bx < 1 ? 1 : (bx > cap_blocks ? cap_blocks : bx);
+    return dim3((unsigned)bx, (unsigned)a.n_sys, 1);
 }
 
 }  // namespace
 
+void gm_launch_flags(const ListArgs &a, bool set, cudaStream_t s) {
+    if (set) set_flags_kernel<<<(a.n_sys + 255) / 256, 256, 0, s>>>(a);
+    else clear_flags_kernel<<<(a.n_sys + 255) / 256, 256, 0, s>>>(a);
+}
+
 void gm_launch_wrap(const ListArgs &a, double *pos, cudaStream_t s) {
     if (!a.periodic || a.n == 0) return;
-    wrap_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.n, pos, a.box[0], a.box[1], a.box[2]);
+    wrap_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a, pos);
 }
 
 void gm_launch_grid(const ListArgs &a, cudaStream_t s) {
-    if (!a.periodic && a.n > 0) bbox_kernel<<<a.bbox_blocks, 256, 0, s>>>(a.n, a.pos, a.bbox_scratch);
-    grid_kernel<<<1, 256, 0, s>>>(a.bbox_scratch, a.periodic || a.n == 0 ? 0 : a.bbox_blocks, a.grid, a.status,
-                                 a.r_list, a.box[0], a.box[1], a.box[2], a.periodic, a.max_cells, a.n);
+    if (!a.periodic && a.n > 0) bbox_kernel<<<dim3((unsigned)a.bbox_blocks, (unsigned)a.n_sys), 256, 0, s>>>(a);
+    grid_kernel<<<a.n_sys, 256, 0, s>>>(a, a.bbox_blocks);
 }
 
 void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
-    cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)a.max_cells, s);
-    cudaMemsetAsync(a.cell_cursor, 0, sizeof(int) * (size_t)a.max_cells, s);
-    const int nb = (a.n + 255) / 256;
-    if (a.n > 0)
-        assign_kernel<<<nb, 256, 0, s>>>(a.n, a.pos, a.ref, a.grid, a.cell_of, a.cell_count, a.max_cells, a.status);
-    const int scan_blocks = (a.max_cells + 1 + 1023) / 1024;
-    scan_local_kernel<<<scan_blocks, 1024, 0, s>>>(a.grid, a.cell_count, a.cell_start, a.scan_scratch, a.max_cells);
-    scan_blocks_kernel<<<1, 1024, 0, s>>>(a.grid, a.scan_scratch, a.max_cells);
-    scan_add_kernel<<<scan_blocks, 1024, 0, s>>>(a.grid, a.cell_start, a.scan_scratch, a.max_cells);
+    clear_cells_kernel<<<dim3((unsigned)std::min(a.scan_blocks * 4, 4096), (unsigned)a.n_sys), 256, 0, s>>>(a);
+    if (a.n > 0) assign_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);
+    scan_local_kernel<<<dim3((unsigned)a.scan_blocks, (unsigned)a.n_sys), 1024, 0, s>>>(a);
+    scan_blocks_kernel<<<a.n_sys, 1024, 0, s>>>(a);
+    scan_add_kernel<<<dim3((unsigned)a.scan_blocks, (unsigned)a.n_sys), 1024, 0, s>>>(a);
     if (a.n > 0) {
-        scatter_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.cell_cursor, a.tmp_atom);
-        rank_kernel<<<nb, 256, 0, s>>>(a.n, a.cell_of, a.cell_start, a.tmp_atom, a.perm, a.cell_sorted, a.status);
+        scatter_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);
+        rank_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);
     }
 }
 
 void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s) {
-    if (a.n == 0) return;
-    pack_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.n, a.pos, a.perm, a.type, a.charge, a.grid, a.hi, a.lo,
-                                                   fp64 ? a.pos64s : nullptr, a.type_sorted, a.charge64, a.force);
+    if (a.n_slots == 0) return;
+    pack_kernel<<<(a.n_slots + 255) / 256, 256, 0, s>>>(a, fp64);
 }
 
 void gm_launch_build(const ListArgs &a, cudaStream_t s) {
-    if (a.n == 0) return;
-    const int groups = (a.n + 31) / 32;
+    if (a.n_slots == 0) return;
+    const int groups = a.n_slots / 32;
     const double rl2 = a.r_list * a.r_list;  // neighbor.rs:25
     const double margin = 1e-3 * (rl2 > 144.0 ? rl2 / 144.0 : 1.0);
     build_kernel<<<(groups + kBuildWarps - 1) / kBuildWarps, kBuildWarps * 32, 0, s>>>(
-        a.n, a.cap, a.hi, a.lo, a.perm, a.cell_sorted, a.cell_start, a.grid, a.pos, a.excl_start, a.excl, a.list,
-        a.count, a.gmax, a.status, (float)(rl2 - margin), (float)(rl2 + margin), rl2, a.box[0], a.box[1], a.box[2]);
+        a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
 }

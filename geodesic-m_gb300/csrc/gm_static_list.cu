@@ -42,6 +42,9 @@ struct Scratch {
     int scan[kScanBlocks];
     int cell_of[kMaxAtoms], tmp_atom[kMaxAtoms], perm[kMaxAtoms], cell_sorted[kMaxAtoms];
     int row_count[kMaxAtoms], row_start[kMaxAtoms + 1];
+    // the one system's tables (atoms, slots, cells) and rebuild flag
+    int sys_atom_off[2], sys_slot_off[2], sys_cell_off[2];
+    unsigned int sys_flag[1];
 };
 static_assert(sizeof(Scratch) <= GM_STATIC_SCRATCH_BYTES, "scratch layout exceeds GM_STATIC_SCRATCH_BYTES");
 
@@ -241,8 +244,21 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int n = n_atoms;
 
+    // the one system: atoms [0, n), slots [0, n) (no list is built, so no
+    // padding is needed), the whole cell budget
+    const int tables[6] = {0, n, 0, n, 0, kMaxCells + 1};
+    if (cudaMemcpyAsync(S->sys_atom_off, tables, sizeof(tables), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return GM_ERR_DEVICE;
     ListArgs a{};
     a.n = n;
+    a.n_slots = n;
+    a.n_sys = 1;
+    a.sys_atom_off = S->sys_atom_off;
+    a.sys_slot_off = S->sys_slot_off;
+    a.sys_cell_off = S->sys_cell_off;
+    a.sys_flag = S->sys_flag;
+    a.max_sys_atoms = n;
+    a.scan_blocks = (kMaxCells + 1 + 1023) / 1024;
     a.pos = d_pos;
     a.ref = S->ref;
     a.perm = S->perm;
@@ -252,7 +268,6 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     a.cell_start = S->cell_start;
     a.cell_cursor = S->cell_cursor;
     a.tmp_atom = S->tmp_atom;
-    a.max_cells = kMaxCells;
     a.grid = &S->grid;
     a.status = &S->status;
     a.r_list = params->r_skin;
@@ -263,6 +278,7 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     a.bbox_blocks = (n + 255) / 256 < kBboxBlocks ? (n + 255) / 256 : kBboxBlocks;
 
     if (cudaMemsetAsync(&S->status, 0, sizeof(DevStatus), s) != cudaSuccess) return GM_ERR_DEVICE;
+    gm_launch_flags(a, true, s);
     gm_launch_wrap(a, d_pos, s);  // neighbor.rs:10-16
     gm_launch_grid(a, s);
     gm_launch_bin(a, s);

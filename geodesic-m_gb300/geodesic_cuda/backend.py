@@ -151,6 +151,10 @@ def lib():
         L.gm_build_pairs_static.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, P(GmParams), C.c_void_p,
                                             C.c_void_p, C.c_int64, P(C.c_int64), C.c_void_p]
         _f32p = P(C.c_float)
+        L.gm_create_ensemble.restype = C.c_void_p
+        L.gm_create_ensemble.argtypes = [C.c_int32, P(GmAtoms), P(GmTopology), P(GmParams), P(C.c_int32)]
+        L.gm_ensemble_info.argtypes = [C.c_void_p, P(C.c_int64)]
+        L.gm_ensemble_energies.argtypes = [C.c_void_p, _f64p, _f64p]
         L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
         L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
         L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
@@ -159,7 +163,7 @@ def lib():
         L.gm_ws_forward.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p]
         L.gm_ws_gradient.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int64, _f32p, P(C.c_double)]
         L.gm_ws_last.argtypes = [C.c_void_p, _f32p, _f64p, _f64p]
-        for f in ("gm_ws_record", "gm_ws_samples", "gm_ws_train", "gm_ws_enable", "gm_ws_params", "gm_ws_forward",
+        for f in ("gm_ensemble_info", "gm_ensemble_energies", "gm_ws_record", "gm_ws_samples", "gm_ws_train", "gm_ws_enable", "gm_ws_params", "gm_ws_forward",
                   "gm_ws_gradient", "gm_ws_last", "gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
@@ -200,10 +204,23 @@ class CudaBackend:
     """`ComputeBackend` for `backend = "cuda"` (geodesic-core/src/backend.rs:11-23)."""
 
     def __init__(self, atoms, topology, params: SimParams):
+        self._create([atoms], [topology], params)
+
+    @classmethod
+    def ensemble(cls, atoms_list, topo_list, params: SimParams):
+        """A batch of independent systems in one context (gm_create_ensemble):
+        per-atom arrays are the systems' arrays concatenated in order."""
+        self = cls.__new__(cls)
+        self._create(list(atoms_list), list(topo_list), params)
+        return self
+
+    def _create(self, atoms_list, topo_list, params):
         L = lib()
-        self._atoms, self._topo, self.params = atoms, topology, params
-        self.n = int(len(atoms.mass))
+        assert len(atoms_list) == len(topo_list) and atoms_list
+        self._atoms, self._topo, self.params = atoms_list[0], topo_list[0], params
+        self.n_sys = len(atoms_list)
         keep = []
+        self._keep = keep
 
         def f(a):
             a = np.ascontiguousarray(a, dtype=np.float64)
@@ -215,27 +232,45 @@ class CudaBackend:
             keep.append(a)
             return _p(a, C.c_uint32)
 
-        el = getattr(atoms, "element", None)
-        elp = None
-        if el is not None:
-            el = np.ascontiguousarray(el, dtype=np.uint8)
-            keep.append(el)
-            elp = _p(el, C.c_uint8)
-        ca = GmAtoms(self.n, f(atoms.sigma), f(atoms.epsilon), f(atoms.mass),
-                     f(getattr(atoms, "charge", np.zeros(self.n))), elp)
-        t = topology
-        ct = GmTopology(len(t.bond_i), u(t.bond_i), u(t.bond_j), f(t.bond_k), f(t.bond_r0),
-                        len(t.angle_i), u(t.angle_i), u(t.angle_j), u(t.angle_k), f(t.angle_kth), f(t.angle_th0),
-                        len(t.dihed_i), u(t.dihed_i), u(t.dihed_j), u(t.dihed_k), u(t.dihed_l), f(t.dihed_kphi),
-                        u(t.dihed_n), f(t.dihed_delta), len(t.constr_i), u(t.constr_i), u(t.constr_j),
-                        f(t.constr_dsq), len(t.excl_i), u(t.excl_i), u(t.excl_j))
+        ca = (GmAtoms * self.n_sys)()
+        ct = (GmTopology * self.n_sys)()
+        sizes = []
+        for k, (atoms, t) in enumerate(zip(atoms_list, topo_list)):
+            n = int(len(atoms.mass))
+            sizes.append(n)
+            el = getattr(atoms, "element", None)
+            elp = None
+            if el is not None:
+                el = np.ascontiguousarray(el, dtype=np.uint8)
+                keep.append(el)
+                elp = _p(el, C.c_uint8)
+            ca[k] = GmAtoms(n, f(atoms.sigma), f(atoms.epsilon), f(atoms.mass),
+                            f(getattr(atoms, "charge", np.zeros(n))), elp)
+            ct[k] = GmTopology(len(t.bond_i), u(t.bond_i), u(t.bond_j), f(t.bond_k), f(t.bond_r0),
+                               len(t.angle_i), u(t.angle_i), u(t.angle_j), u(t.angle_k), f(t.angle_kth),
+                               f(t.angle_th0), len(t.dihed_i), u(t.dihed_i), u(t.dihed_j), u(t.dihed_k),
+                               u(t.dihed_l), f(t.dihed_kphi), u(t.dihed_n), f(t.dihed_delta), len(t.constr_i),
+                               u(t.constr_i), u(t.constr_j), f(t.constr_dsq), len(t.excl_i), u(t.excl_i),
+                               u(t.excl_j))
+        self.n = int(sum(sizes))
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
         st = C.c_int32()
         cp = params.to_c()
-        self._h = L.gm_create(C.byref(ca), C.byref(ct), C.byref(cp), C.byref(st))
+        if self.n_sys == 1:
+            self._h = L.gm_create(C.byref(ca[0]), C.byref(ct[0]), C.byref(cp), C.byref(st))
+        else:
+            self._h = L.gm_create_ensemble(self.n_sys, ca, ct, C.byref(cp), C.byref(st))
         if not self._h:
             raise BackendError(st.value, "gm_create failed")
         self._forces = np.zeros((3, self.n))
         self._energy = 0.0
+
+    def ensemble_energies(self):
+        """Per-system (potential, kinetic) energies (gm_ensemble_energies)."""
+        ep = np.zeros(self.n_sys)
+        ek = np.zeros(self.n_sys)
+        self._check(lib().gm_ensemble_energies(self._h, _p(ep), _p(ek)))
+        return ep, ek
 
     def close(self):
         if getattr(self, "_h", None):

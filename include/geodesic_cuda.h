@@ -184,6 +184,28 @@ void *gm_stream(gm_ctx *ctx);
  * of their SHAKE / RATTLE iteration counts, [11] warm-start solves recorded. */
 int32_t gm_counters(const gm_ctx *ctx, int64_t *out, int64_t n);
 
+/* ---- batches of independent systems (no reference counterpart) --------
+ *
+ * One context holding n_systems independent systems (the reference runs one
+ * ComputeBackend per system): atoms[s], topos[s] describe system s with its
+ * own atom indices; they share params.  The systems are concatenated in
+ * order (system s's atoms at offsets [off[s], off[s+1]) of every per-atom
+ * array the entry points above take), never interact, and advance together:
+ * one graph launch per step covers all of them, with one kernel launch per
+ * kernel for the whole batch, and each system's list is rebuilt only when
+ * one of its own atoms moved more than half the skin.  Each system has its
+ * own cell grid and Lennard-Jones type table (up to 64 types per system).
+ * The SHAKE/RATTLE stop rule runs over the whole batch (every cluster
+ * iterates to the batch's largest count, each converged to the tolerance). */
+gm_ctx *gm_create_ensemble(int32_t n_systems, const gm_atoms *atoms, const gm_topology *topos,
+                           const gm_params *params, int32_t *status);
+/* off[0..n_systems]: the first atom of each system, then the atom count. */
+int32_t gm_ensemble_info(const gm_ctx *ctx, int64_t *atom_offsets);
+/* Per-system potential energy at the last force evaluation (int64 fixed-point
+ * sums, so a system's value does not depend on the batch around it) and
+ * kinetic energy of the resident velocities (lib.rs:68-77); NULL skips. */
+int32_t gm_ensemble_energies(gm_ctx *ctx, double *e_pot, double *e_kin);
+
 /* ---- constraint warm start (no reference counterpart) ------------------
  *
  * A 12-64-64-1 SiLU network (BF16 matmul weights and activations, FP32
