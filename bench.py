@@ -147,6 +147,7 @@ def run_cuda(args, rank, world):
     be = backend.CudaBackend(atoms, topo, p)
     be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
     be.forces_resident()
+    tuned = be.autotune(reps=3)  # pair kernel split / block size / grid, same bits for every choice
     be.run_resident(DT_PS, args.warmup)
     be.synchronize()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -177,7 +178,7 @@ def run_cuda(args, rank, world):
                 "ms_per_step": round(1e3 * sec / args.steps, 5), "quick": True, "half_list_pairs": pairs,
                 "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"]),
                 "kernel_ms": {"pair": round(be.profile("pair", 3), 5), "rebuild": round(be.profile("rebuild", 2), 5)},
-                "split": be.counters().get("split")}
+                "autotuner": tuned}
     # steady state: back-to-back steps, no flush (L2 keeps part of the list)
     t_bb = be.time_steps(DT_PS, min(args.steps, 2000), first_step=args.warmup + args.steps) / 1e3
     # roofline of the pair kernel: SURVEY algorithmic bytes 4 P + 52 N per launch
@@ -268,6 +269,7 @@ def run_cuda(args, rank, world):
         "e2e": {"value": round(ns_per_day(n_e2e, t_e2e), 3), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
         "gpu_launches": int(result["launches"]),
+        "autotuner": tuned,
         "clocks": result["clocks"],
         "cpu_baseline": cpu,
     }
@@ -361,6 +363,211 @@ def run_reference(args):
             "e2e": {"value": round(val, 4), "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------- other configs
+# Each prints its own JSON line (python bench.py --config NAME); the default
+# line above is the headline workload.
+
+def _gen_one(args_):
+    """Worker of the generator pool (spawned before any GPU work): one
+    system with a single generator thread."""
+    n, seed, relax, h = args_
+    sys.path[:0] = [os.path.join(ROOT, "geodesic-m_gb300")]
+    from geodesic_cuda import synth
+    return synth.generate(n, seed=seed, temperature=300.0, relax_iters=relax, h_fraction=h, n_threads=1)[:3]
+
+
+def _clock_ok(clk):
+    return {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons") if k in clk}
+
+
+def run_ensemble(args):
+    """configs[3]: 256 independent systems, N log-uniform in [500, 20000],
+    per-system seeds, MB 300 K, mixed precision: one context, one graph
+    launch per step for the whole batch, pair kernel shape from the
+    autotuner; against the same systems run one by one (each in its own
+    context and graph)."""
+    import multiprocessing as mp
+    rng = np.random.default_rng(SEED)
+    n_sys = args.systems
+    sizes = np.exp(rng.uniform(np.log(500), np.log(20000), n_sys)).astype(int)
+    jobs = [(int(n), SEED + 1000 + k, 200, 0.0) for k, n in enumerate(sizes)]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(os.cpu_count() or 1, 32)) as pool:
+        syss = pool.map(_gen_one, jobs, chunksize=1)
+    t_gen = time.perf_counter() - t0
+    import torch
+    from geodesic_cuda import backend
+    torch.cuda.set_device(0)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **PHYS)
+    pos = np.ascontiguousarray(np.concatenate([s[2].pos for s in syss], axis=1))
+    vel = np.ascontiguousarray(np.concatenate([s[2].vel for s in syss], axis=1))
+    be = backend.CudaBackend.ensemble([s[0] for s in syss], [s[1] for s in syss], p)
+    be.upload_state(pos, vel)
+    be.forces_resident()
+    choice = be.autotune(reps=3)
+    be.run_resident(DT_PS, args.warmup)
+    be.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
+    c0 = be.counters()
+    with ClockSampler(0) as clk:
+        dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                               flush_bytes=L2_FLUSH_BYTES)
+    c1 = be.counters()
+    sec = dev_ms / 1e3
+    batched = n_sys * ns_per_day(args.steps, sec)
+    be.close()
+    # one by one: each system alone, its own context and graph
+    k1 = max(20, min(args.steps, args.single_steps))
+    t_single = 0.0
+    for atoms, topo, state in syss:
+        b1 = backend.CudaBackend(atoms, topo, p)
+        b1.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
+        b1.forces_resident()
+        b1.run_resident(DT_PS, args.warmup)
+        b1.synchronize()
+        t_single += b1.time_steps(DT_PS, k1, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                                  flush_bytes=L2_FLUSH_BYTES) / 1e3 / k1
+        b1.close()
+    one_by_one = n_sys * ns_per_day(1, t_single)
+    return {"metric": "aggregate ns/day of a 256-system batch, batched vs one by one", "value": round(batched, 2),
+            "unit": "ns/day", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * sec / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 pair math, int64 fixed-point forces, fp64 state/energy",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": f"{n_sys} independent lattice-chain systems, N log-uniform in [500, 20000] "
+                                   f"(total {int(sizes.sum())} atoms), per-system seeds, MB 300 K, 2 fs, "
+                                   "FIRE 200 iterations", "n_systems": n_sys, "total_atoms": int(sizes.sum()),
+                       "l2": "flushed between timed steps"},
+            "one_by_one_ns_per_day": round(one_by_one, 2), "batched_over_one_by_one": round(batched / one_by_one, 2),
+            "one_by_one_sample": f"{k1} timed steps per system after {args.warmup} warm-up steps, summed",
+            "autotuner": choice, "list_rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
+            "gpu_launches": int(c1["launches"] - c0["launches"]), "generation_s": round(t_gen, 1),
+            "clocks": _clock_ok(clk.summary())}
+
+
+def run_warm_start(args):
+    """configs[4]: 50,000 atoms with 40 % hydrogens (H bonds constrained at
+    1.09 A), FP64 SHAKE/RATTLE to 1e-10: the network is trained on solver
+    multipliers of a different seed (2,000 recorded steps), then the same
+    run is timed cold and warm-started.  At 2 fs: with H at 1.008 amu and only
+    the H bonds constrained this lattice fails within 20 steps at 4 fs and
+    within ~1,000 at 3 fs (the oracle fails the same way)."""
+    import torch
+    from geodesic_cuda import amber, backend, synth
+    torch.cuda.set_device(0)
+    dt = 0.002
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, max_constr_iter=200, constr_tol=1e-10, **{
+        k: v for k, v in PHYS.items() if k not in ("max_constr_iter", "constr_tol")})
+
+    def system(seed):
+        atoms, topo, state, _ = synth.generate(N_ATOMS, seed=seed, h_fraction=0.4, temperature=300.0,
+                                               relax_iters=1000)
+        return atoms, amber.promote_hydrogen_bonds(topo, atoms), state
+    t0 = time.perf_counter()
+    tr = system(SEED + 7)
+    ev = system(SEED)
+    t_gen = time.perf_counter() - t0
+    # training data: the solver's own multipliers along a trajectory
+    b = backend.CudaBackend(tr[0], tr[1], p)
+    b.upload_state(np.ascontiguousarray(tr[2].pos), np.ascontiguousarray(tr[2].vel))
+    b.forces_resident()
+    b.ws_record(args.train_steps, 1)
+    b.run_resident(dt, args.train_steps)
+    b.synchronize()
+    b.ws_record(0)
+    n_samples = b.counters()["ws_records"] * len(tr[1].constr_i)
+    t1 = time.perf_counter()
+    loss = b.ws_train(args.train_iters, blocks=64, lr=3e-3, seed=11)
+    t_train = time.perf_counter() - t1
+    P, norm = b.ws_params()
+    b.close()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
+    out = {}
+    for name, warm in (("cold", False), ("warm", True)):
+        be = backend.CudaBackend(ev[0], ev[1], p)
+        be.upload_state(np.ascontiguousarray(ev[2].pos), np.ascontiguousarray(ev[2].vel))
+        be.forces_resident()
+        if warm:
+            be.ws_params(P, norm)
+            be.ws_enable(True)
+        be.run_resident(dt, args.warmup)
+        be.synchronize()
+        c0 = be.counters()
+        with ClockSampler(0) as clk:
+            sec = be.time_steps(dt, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                                flush_bytes=L2_FLUSH_BYTES) / 1e3
+        c1 = be.counters()
+        steps = c1["constrained_steps"] - c0["constrained_steps"]
+        out[name] = dict(ns_per_day=round(dt * 1e-3 * args.steps / sec * 86400.0, 3),
+                         mean_shake_iters=round((c1["shake_iter_sum"] - c0["shake_iter_sum"]) / max(steps, 1), 3),
+                         mean_rattle_iters=round((c1["rattle_iter_sum"] - c0["rattle_iter_sum"]) / max(steps, 1), 3),
+                         ms_per_step=round(1e3 * sec / args.steps, 4), clocks=_clock_ok(clk.summary()))
+        be.close()
+    return {"metric": "mean SHAKE iterations and ns/day, BF16 warm start vs cold start, equal tolerance",
+            "value": out["warm"]["ns_per_day"], "unit": "ns/day", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 pair math, fp64 SHAKE/RATTLE, bf16 network", "data": "synthetic (seeded generator)",
+            "config": {"workload": "50,000-atom lattice chain, 40 % H (1.008 amu, constrained 1.09 A bonds), "
+                                   "2 fs, tol 1e-10", "train_seed": SEED + 7, "eval_seed": SEED,
+                       "train_steps_recorded": args.train_steps, "train_samples": int(n_samples),
+                       "train_iters": args.train_iters, "l2": "flushed between timed steps"},
+            "cold": out["cold"], "warm": out["warm"],
+            "warm_over_cold_ns_per_day": round(out["warm"]["ns_per_day"] / out["cold"]["ns_per_day"], 3),
+            "train_loss_standardised": round(loss, 5), "train_s": round(t_train, 2), "generation_s": round(t_gen, 1)}
+
+
+def run_scaled(args, n_atoms, precision, relax, steps_default):
+    """configs[2] (1,000,000 atoms, mixed, 200 steps) and configs[0] (5,000
+    atoms, FP64, 1,000 steps): timed device steps, list rebuild and pair
+    kernel bandwidth."""
+    import torch
+    from geodesic_cuda import backend, synth
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    atoms, topo, state, _ = synth.generate(n_atoms, seed=SEED, temperature=300.0, relax_iters=relax)
+    t_gen = time.perf_counter() - t0
+    p = backend.SimParams(precision=precision, **PHYS)
+    be = backend.CudaBackend(atoms, topo, p)
+    be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
+    be.forces_resident()
+    choice = be.autotune(reps=3) if precision == backend.PRECISION_MIXED else None
+    be.run_resident(DT_PS, args.warmup)
+    be.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
+    steps = args.steps if args.steps_given else steps_default
+    c0 = be.counters()
+    with ClockSampler(0) as clk:
+        sec = be.time_steps(DT_PS, steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                            flush_bytes=L2_FLUSH_BYTES) / 1e3
+    c1 = be.counters()
+    pairs = c1["pairs"]
+    t_pair = be.profile("pair", 10) / 1e3
+    t_reb = be.profile("rebuild", 3) / 1e3
+    peak, peak_kind = measured_peaks()
+    alg_pair = 4 * pairs + 52 * n_atoms
+    # list build algorithmic bytes (SURVEY 8d B_list): N (16 + 8 + 16) + 4 P + 4 N
+    alg_list = n_atoms * 44 + 4 * 2 * pairs
+    return {"metric": f"ns/day at {n_atoms} atoms", "value": round(ns_per_day(steps, sec), 3), "unit": "ns/day",
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sec / steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64" if precision == backend.PRECISION_FP64 else "fp32 pair math, int64 fixed-point forces",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": f"synthetic lattice chain, {n_atoms} atoms, 2 fs, FIRE {relax} iterations",
+                       "n_atoms": n_atoms, "l2": "flushed between timed steps"},
+            "pairs_per_s": round(pairs * steps / sec, 1), "half_list_pairs": pairs,
+            "list_rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
+            "pair_kernel": {"ms": round(t_pair * 1e3, 4), "algorithmic_bytes": alg_pair,
+                            "achieved_gbs": round(alg_pair / t_pair / 1e9, 1),
+                            "frac": round(alg_pair / t_pair / 1e9 / peak, 4)},
+            "list_rebuild": {"ms": round(t_reb * 1e3, 4), "algorithmic_bytes": alg_list,
+                             "achieved_gbs": round(alg_list / t_reb / 1e9, 1),
+                             "frac": round(alg_list / t_reb / 1e9 / peak, 4)},
+            "peak_gbs": peak, "peak_source": peak_kind, "autotuner": choice,
+            "gpu_launches": int(c1["launches"] - c0["launches"]), "generation_s": round(t_gen, 1),
+            "clocks": _clock_ok(clk.summary())}
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -369,8 +576,33 @@ def main():
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no error, CPU-baseline, FP64 or e2e legs); for profiler runs")
-    args = ap.parse_args()
+    ap.add_argument("--config", default="headline",
+                    choices=["headline", "ensemble", "warm_start", "scale_1m", "small_5k"],
+                    help="headline: 50k atoms (the default line); the others print their own line")
+    ap.add_argument("--systems", type=int, default=256, help="ensemble: number of systems")
+    ap.add_argument("--single-steps", type=int, default=200, help="ensemble: timed steps per system one by one")
+    ap.add_argument("--train-steps", type=int, default=2000, help="warm_start: recorded steps")
+    ap.add_argument("--train-iters", type=int, default=4000, help="warm_start: Adam steps")
+    argv = sys.argv[1:]
+    args = ap.parse_args(argv)
+    args.steps_given = any(a == "--steps" or a.startswith("--steps=") for a in argv)
     args.warmup = max(args.warmup, 3)
+    if args.config != "headline":
+        from geodesic_cuda import backend
+        if args.config == "ensemble":
+            if not args.steps_given:
+                args.steps = 1000
+            line = run_ensemble(args)
+        elif args.config == "warm_start":
+            if not args.steps_given:
+                args.steps = 1000
+            line = run_warm_start(args)
+        elif args.config == "scale_1m":
+            line = run_scaled(args, 1_000_000, backend.PRECISION_MIXED, 300, 200)
+        else:
+            line = run_scaled(args, 5_000, backend.PRECISION_FP64, 1000, 1000)
+        print(json.dumps(line), flush=True)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

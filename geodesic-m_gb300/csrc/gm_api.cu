@@ -71,6 +71,7 @@ struct gm_ctx {
     // list
     int cap = 0, n_groups = 0;
     int split = 1;                   // warps per group in the FP32 pair kernel
+    int pair_warps = 4, pair_grid = 0;  // FP32 pair kernel block size and grid (0: one item per warp)
     int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr;
     bool built = false;
     // exclusions
@@ -239,6 +240,8 @@ ForceArgs force_args(gm_ctx *c) {
     a.e_sys = c->n_sys > 1 ? c->d_e_sys : nullptr;
     a.cap = c->cap;
     a.split = c->fp64 ? 1 : c->split;
+    a.pair_warps = c->pair_warps;
+    a.pair_grid = c->pair_grid;
     a.hi = c->d_hi;
     a.lo = c->d_lo;
     a.pos64s = c->d_pos64s;
@@ -1811,6 +1814,54 @@ int32_t gm_ensemble_energies(gm_ctx *c, double *e_pot, double *e_kin) {
         }
     }
     return GM_OK;
+}
+
+/* ---- autotuner ---------------------------------------------------------- */
+
+int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
+    if (!c || reps < 1) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (c->fp64) return fail(c, GM_ERR_UNSUPPORTED, "the autotuner tunes the FP32 pair kernel");
+    int rc = ensure_forces(c);
+    if (rc) return rc;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    cudaEvent_t e0, e1;
+    GM_CUDA(c, cudaEventCreate(&e0));
+    GM_CUDA(c, cudaEventCreate(&e1));
+    const int splits[] = {1, 2, 3, 4, 6, 8, 12, 16};
+    const int warps[] = {2, 4, 8};
+    const int grids[] = {0, 2, 4, 8, 16};  // 0: one work item per warp, else blocks per SM (persistent)
+    double best = 1e300;
+    int bs = c->split, bw = c->pair_warps, bg = c->pair_grid;
+    for (int sp : splits)
+        for (int w : warps)
+            for (int gk : grids) {
+                c->split = sp;
+                c->pair_warps = w;
+                c->pair_grid = gk ? gk * std::max(sms, 1) : 0;
+                ForceArgs fa = force_args(c);
+                gm_launch_pair(fa, false, c->stream);  // warm-up
+                cudaEventRecord(e0, c->stream);
+                for (int r = 0; r < reps; r++) gm_launch_pair(fa, false, c->stream);
+                cudaEventRecord(e1, c->stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                c->launches += reps + 1;
+                if (ms < best) { best = ms; bs = sp; bw = w; bg = c->pair_grid; }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->split = bs;
+    c->pair_warps = bw;
+    c->pair_grid = bg;
+    GM_CUDA(c, cudaGetLastError());
+    // the timing runs added forces many times over: evaluate them once more
+    c->launches += seq_forces(c, c->stream);
+    drop_graph(c);
+    if (choice) { choice[0] = bs; choice[1] = bw; choice[2] = bg; }
+    return check_status(c, nullptr);
 }
 
 }  // extern "C"

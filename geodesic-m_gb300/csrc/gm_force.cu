@@ -26,8 +26,8 @@ constexpr double kCoulomb64 = 332.0522173;
 // result independent of the order in which the parts land.
 // BATCH: systems of a batch have their own type tables ([system][type][type],
 // read through L1); a single system keeps its table in shared memory.
-template <bool PERIODIC, bool COULOMB, bool BATCH>
-__global__ void __launch_bounds__(kPairWarps * 32)
+template <bool PERIODIC, bool COULOMB, bool BATCH, int W>
+__global__ void __launch_bounds__(W * 32)
 pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
                 const int *__restrict__ gmax, int ntypes, const float2 *__restrict__ tab, float rc2, float rsw,
@@ -40,9 +40,11 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    // work items (group, part of its columns); a grid smaller than the work
+    // makes the kernel persistent, every item is computed the same either way
+    const int n_work = (n_slots / 32) * split;
+    for (int wid = blockIdx.x * W + (threadIdx.x >> 5); wid < n_work; wid += gridDim.x * W) {
     const int group = wid / split, part = wid - group * split;
-    if (group * 32 >= n_slots) return;
     const int s = group * 32 + lane;
     const int atom = perm[s];  // -1 on a padding slot
     const bool valid = atom >= 0;
@@ -125,6 +127,7 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
     if (e_sys && lane == 0) gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
+    }
 }
 
 template <bool PERIODIC, bool COULOMB, bool BATCH>
@@ -408,18 +411,23 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
     const int blocks = (a.n_groups + kPairWarps - 1) / kPairWarps;
     const bool batch = a.e_sys != nullptr;
     if (!fp64) {
-        const int blocks32 = (a.n_groups * a.split + kPairWarps - 1) / kPairWarps;
+        const int W = a.pair_warps == 2 || a.pair_warps == 8 ? a.pair_warps : 4;
+        int blocks32 = (a.n_groups * a.split + W - 1) / W;
+        if (a.pair_grid > 0 && a.pair_grid < blocks32) blocks32 = a.pair_grid;
         const size_t smem = batch ? 0 : sizeof(float2) * (size_t)a.ntypes * a.ntypes;
-#define GM_PAIR32(P, Q, B)                                                                                   \
-    pair_kernel_f32<P, Q, B><<<blocks32, kPairWarps * 32, smem, s>>>(                                        \
+#define GM_PAIR32W(P, Q, B, WW)                                                                              \
+    pair_kernel_f32<P, Q, B, WW><<<blocks32, WW * 32, smem, s>>>(                                            \
         a.n, a.n_slots, a.cap, a.split, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, \
         a.inv_wsw, a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status, \
         a.group_sys, a.e_sys)
-#define GM_PAIR32B(P, Q) { if (batch) GM_PAIR32(P, Q, true); else GM_PAIR32(P, Q, false); }
+#define GM_PAIR32(P, Q, B) { if (W == 2) GM_PAIR32W(P, Q, B, 2); else if (W == 8) GM_PAIR32W(P, Q, B, 8); \
+                             else GM_PAIR32W(P, Q, B, 4); }
+#define GM_PAIR32B(P, Q) { if (batch) GM_PAIR32(P, Q, true) else GM_PAIR32(P, Q, false) }
         if (a.periodic) { if (a.coulomb) GM_PAIR32B(true, true) else GM_PAIR32B(true, false) }
         else { if (a.coulomb) GM_PAIR32B(false, true) else GM_PAIR32B(false, false) }
 #undef GM_PAIR32B
 #undef GM_PAIR32
+#undef GM_PAIR32W
     } else {
         const size_t smem = batch ? 0 : sizeof(double2) * (size_t)a.ntypes * a.ntypes;
 #define GM_PAIR64(P, Q, B)                                                                                        \

@@ -161,6 +161,8 @@ struct ForceArgs {
     const int *group_sys, *atom_sys;
     long long *e_sys;        // per-system potential energy, fixed point 2^-32 kcal/mol (batches), or nullptr
     int split;               // warps per 32-atom group in the FP32 pair kernel
+    int pair_warps;          // warps per block of the FP32 pair kernel (2, 4, 8)
+    int pair_grid;           // blocks of the FP32 pair kernel (0: one work item per warp; fewer: persistent)
     const float4 *hi, *lo;
     const double4 *pos64s;
     const int *type_sorted;  // FP64 mode

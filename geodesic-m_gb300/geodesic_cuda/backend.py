@@ -155,6 +155,7 @@ def lib():
         L.gm_create_ensemble.argtypes = [C.c_int32, P(GmAtoms), P(GmTopology), P(GmParams), P(C.c_int32)]
         L.gm_ensemble_info.argtypes = [C.c_void_p, P(C.c_int64)]
         L.gm_ensemble_energies.argtypes = [C.c_void_p, _f64p, _f64p]
+        L.gm_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int64)]
         L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
         L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
         L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
@@ -163,7 +164,7 @@ def lib():
         L.gm_ws_forward.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p]
         L.gm_ws_gradient.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int64, _f32p, P(C.c_double)]
         L.gm_ws_last.argtypes = [C.c_void_p, _f32p, _f64p, _f64p]
-        for f in ("gm_ensemble_info", "gm_ensemble_energies", "gm_ws_record", "gm_ws_samples", "gm_ws_train", "gm_ws_enable", "gm_ws_params", "gm_ws_forward",
+        for f in ("gm_autotune", "gm_ensemble_info", "gm_ensemble_energies", "gm_ws_record", "gm_ws_samples", "gm_ws_train", "gm_ws_enable", "gm_ws_params", "gm_ws_forward",
                   "gm_ws_gradient", "gm_ws_last", "gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
@@ -264,6 +265,13 @@ class CudaBackend:
             raise BackendError(st.value, "gm_create failed")
         self._forces = np.zeros((3, self.n))
         self._energy = 0.0
+
+    def autotune(self, reps=5):
+        """Pick the FP32 pair kernel's split, block size and grid by timing
+        (gm_autotune); returns them."""
+        out = (C.c_int64 * 3)()
+        self._check(lib().gm_autotune(self._h, int(reps), out))
+        return dict(split=out[0], warps_per_block=out[1], grid=out[2])
 
     def ensemble_energies(self):
         """Per-system (potential, kinetic) energies (gm_ensemble_energies)."""

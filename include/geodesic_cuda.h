@@ -206,6 +206,17 @@ int32_t gm_ensemble_info(const gm_ctx *ctx, int64_t *atom_offsets);
  * kinetic energy of the resident velocities (lib.rs:68-77); NULL skips. */
 int32_t gm_ensemble_energies(gm_ctx *ctx, double *e_pot, double *e_kin);
 
+/* ---- autotuner (no reference counterpart) ------------------------------
+ *
+ * Times the FP32 pair kernel on the current list (reps launches per
+ * candidate, CUDA events on the context's stream) over warps per 32-atom
+ * group (1-16: list columns per warp), warps per block (2, 4, 8) and grid
+ * (one work item per warp, or a persistent grid of 2-16 blocks per SM), and
+ * keeps the fastest.  Every candidate computes the same bits (fixed 32-entry
+ * FP32 chunks folded into int64 sums).  choice (nullable): split, warps per
+ * block, grid (0 = one item per warp). */
+int32_t gm_autotune(gm_ctx *ctx, int32_t reps, int64_t *choice);
+
 /* ---- constraint warm start (no reference counterpart) ------------------
  *
  * A 12-64-64-1 SiLU network (BF16 matmul weights and activations, FP32

@@ -111,3 +111,19 @@ def test_batch_with_constraints_converges():
         d = pb[:, sl][:, topo.constr_i] - pb[:, sl][:, topo.constr_j]
         assert np.max(np.abs((d * d).sum(0) - topo.constr_dsq)) < 1e-6
     assert batch.counters()["constrained_steps"] == 50
+
+
+def test_autotuner_keeps_forces_bit_identical():
+    """Every autotuner candidate computes the same sums: the forces after
+    tuning equal the forces before, for a batch and for a single system."""
+    syss = systems()
+    p = backend.SimParams(**PHYS)
+    for be in (backend.CudaBackend.ensemble([s[0] for s in syss], [s[1] for s in syss], p),
+               backend.CudaBackend(*syss[2][:2], p)):
+        pos = concat([s[2].pos for s in syss]) if be.n_sys > 1 else np.ascontiguousarray(syss[2][2].pos)
+        be.build_neighbor_list(pos)
+        f0 = be.compute_forces(pos).copy()
+        choice = be.autotune(reps=2)
+        assert 1 <= choice["split"] <= 16 and choice["warps_per_block"] in (2, 4, 8) and choice["grid"] >= 0
+        f1 = be.compute_forces(pos).copy()
+        assert np.array_equal(f0, f1)
