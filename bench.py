@@ -463,6 +463,35 @@ def run_warm_start(args):
         atoms, topo, state, _ = synth.generate(N_ATOMS, seed=seed, h_fraction=0.4, temperature=300.0,
                                                relax_iters=1000)
         return atoms, amber.promote_hydrogen_bonds(topo, atoms), state
+    if args.quick:
+        # the evaluation system, cold, timed steps only (profiler runs)
+        ev = system(SEED)
+        be = backend.CudaBackend(ev[0], ev[1], p)
+        be.upload_state(np.ascontiguousarray(ev[2].pos), np.ascontiguousarray(ev[2].vel))
+        be.forces_resident()
+        be.run_resident(dt, args.warmup)
+        be.synchronize()
+        c0 = be.counters()
+        sec = be.time_steps(dt, args.steps, first_step=args.warmup) / 1e3
+        c1 = be.counters()
+        cold = {"ms_per_step": round(1e3 * sec / args.steps, 4),
+                "mean_shake_iters": (c1["shake_iter_sum"] - c0["shake_iter_sum"]) / max(args.steps, 1),
+                "rebuilds": c1["rebuilds"] - c0["rebuilds"]}
+        # then warm-started, with a network trained briefly on this run's own
+        # multipliers (profiling the warm-start kernels, not its benefit)
+        be.ws_record(50, 1)
+        be.run_resident(dt, 50, first_step=args.warmup + args.steps)
+        be.synchronize()
+        be.ws_record(0)
+        be.ws_train(300, blocks=32, lr=3e-3, seed=5)
+        be.ws_enable(True)
+        c0 = be.counters()
+        sec = be.time_steps(dt, args.steps, first_step=args.warmup + args.steps + 50) / 1e3
+        c1 = be.counters()
+        warm = {"ms_per_step": round(1e3 * sec / args.steps, 4),
+                "mean_shake_iters": (c1["shake_iter_sum"] - c0["shake_iter_sum"]) / max(args.steps, 1)}
+        return {"metric": "constrained 50k step time (quick)", "value": cold["ms_per_step"], "unit": "ms/step",
+                "steps": args.steps, "quick": True, "cold": cold, "warm": warm}
     t0 = time.perf_counter()
     tr = system(SEED + 7)
     ev = system(SEED)

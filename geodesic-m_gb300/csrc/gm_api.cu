@@ -86,7 +86,7 @@ struct gm_ctx {
     int n14 = 0, blocks14 = 0;
     int *d_p14i = nullptr, *d_p14j = nullptr;
     // constraints
-    int n_constr = 0, n_clusters = 0;
+    int n_constr = 0, n_clusters = 0, n_single = 0, n_warp_end = 0;
     int *d_ci = nullptr, *d_cj = nullptr, *d_cl_cstart = nullptr, *d_cl_cons = nullptr, *d_cl_astart = nullptr,
         *d_cl_atoms = nullptr, *d_cl_acstart = nullptr, *d_cl_acons = nullptr, *d_cl_iters = nullptr,
         *d_cl_worst_idx = nullptr;
@@ -296,6 +296,8 @@ ForceArgs force_args(gm_ctx *c) {
 ClusterArgs cluster_args(gm_ctx *c) {
     ClusterArgs a{};
     a.n_clusters = c->n_clusters;
+    a.n_single = c->n_single;
+    a.n_warp_end = c->n_warp_end;
     a.cl_cstart = c->d_cl_cstart; a.cl_cons = c->d_cl_cons;
     a.cl_astart = c->d_cl_astart; a.cl_atoms = c->d_cl_atoms;
     a.cl_acstart = c->d_cl_acstart; a.cl_acons = c->d_cl_acons;
@@ -688,11 +690,39 @@ void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int
         if (it == root_id.end()) { it = root_id.emplace(r, (int)ccons.size()).first; ccons.emplace_back(); catoms.emplace_back(); }
         ccons[(size_t)it->second].push_back(k);  // ascending k
     }
+    // clusters in three classes, in this order: one constraint on two atoms
+    // (one per thread), 2-32 constraints on at most 32 atoms with at most 8
+    // constraints per atom (one per warp), the rest; within a class by size
+    // (stable), so a warp's threads run loops of the same lengths.  The
+    // solution does not depend on the cluster order.
+    const size_t ncl = ccons.size();
+    std::vector<int> cls(ncl);
+    for (size_t q = 0; q < ncl; q++) {
+        std::vector<int> at, deg;
+        for (int k : ccons[q]) { at.push_back(ci[(size_t)k]); at.push_back(cj[(size_t)k]); }
+        std::sort(at.begin(), at.end());
+        int maxdeg = 0, run = 0;
+        for (size_t t = 0; t < at.size(); t++) {
+            run = (t > 0 && at[t] == at[t - 1]) ? run + 1 : 1;
+            maxdeg = std::max(maxdeg, run);
+        }
+        at.erase(std::unique(at.begin(), at.end()), at.end());
+        const int nc = (int)ccons[q].size(), na = (int)at.size();
+        cls[q] = (nc == 1 && na == 2) ? 0 : (nc <= 32 && na <= 32 && maxdeg <= 8 ? 1 : 2);
+    }
+    std::vector<size_t> order(ncl);
+    std::iota(order.begin(), order.end(), (size_t)0);
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+        if (cls[x] != cls[y]) return cls[x] < cls[y];
+        return ccons[x].size() < ccons[y].size();
+    });
+    c->n_single = (int)std::count(cls.begin(), cls.end(), 0);
+    c->n_warp_end = c->n_single + (int)std::count(cls.begin(), cls.end(), 1);
     cstart.assign(1, 0);
     astart.assign(1, 0);
     acstart.assign(1, 0);
     cons.clear(); atoms.clear(); acons.clear();
-    for (size_t q = 0; q < ccons.size(); q++) {
+    for (size_t q : order) {
         std::vector<int> at;
         for (int k : ccons[q]) { at.push_back(ci[(size_t)k]); at.push_back(cj[(size_t)k]); }
         std::sort(at.begin(), at.end());
@@ -1056,6 +1086,14 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         std::vector<int> cstart, cons, astart, cat, acstart, acons;
         build_clusters(c, c->h_ci, c->h_cj, cstart, cons, astart, cat, acstart, acons);
         c->n_clusters = (int)cstart.size() - 1;
+        // the kernels index these prefix tables without bounds checks
+        if (cstart.empty() || cstart.front() != 0 || cstart.back() != c->n_constr || astart.size() != cstart.size() ||
+            astart.front() != 0 || astart.back() != (int)cat.size() || acstart.size() != cat.size() + 1 ||
+            acstart.front() != 0 || acstart.back() != (int)acons.size() || c->n_single > c->n_warp_end ||
+            c->n_warp_end > c->n_clusters) {
+            fail(c, GM_ERR_DEVICE, "inconsistent constraint cluster tables");
+            return bail(GM_ERR_DEVICE);
+        }
         TRY(dupload(c, &c->d_ci, c->h_ci.data(), c->h_ci.size()));
         TRY(dupload(c, &c->d_cj, c->h_cj.data(), c->h_cj.size()));
         TRY(dupload(c, &c->d_cdsq, t->constr_dsq, (size_t)c->n_constr));

@@ -203,12 +203,318 @@ __global__ void shake_prepare(ClusterArgs c, const double *dref, int n_atoms) {
     if (c.lam_sum) c.lam_sum[k] = 0.0;
 }
 
+// Clusters of 2-32 constraints on at most 32 atoms (a heavy atom with its H
+// atoms): one warp per cluster.  Lane a keeps atom a's coordinates and its
+// constraint list in registers, lane q keeps constraint q's bond vector and
+// multiplier; values move between lanes by shuffles.  Each lane's arithmetic
+// is that of shake_iteration / rattle_iteration in the same order, and the
+// largest |lambda| and its constraint (the first in ascending order on ties)
+// come from a warp reduction, so the bits are those of the sequential sweep.
+constexpr int kWarpRefs = 8;  // constraints per atom handled by the warp path
+
+// Lane a < na adds its atom's displacement over its constraints (ascending,
+// from 0.0): every lane runs the loop to the warp's longest list so that
+// every shuffle has all 32 lanes.
+__device__ __forceinline__ void warp_atom_update(int lane, int na, int nref, int maxref, const int *ref_l,
+                                                 const int *ref_s, double im_a, double lam, double rx, double ry,
+                                                 double rz, double &X, double &Y, double &Z) {
+    double ddx = 0.0, ddy = 0.0, ddz = 0.0;
+    for (int r = 0; r < maxref; r++) {
+        const bool mine = lane < na && r < nref;
+        const int l = mine ? ref_l[r] : 0;
+        const double lam_l = __shfl_sync(0xffffffffu, lam, l);
+        const double rx_l = __shfl_sync(0xffffffffu, rx, l);
+        const double ry_l = __shfl_sync(0xffffffffu, ry, l);
+        const double rz_l = __shfl_sync(0xffffffffu, rz, l);
+        if (mine) {
+            const double w = lam_l * im_a;
+            const double tx = w * rx_l, ty = w * ry_l, tz = w * rz_l;
+            if (ref_s[r] < 0) { ddx -= tx; ddy -= ty; ddz -= tz; }
+            else { ddx += tx; ddy += ty; ddz += tz; }
+        }
+    }
+    if (lane < na) {
+        X += ddx;
+        Y += ddy;
+        Z += ddz;
+    }
+}
+
+template <bool RATTLE>
+__device__ void cluster_warp(const ClusterArgs &c, int cl, double *pos, double *vel, int n, bool phase2) {
+    const int lane = threadIdx.x & 31;
+    const DevStatus *st = c.status;
+    unsigned T = 0;
+    if (!phase2) {
+        if (st->error) return;
+    } else {
+        T = RATTLE ? st->rattle_T : st->shake_T;
+        if ((st->error & ~(unsigned)(GM_DEV_SHAKE_FAIL | GM_DEV_RATTLE_FAIL)) != 0) return;
+        if ((unsigned)c.cl_iters[cl] >= T) return;
+    }
+    const int c0 = c.cl_cstart[cl], nc = c.cl_cstart[cl + 1] - c0;
+    const int a0 = c.cl_astart[cl], na = c.cl_astart[cl + 1] - a0;
+    const int ncst = c.n_constr;
+    double *v = RATTLE ? vel : pos;
+    // atoms: lane a holds atom a and its constraint list (local indices)
+    int ag = 0;
+    double im_a = 0.0, X = 0.0, Y = 0.0, Z = 0.0;
+    int nref = 0, ref_l[kWarpRefs], ref_s[kWarpRefs];
+    if (lane < na) {
+        ag = c.cl_atoms[a0 + lane];
+        im_a = c.inv_mass[ag];
+        X = v[ag]; Y = v[n + ag]; Z = v[2 * n + ag];
+        const int r0 = c.cl_acstart[a0 + lane], r1 = c.cl_acstart[a0 + lane + 1];
+        for (int r = r0; r < r1 && nref < kWarpRefs; r++) {
+            const int ref = c.cl_acons[r];
+            const int kk = ref >= 0 ? ref : -ref - 1;
+            int l = 0;
+            for (int t = 0; t < nc; t++) if (c.cl_cons[c0 + t] == kk) l = t;
+            ref_l[nref] = l;
+            ref_s[nref] = ref >= 0 ? 1 : -1;
+            nref++;
+        }
+    }
+    int maxref = nref;
+    for (int o = 16; o > 0; o >>= 1) maxref = max(maxref, __shfl_xor_sync(0xffffffffu, maxref, o));
+    // constraints: lane q holds constraint q
+    int k = 0, il = 0, jl = 0;
+    double wq = 0.0, dsq = 0.0, acc = 0.0, rx = 0.0, ry = 0.0, rz = 0.0, lam = 0.0;
+    if (lane < nc) {
+        k = c.cl_cons[c0 + lane];
+        const int i = c.constr_i[k], j = c.constr_j[k];
+        for (int t = 0; t < na; t++) {
+            const int a = c.cl_atoms[a0 + t];
+            if (a == i) il = t;
+            if (a == j) jl = t;
+        }
+        const double inv_mi = c.inv_mass[i], inv_mj = c.inv_mass[j];
+        if (!RATTLE) {
+            dsq = c.constr_dsq[k];
+            rx = c.rvec[k]; ry = c.rvec[ncst + k]; rz = c.rvec[2 * ncst + k];
+            wq = 2.0 * (inv_mi + inv_mj);
+        } else {
+            // constraint.rs:205-215: the bond vector of the fixed positions
+            rx = pos[i] - pos[j];
+            ry = pos[n + i] - pos[n + j];
+            rz = pos[2 * n + i] - pos[2 * n + j];
+            const double rsq = rx * rx + ry * ry + rz * rz;
+            wq = (inv_mi + inv_mj) * rsq;
+        }
+    }
+    const int k0 = __shfl_sync(0xffffffffu, k, 0);
+    const bool keep_sum = !RATTLE && c.lam_sum;
+    unsigned it;
+    double mx;
+    int worst;
+    if (!phase2) {
+        it = 0;
+        mx = 0.0;
+        worst = 0;
+        if (!RATTLE && c.lam0) {
+            if (lane < nc) { acc = c.lam0[k]; lam = acc; }
+            warp_atom_update(lane, na, nref, maxref, ref_l, ref_s, im_a, lam, rx, ry, rz, X, Y, Z);
+        }
+    } else {
+        it = (unsigned)c.cl_iters[cl];
+        mx = c.cl_worst[cl];
+        worst = c.cl_worst_idx[cl];
+        if (keep_sum && lane < nc) acc = c.lam_sum[k];
+    }
+    bool ok = false;
+    const unsigned stop = phase2 ? T : c.max_iter;
+    while (it < stop) {
+        // constraint lanes fetch their two atoms
+        const double xi = __shfl_sync(0xffffffffu, X, il), yi = __shfl_sync(0xffffffffu, Y, il),
+                     zi = __shfl_sync(0xffffffffu, Z, il);
+        const double xj = __shfl_sync(0xffffffffu, X, jl), yj = __shfl_sync(0xffffffffu, Y, jl),
+                     zj = __shfl_sync(0xffffffffu, Z, jl);
+        double la = 0.0;
+        lam = 0.0;
+        if (lane < nc) {
+            double l_;
+            if (RATTLE) {
+                const double dvx = xi - xj;
+                const double dvy = yi - yj;
+                const double dvz = zi - zj;
+                const double rel_vel = dvx * rx + dvy * ry + dvz * rz;
+                l_ = wq == 0.0 ? 0.0 : rel_vel / wq;
+            } else {
+                const double dx = xi - xj;
+                const double dy = yi - yj;
+                const double dz = zi - zj;
+                const double diff = dx * dx + dy * dy + dz * dz - dsq;
+                const double dot_new_old = dx * rx + dy * ry + dz * rz;
+                const double denom = wq * dot_new_old;
+                l_ = denom == 0.0 ? 0.0 : diff / denom;
+                if (keep_sum) acc += l_;
+            }
+            la = fabs(l_);
+            lam = l_;
+        }
+        // the largest |lambda| (a NaN never wins, as with the sequential '>')
+        // and the first constraint that reaches it
+        double m = la > 0.0 ? la : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const unsigned hit = __ballot_sync(0xffffffffu, lane < nc && la == m && m > 0.0);
+        worst = __shfl_sync(0xffffffffu, k, hit ? __ffs(hit) - 1 : 0);
+        if (!hit) worst = k0;
+        mx = m;
+        warp_atom_update(lane, na, nref, maxref, ref_l, ref_s, im_a, lam, rx, ry, rz, X, Y, Z);
+        it++;
+        if (!phase2 && mx < c.tol) { ok = true; break; }
+    }
+    if (lane < na) { v[ag] = X; v[n + ag] = Y; v[2 * n + ag] = Z; }
+    if (keep_sum && lane < nc) c.lam_sum[k] = acc;
+    if (lane == 0) {
+        c.cl_iters[cl] = (int)it;
+        c.cl_worst[cl] = mx;
+        c.cl_worst_idx[cl] = worst;
+        if (!phase2) {
+            if (!ok) {
+                atomicOr(&c.status->error, RATTLE ? (unsigned)GM_DEV_RATTLE_FAIL : (unsigned)GM_DEV_SHAKE_FAIL);
+                atomicMin(&c.status->fail_step, c.status->step);
+            }
+            atomicMax(RATTLE ? &c.status->rattle_T : &c.status->shake_T, it);
+        } else if (!(mx < c.tol) && T < c.max_iter) {
+            atomicOr(&c.status->error, (unsigned)GM_DEV_ITER_MISMATCH);
+        }
+    }
+}
+
+// The per-atom update of a one-constraint cluster for multiplier l: atom i
+// subtracts, atom j adds, each sum starting from 0.0.
+__device__ __forceinline__ void single_apply(double l, double inv_mi, double inv_mj, double rx, double ry, double rz,
+                                             double &xi, double &yi, double &zi, double &xj, double &yj, double &zj) {
+    const double wi = l * inv_mi;
+    double ddx = 0.0, ddy = 0.0, ddz = 0.0;
+    ddx -= wi * rx; ddy -= wi * ry; ddz -= wi * rz;
+    const double wj = l * inv_mj;
+    double edx = 0.0, edy = 0.0, edz = 0.0;
+    edx += wj * rx; edy += wj * ry; edz += wj * rz;
+    xi += ddx; yi += ddy; zi += ddz;
+    xj += edx; yj += edy; zj += edz;
+}
+
+// A cluster of one constraint (one heavy atom and one H: most H-bond
+// clusters) entirely in scalar registers.  The operations are those of the
+// general path in the same order, including the per-atom sums that start
+// from 0.0, so the bits are the same.
+template <bool RATTLE>
+__device__ void cluster_single(const ClusterArgs &c, int cl, double *pos, double *vel, int n, bool phase2) {
+    const DevStatus *st = c.status;
+    unsigned T = 0;
+    if (!phase2) {
+        if (st->error) return;
+    } else {
+        T = RATTLE ? st->rattle_T : st->shake_T;
+        if ((st->error & ~(unsigned)(GM_DEV_SHAKE_FAIL | GM_DEV_RATTLE_FAIL)) != 0) return;
+        if ((unsigned)c.cl_iters[cl] >= T) return;
+    }
+    const int k = c.cl_cons[c.cl_cstart[cl]];
+    const int i = c.constr_i[k], j = c.constr_j[k];
+    const double inv_mi = c.inv_mass[i], inv_mj = c.inv_mass[j];
+    double *v = RATTLE ? vel : pos;
+    double xi = v[i], yi = v[n + i], zi = v[2 * n + i];
+    double xj = v[j], yj = v[n + j], zj = v[2 * n + j];
+    const int ncst = c.n_constr;
+    double rx, ry, rz, wq, dsq = 0.0;
+    if (!RATTLE) {
+        dsq = c.constr_dsq[k];
+        rx = c.rvec[k]; ry = c.rvec[ncst + k]; rz = c.rvec[2 * ncst + k];
+        wq = 2.0 * (inv_mi + inv_mj);
+    } else {
+        rx = pos[i] - pos[j];
+        ry = pos[n + i] - pos[n + j];
+        rz = pos[2 * n + i] - pos[2 * n + j];
+        const double rsq = rx * rx + ry * ry + rz * rz;
+        wq = (inv_mi + inv_mj) * rsq;
+    }
+    const bool keep_sum = !RATTLE && c.lam_sum;
+    double acc = 0.0;
+    unsigned it;
+    double mx;
+    int worst;
+    if (!phase2) {
+        it = 0;
+        mx = 0.0;
+        worst = 0;
+        if (!RATTLE && c.lam0) {
+            acc = c.lam0[k];
+            single_apply(acc, inv_mi, inv_mj, rx, ry, rz, xi, yi, zi, xj, yj, zj);
+        }
+    } else {
+        it = (unsigned)c.cl_iters[cl];
+        mx = c.cl_worst[cl];
+        worst = c.cl_worst_idx[cl];
+        if (keep_sum) acc = c.lam_sum[k];
+    }
+    bool ok = false;
+    const unsigned stop = phase2 ? T : c.max_iter;
+    while (it < stop) {
+        double l_;
+        if (RATTLE) {
+            const double dvx = xi - xj;
+            const double dvy = yi - yj;
+            const double dvz = zi - zj;
+            const double rel_vel = dvx * rx + dvy * ry + dvz * rz;
+            l_ = wq == 0.0 ? 0.0 : rel_vel / wq;
+        } else {
+            const double dx = xi - xj;
+            const double dy = yi - yj;
+            const double dz = zi - zj;
+            const double diff = dx * dx + dy * dy + dz * dz - dsq;
+            const double dot_new_old = dx * rx + dy * ry + dz * rz;
+            const double denom = wq * dot_new_old;
+            l_ = denom == 0.0 ? 0.0 : diff / denom;
+            if (keep_sum) acc += l_;
+        }
+        const double la = fabs(l_);
+        mx = 0.0;
+        worst = k;
+        if (la > mx) mx = la;
+        single_apply(l_, inv_mi, inv_mj, rx, ry, rz, xi, yi, zi, xj, yj, zj);
+        it++;
+        if (!phase2 && mx < c.tol) { ok = true; break; }
+    }
+    v[i] = xi; v[n + i] = yi; v[2 * n + i] = zi;
+    v[j] = xj; v[n + j] = yj; v[2 * n + j] = zj;
+    if (keep_sum) c.lam_sum[k] = acc;
+    c.cl_iters[cl] = (int)it;
+    c.cl_worst[cl] = mx;
+    c.cl_worst_idx[cl] = worst;
+    if (!phase2) {
+        if (!ok) {
+            atomicOr(&c.status->error, RATTLE ? (unsigned)GM_DEV_RATTLE_FAIL : (unsigned)GM_DEV_SHAKE_FAIL);
+            atomicMin(&c.status->fail_step, c.status->step);
+        }
+        atomicMax(RATTLE ? &c.status->rattle_T : &c.status->shake_T, it);
+    } else if (!(mx < c.tol) && T < c.max_iter) {
+        atomicOr(&c.status->error, (unsigned)GM_DEV_ITER_MISMATCH);
+    }
+}
+
 // Warm start: one displacement with the predicted multipliers lam0, by the
 // update of a Jacobi sweep (per-atom deltas over the atom's constraints in
 // ascending order from 0.0, then added), before the unchanged iterations.
 // The multiplier totals start from lam0.
+// Clusters come in three ranges: [0, n_single) single constraints, one per
+// thread; [n_single, n_warp_end) 2-32 constraints, one per warp; the rest one
+// per thread through global memory.  Launched with 32-thread blocks.
+__device__ __forceinline__ int big_cluster(const ClusterArgs &c, int block) {
+    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
+    return c.n_warp_end + (block - b_single - b_warp) * 32 + (int)threadIdx.x;
+}
+
+int cluster_blocks(const ClusterArgs &c) {
+    return (c.n_single + 31) / 32 + (c.n_warp_end - c.n_single) + (c.n_clusters - c.n_warp_end + 31) / 32;
+}
+
 __global__ void warm_start_apply(ClusterArgs c, double *pos, int n_atoms) {
-    int cl = blockIdx.x * blockDim.x + threadIdx.x;
+    // big clusters only: the other paths apply the warm start themselves
+    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
+    if ((int)blockIdx.x < b_single + b_warp) return;
+    const int cl = big_cluster(c, blockIdx.x);
     if (cl >= c.n_clusters || c.status->error) return;
     const int nc = c.n_constr;
     if (c.lam_sum)
@@ -233,8 +539,19 @@ __global__ void warm_start_apply(ClusterArgs c, double *pos, int n_atoms) {
 
 template <bool RATTLE>
 __global__ void cluster_phase1(ClusterArgs c, double *pos, double *vel, int n_atoms) {
-    int cl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cl >= c.n_clusters || c.status->error) return;
+    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
+    if ((int)blockIdx.x < b_single) {
+        const int cl = blockIdx.x * 32 + threadIdx.x;
+        if (cl < c.n_single) cluster_single<RATTLE>(c, cl, pos, vel, n_atoms, false);
+        return;
+    }
+    if ((int)blockIdx.x < b_single + b_warp) {
+        cluster_warp<RATTLE>(c, c.n_single + (blockIdx.x - b_single), pos, vel, n_atoms, false);
+        return;
+    }
+    const int cl = big_cluster(c, blockIdx.x);
+    if (cl >= c.n_clusters) return;
+    if (c.status->error) return;
     double mx = 0.0;
     int worst = 0;
     unsigned it = 0;
@@ -257,7 +574,17 @@ __global__ void cluster_phase1(ClusterArgs c, double *pos, double *vel, int n_at
 
 template <bool RATTLE>
 __global__ void cluster_phase2(ClusterArgs c, double *pos, double *vel, int n_atoms) {
-    int cl = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
+    if ((int)blockIdx.x < b_single) {
+        const int cl = blockIdx.x * 32 + threadIdx.x;
+        if (cl < c.n_single) cluster_single<RATTLE>(c, cl, pos, vel, n_atoms, true);
+        return;
+    }
+    if ((int)blockIdx.x < b_single + b_warp) {
+        cluster_warp<RATTLE>(c, c.n_single + (blockIdx.x - b_single), pos, vel, n_atoms, true);
+        return;
+    }
+    const int cl = big_cluster(c, blockIdx.x);
     if (cl >= c.n_clusters) return;
     const unsigned T = RATTLE ? c.status->rattle_T : c.status->shake_T;
     if ((c.status->error & ~(unsigned)(GM_DEV_SHAKE_FAIL | GM_DEV_RATTLE_FAIL)) != 0) return;
@@ -365,11 +692,13 @@ void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dr
 
 int gm_launch_shake_solve(const ClusterArgs &c, int n_atoms, double *pos, cudaStream_t s) {
     if (c.n_clusters == 0) return 0;
-    const int b = (c.n_clusters + 127) / 128;
+    // 32-thread blocks over the three cluster ranges: the FP64 pipe of
+    // every SM gets a share of the (few) clusters
+    const int b = cluster_blocks(c);
     int k = 0;
-    if (c.lam0) { warm_start_apply<<<b, 128, 0, s>>>(c, pos, n_atoms); k++; }
-    cluster_phase1<false><<<b, 128, 0, s>>>(c, pos, nullptr, n_atoms);
-    cluster_phase2<false><<<b, 128, 0, s>>>(c, pos, nullptr, n_atoms);
+    if (c.lam0) { warm_start_apply<<<b, 32, 0, s>>>(c, pos, n_atoms); k++; }
+    cluster_phase1<false><<<b, 32, 0, s>>>(c, pos, nullptr, n_atoms);
+    cluster_phase2<false><<<b, 32, 0, s>>>(c, pos, nullptr, n_atoms);
     return k + 2;
 }
 
@@ -381,9 +710,9 @@ void gm_launch_shake(const ClusterArgs &c, int n_atoms, const double *dref, doub
 void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s) {
     if (c.n_clusters == 0) return;
     reset_T<<<1, 1, 0, s>>>(c.status, 1);
-    const int b = (c.n_clusters + 127) / 128;
-    cluster_phase1<true><<<b, 128, 0, s>>>(c, const_cast<double *>(pos), vel, n_atoms);
-    cluster_phase2<true><<<b, 128, 0, s>>>(c, const_cast<double *>(pos), vel, n_atoms);
+    const int b = cluster_blocks(c);
+    cluster_phase1<true><<<b, 32, 0, s>>>(c, const_cast<double *>(pos), vel, n_atoms);
+    cluster_phase2<true><<<b, 32, 0, s>>>(c, const_cast<double *>(pos), vel, n_atoms);
 }
 
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,

@@ -205,6 +205,8 @@ int gm_bonded_blocks(int n_bonds, int n_angles, int n_diheds);
 
 struct ClusterArgs {
     int n_clusters;
+    int n_single;                         // clusters [0, n_single): one constraint on two atoms
+    int n_warp_end;                       // clusters [n_single, n_warp_end): 2-32 constraints, <= 32 atoms
     const int *cl_cstart, *cl_cons;       // cluster -> constraints (ascending)
     const int *cl_astart, *cl_atoms;      // cluster -> atoms
     const int *cl_acstart, *cl_acons;     // cluster-atom slot -> signed constraint refs (ascending)
@@ -269,6 +271,7 @@ constexpr int GM_WS_TILE = 128;  // samples per block of the training kernel
 //  atom a of (1/m_a) / w_k cos(r_k, r_l) s_k s_l t1_l w_k / w_l (the first
 //  order coupling; s = +1 where a is the constraint's i, -1 where it is j)
 //  9 sum of the squared coupling coefficients   10 max |cos|   11 sum of t1_l
+//  (8-11 in FP32)
 struct WsFeatureArgs {
     int n_constr, n_atoms;
     const int *constr_i, *constr_j;

@@ -33,15 +33,20 @@ __device__ __forceinline__ double dot3(double ax, double ay, double az, double b
     return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
 }
 
-// Reference bond direction r_k / |r_k| (FP64, fixed operation order).
-__device__ __forceinline__ void ref_unit(const WsFeatureArgs &a, int k, double &ux, double &uy, double &uz) {
+__device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// Reference bond direction r_k / |r_k| in FP32 (the FP64 difference rounded
+// once, then correctly rounded FP32 operations in a fixed order).
+__device__ __forceinline__ void ref_unit(const WsFeatureArgs &a, int k, float &ux, float &uy, float &uz) {
     const int i = a.constr_i[k], j = a.constr_j[k], n = a.n_atoms;
-    const double rx = __dsub_rn(a.dref[i], a.dref[j]), ry = __dsub_rn(a.dref[n + i], a.dref[n + j]),
-                 rz = __dsub_rn(a.dref[2 * n + i], a.dref[2 * n + j]);
-    const double il = __ddiv_rn(1.0, __dsqrt_rn(dot3(rx, ry, rz, rx, ry, rz)));
-    ux = __dmul_rn(rx, il);
-    uy = __dmul_rn(ry, il);
-    uz = __dmul_rn(rz, il);
+    const float rx = (float)__dsub_rn(a.dref[i], a.dref[j]), ry = (float)__dsub_rn(a.dref[n + i], a.dref[n + j]),
+                rz = (float)__dsub_rn(a.dref[2 * n + i], a.dref[2 * n + j]);
+    const float il = __fdiv_rn(1.0f, __fsqrt_rn(dot3f(rx, ry, rz, rx, ry, rz)));
+    ux = __fmul_rn(rx, il);
+    uy = __fmul_rn(ry, il);
+    uz = __fmul_rn(rz, il);
 }
 
 // Pass 1: the constraint's own features 0-7, t1 and the scale.
@@ -71,40 +76,42 @@ __global__ void ws_features_kernel(WsFeatureArgs a) {
 }
 
 // Pass 2: coupling to the other constraints on the constraint's two atoms
-// (features 8-11), atom i's constraints then atom j's, each ascending.
+// (features 8-11) in FP32, atom i's constraints then atom j's, each
+// ascending; masses and t1 enter rounded to FP32.
 __global__ void ws_coupling_kernel(WsFeatureArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n_constr) return;
     const int ends[2] = {a.constr_i[k], a.constr_j[k]};
-    const double wk = __dadd_rn(a.inv_mass[ends[0]], a.inv_mass[ends[1]]);
-    double ux, uy, uz;
+    const float wk = __fadd_rn((float)a.inv_mass[ends[0]], (float)a.inv_mass[ends[1]]);
+    float ux, uy, uz;
     ref_unit(a, k, ux, uy, uz);
-    double c1 = 0.0, c2 = 0.0, cmax = 0.0, ct = 0.0;
+    float c1 = 0.0f, c2 = 0.0f, cmax = 0.0f, ct = 0.0f;
     for (int e = 0; e < 2; e++) {
         const int at = ends[e];
-        const double sk = e == 0 ? 1.0 : -1.0;
-        const double inv_a = a.inv_mass[at];
+        const float sk = e == 0 ? 1.0f : -1.0f;
+        const float inv_a = (float)a.inv_mass[at];
         for (int q = a.atom_cstart[at]; q < a.atom_cstart[at + 1]; q++) {
             const int ref = a.atom_cref[q];
             const int l = ref >= 0 ? ref : -ref - 1;
             if (l == k) continue;
-            const double sl = ref >= 0 ? 1.0 : -1.0;
-            double vx, vy, vz;
+            const float sl = ref >= 0 ? 1.0f : -1.0f;
+            float vx, vy, vz;
             ref_unit(a, l, vx, vy, vz);
-            const double cs = dot3(ux, uy, uz, vx, vy, vz);
-            const double wl = __dadd_rn(a.inv_mass[a.constr_i[l]], a.inv_mass[a.constr_j[l]]);
-            const double coup = __dmul_rn(__dmul_rn(__ddiv_rn(inv_a, wk), cs), __dmul_rn(sk, sl));
-            c1 = __dadd_rn(c1, __ddiv_rn(__dmul_rn(__dmul_rn(coup, a.t1[l]), wk), wl));
-            c2 = __dadd_rn(c2, __dmul_rn(coup, coup));
-            cmax = fmax(cmax, fabs(cs));
-            ct = __dadd_rn(ct, a.t1[l]);
+            const float cs = dot3f(ux, uy, uz, vx, vy, vz);
+            const float wl = __fadd_rn((float)a.inv_mass[a.constr_i[l]], (float)a.inv_mass[a.constr_j[l]]);
+            const float coup = __fmul_rn(__fmul_rn(__fdiv_rn(inv_a, wk), cs), __fmul_rn(sk, sl));
+            const float tl = (float)a.t1[l];
+            c1 = __fadd_rn(c1, __fdiv_rn(__fmul_rn(__fmul_rn(coup, tl), wk), wl));
+            c2 = __fadd_rn(c2, __fmul_rn(coup, coup));
+            cmax = fmaxf(cmax, fabsf(cs));
+            ct = __fadd_rn(ct, tl);
         }
     }
     float *f = a.feat + (size_t)k * kIn;
-    f[8] = (float)c1;
-    f[9] = (float)c2;
-    f[10] = (float)cmax;
-    f[11] = (float)ct;
+    f[8] = c1;
+    f[9] = c2;
+    f[10] = cmax;
+    f[11] = ct;
 }
 
 // Weights into shared memory: matmul weights BF16-rounded, biases as is.

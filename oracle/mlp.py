@@ -48,8 +48,9 @@ def features(constr_i, constr_j, dsq, pos, ref, inv_mass):
       9 sum of the squared coupling coefficients   10 max |cos|   11 sum t1_l
 
     (s = +1 where a is the constraint's i, -1 where it is its j; w = 1/m_i +
-    1/m_j.)  Plain FP64 operations in the device's order: atom i's
-    constraints, then atom j's, each ascending."""
+    1/m_j.)  Features 0-7 from FP64 operations rounded once, 8-11 in FP32
+    (masses, t1 and the FP64 bond vectors rounded to FP32 first), in the
+    device's order: atom i's constraints, then atom j's, each ascending."""
     ci = [int(v) for v in constr_i]
     cj = [int(v) for v in constr_j]
     dsq = [float(v) for v in dsq]
@@ -65,10 +66,13 @@ def features(constr_i, constr_j, dsq, pos, ref, inv_mass):
     def dot3(ax, ay, az, bx, by, bz):
         return (ax * bx + ay * by) + az * bz
 
+    f32 = np.float32
+
     def unit(k):
+        # FP32: the FP64 difference rounded once, then float32 operations
         i, j = ci[k], cj[k]
-        rx, ry, rz = RX[i] - RX[j], RY[i] - RY[j], RZ[i] - RZ[j]
-        il = 1.0 / np.sqrt(dot3(rx, ry, rz, rx, ry, rz))
+        rx, ry, rz = f32(RX[i] - RX[j]), f32(RY[i] - RY[j]), f32(RZ[i] - RZ[j])
+        il = f32(1.0) / np.sqrt(dot3(rx, ry, rz, rx, ry, rz))
         return rx * il, ry * il, rz * il
 
     f = np.empty((C, N_IN), np.float32)
@@ -85,21 +89,23 @@ def features(constr_i, constr_j, dsq, pos, ref, inv_mass):
         f[k, :8] = [(t2 - dsq[k]) / dsq[k], dr / dsq[k], np.sqrt(dsq[k]), inv[i], inv[j], len(rows[i]),
                     len(rows[j]), t1[k]]
     for k in range(C):
-        wk = inv[ci[k]] + inv[cj[k]]
+        wk = f32(inv[ci[k]]) + f32(inv[cj[k]])
         ux, uy, uz = unit(k)
-        c1 = c2 = cmax = ct = 0.0
-        for at, sk in ((ci[k], 1.0), (cj[k], -1.0)):
+        c1 = c2 = cmax = ct = f32(0.0)
+        for at, sk in ((ci[k], f32(1.0)), (cj[k], f32(-1.0))):
+            ia = f32(inv[at])
             for l, sl in rows[at]:
                 if l == k:
                     continue
                 vx, vy, vz = unit(l)
                 cs = dot3(ux, uy, uz, vx, vy, vz)
-                wl = inv[ci[l]] + inv[cj[l]]
-                coup = ((inv[at] / wk) * cs) * (sk * sl)
-                c1 = c1 + ((coup * t1[l]) * wk) / wl
+                wl = f32(inv[ci[l]]) + f32(inv[cj[l]])
+                coup = ((ia / wk) * cs) * (sk * f32(sl))
+                tl = f32(t1[l])
+                c1 = c1 + ((coup * tl) * wk) / wl
                 c2 = c2 + coup * coup
                 cmax = max(cmax, abs(cs))
-                ct = ct + t1[l]
+                ct = ct + tl
         f[k, 8:] = [c1, c2, cmax, ct]
     return f, scale, t1
 

@@ -238,6 +238,48 @@ def test_integrator_bit_exact(load_fixture):
     assert np.array_equal(vg.view(np.uint64), vr.view(np.uint64))
 
 
+def test_integrator_bit_exact_mixed_cluster_sizes():
+    """SHAKE/RATTLE with single-constraint clusters (one thread each),
+    H-star clusters and a 12-bond chain (one warp each) and a 40-bond chain
+    (more than 32 constraints: one thread, global memory) in the same system:
+    every cluster returns the oracle's exact bits, for 5 steps."""
+    atoms, topo, state, _ = synth.generate(400, seed=17, h_fraction=0.3, relax_iters=200)
+    t = amber.promote_hydrogen_bonds(topo, atoms)
+    # constrain two runs of consecutive chain bonds as well
+    heavy = np.flatnonzero(atoms.element != 0)
+    chain = [(int(a), int(b)) for a, b in zip(t.bond_i, t.bond_j)]
+    runs = set(range(5, 17)) | set(range(40, 80))
+    sel = [chain[k] for k in sorted(runs)]
+    keep = [k for k in range(len(t.bond_i)) if k not in runs]
+    ci = np.concatenate([t.constr_i, np.array([a for a, b in sel], np.uint32)])
+    cj = np.concatenate([t.constr_j, np.array([b for a, b in sel], np.uint32)])
+    d = state.pos[:, ci] - state.pos[:, cj]
+    t.constr_i, t.constr_j, t.constr_dsq = ci, cj, (d * d).sum(0)
+    t.bond_i, t.bond_j, t.bond_k, t.bond_r0 = t.bond_i[keep], t.bond_j[keep], t.bond_k[keep], t.bond_r0[keep]
+    assert len(heavy) > 80
+    # Jacobi converges slowly on the long chain: tolerance 1e-8 within 2000
+    # iterations (the oracle needs ~130-195; at 1e-10 / 200 both stop with
+    # the same ConvergenceError)
+    p = backend.SimParams(box_size=(1000.0,) * 3, periodic=False, constr_tol=1e-8, max_constr_iter=2000)
+    be = backend.CudaBackend(atoms, t, p)
+    rng = np.random.default_rng(1)
+    pg, pr = np.ascontiguousarray(state.pos.copy()), np.ascontiguousarray(state.pos.copy())
+    vg = np.ascontiguousarray(rng.normal(0, 2.0, (3, atoms.n)))
+    vr = vg.copy()
+    force = np.ascontiguousarray(rng.normal(0, 20.0, (3, atoms.n)))
+    for step in range(5):
+        be.half_kick(vg, force, 0.001)
+        oracle.half_kick(vr, force, atoms.mass, 0.001)
+        be.geodesic_drift(pg, vg, 0.002, step=step)
+        oracle.drift_and_constrain(pr, vr, t, atoms, 0.002, 2000, 1e-8, step)
+        assert np.array_equal(pg.view(np.uint64), pr.view(np.uint64)), step
+        be.half_kick(vg, force, 0.001)
+        oracle.half_kick(vr, force, atoms.mass, 0.001)
+        be.constrain_velocities(pg, vg, step=step)
+        oracle.constrain_velocities(t, atoms, pr, vr, 2000, 1e-8, step)
+        assert np.array_equal(vg.view(np.uint64), vr.view(np.uint64)), step
+
+
 def test_constraint_failure_reports_reference_error():
     """constraint_solver.rs:98-120: max_iter = 1 gives ConvergenceError with
     the step and the worst constraint's atoms."""
