@@ -86,7 +86,7 @@ struct gm_ctx {
     int n14 = 0, blocks14 = 0;
     int *d_p14i = nullptr, *d_p14j = nullptr;
     // constraints
-    int n_constr = 0, n_clusters = 0, n_single = 0, n_warp_end = 0;
+    int n_constr = 0, n_clusters = 0, n_single = 0, n_star_end = 0, n_warp_end = 0;
     int *d_ci = nullptr, *d_cj = nullptr, *d_cl_cstart = nullptr, *d_cl_cons = nullptr, *d_cl_astart = nullptr,
         *d_cl_atoms = nullptr, *d_cl_acstart = nullptr, *d_cl_acons = nullptr, *d_cl_iters = nullptr,
         *d_cl_worst_idx = nullptr;
@@ -297,6 +297,7 @@ ClusterArgs cluster_args(gm_ctx *c) {
     ClusterArgs a{};
     a.n_clusters = c->n_clusters;
     a.n_single = c->n_single;
+    a.n_star_end = c->n_star_end;
     a.n_warp_end = c->n_warp_end;
     a.cl_cstart = c->d_cl_cstart; a.cl_cons = c->d_cl_cons;
     a.cl_astart = c->d_cl_astart; a.cl_atoms = c->d_cl_atoms;
@@ -690,10 +691,11 @@ void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int
         if (it == root_id.end()) { it = root_id.emplace(r, (int)ccons.size()).first; ccons.emplace_back(); catoms.emplace_back(); }
         ccons[(size_t)it->second].push_back(k);  // ascending k
     }
-    // clusters in three classes, in this order: one constraint on two atoms
-    // (one per thread), 2-32 constraints on at most 32 atoms with at most 8
-    // constraints per atom (one per warp), the rest; within a class by size
-    // (stable), so a warp's threads run loops of the same lengths.  The
+    // clusters in four classes, in this order: one constraint on two atoms
+    // (one per thread), stars of 2-8 constraints on one centre atom (one per
+    // thread), other clusters of 2-32 constraints on at most 32 atoms with at
+    // most 8 constraints per atom (one per warp), the rest; within a class by
+    // size (stable), so a warp's threads run loops of the same lengths.  The
     // solution does not depend on the cluster order.
     const size_t ncl = ccons.size();
     std::vector<int> cls(ncl);
@@ -708,7 +710,15 @@ void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int
         }
         at.erase(std::unique(at.begin(), at.end()), at.end());
         const int nc = (int)ccons[q].size(), na = (int)at.size();
-        cls[q] = (nc == 1 && na == 2) ? 0 : (nc <= 32 && na <= 32 && maxdeg <= 8 ? 1 : 2);
+        // a star: every constraint shares one centre atom, the others are distinct
+        bool star = nc >= 2 && nc <= 8 && na == nc + 1;
+        if (star) {
+            const int k0 = ccons[q][0], k1 = ccons[q][1];
+            const int cen = (ci[(size_t)k0] == ci[(size_t)k1] || ci[(size_t)k0] == cj[(size_t)k1]) ? ci[(size_t)k0]
+                                                                                                   : cj[(size_t)k0];
+            for (int k : ccons[q]) star = star && (ci[(size_t)k] == cen || cj[(size_t)k] == cen);
+        }
+        cls[q] = (nc == 1 && na == 2) ? 0 : star ? 1 : (nc <= 32 && na <= 32 && maxdeg <= 8 ? 2 : 3);
     }
     std::vector<size_t> order(ncl);
     std::iota(order.begin(), order.end(), (size_t)0);
@@ -717,7 +727,8 @@ void build_clusters(gm_ctx *c, const std::vector<int> &ci, const std::vector<int
         return ccons[x].size() < ccons[y].size();
     });
     c->n_single = (int)std::count(cls.begin(), cls.end(), 0);
-    c->n_warp_end = c->n_single + (int)std::count(cls.begin(), cls.end(), 1);
+    c->n_star_end = c->n_single + (int)std::count(cls.begin(), cls.end(), 1);
+    c->n_warp_end = c->n_star_end + (int)std::count(cls.begin(), cls.end(), 2);
     cstart.assign(1, 0);
     astart.assign(1, 0);
     acstart.assign(1, 0);
@@ -1089,8 +1100,8 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         // the kernels index these prefix tables without bounds checks
         if (cstart.empty() || cstart.front() != 0 || cstart.back() != c->n_constr || astart.size() != cstart.size() ||
             astart.front() != 0 || astart.back() != (int)cat.size() || acstart.size() != cat.size() + 1 ||
-            acstart.front() != 0 || acstart.back() != (int)acons.size() || c->n_single > c->n_warp_end ||
-            c->n_warp_end > c->n_clusters) {
+            acstart.front() != 0 || acstart.back() != (int)acons.size() || c->n_single > c->n_star_end ||
+            c->n_star_end > c->n_warp_end || c->n_warp_end > c->n_clusters) {
             fail(c, GM_ERR_DEVICE, "inconsistent constraint cluster tables");
             return bail(GM_ERR_DEVICE);
         }

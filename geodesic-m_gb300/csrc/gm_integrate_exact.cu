@@ -203,6 +203,183 @@ __global__ void shake_prepare(ClusterArgs c, const double *dref, int n_atoms) {
     if (c.lam_sum) c.lam_sum[k] = 0.0;
 }
 
+// A star cluster: NC constraints that all share one centre atom (a heavy
+// atom and its NC hydrogens), one cluster per thread with every value in a
+// register.  The operations are those of the general sweep in the same
+// order: each constraint's multiplier, then each atom's sum over its
+// constraints (the centre's in ascending constraint order, from 0.0).
+template <bool RATTLE, int NC>
+__device__ void cluster_star(const ClusterArgs &c, int cl, double *pos, double *vel, int n, bool phase2) {
+    const DevStatus *st = c.status;
+    unsigned T = 0;
+    if (!phase2) {
+        if (st->error) return;
+    } else {
+        T = RATTLE ? st->rattle_T : st->shake_T;
+        if ((st->error & ~(unsigned)(GM_DEV_SHAKE_FAIL | GM_DEV_RATTLE_FAIL)) != 0) return;
+        if ((unsigned)c.cl_iters[cl] >= T) return;
+    }
+    const int c0 = c.cl_cstart[cl];
+    int kk[NC], hq[NC];
+    bool cen_i[NC];  // the centre is the constraint's i (it subtracts)
+    {
+        const int k0 = c.cl_cons[c0], k1 = c.cl_cons[c0 + 1];
+        const int i0 = c.constr_i[k0], j0 = c.constr_j[k0];
+        const int cen_ = (i0 == c.constr_i[k1] || i0 == c.constr_j[k1]) ? i0 : j0;
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            const int k = c.cl_cons[c0 + q];
+            kk[q] = k;
+            const int i = c.constr_i[k];
+            cen_i[q] = i == cen_;
+            hq[q] = cen_i[q] ? c.constr_j[k] : i;
+        }
+        // centre
+        const int cen = cen_;
+        const double inv_c = c.inv_mass[cen];
+        double *v = RATTLE ? vel : pos;
+        double cx = v[cen], cy = v[n + cen], cz = v[2 * n + cen];
+        double hx[NC], hy[NC], hz[NC], inv_h[NC], rx[NC], ry[NC], rz[NC], wq[NC], dsq[NC], acc[NC];
+        const int ncst = c.n_constr;
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            const int h = hq[q];
+            hx[q] = v[h]; hy[q] = v[n + h]; hz[q] = v[2 * n + h];
+            inv_h[q] = c.inv_mass[h];
+            const int k = kk[q];
+            const double inv_mi = cen_i[q] ? inv_c : inv_h[q], inv_mj = cen_i[q] ? inv_h[q] : inv_c;
+            if (!RATTLE) {
+                dsq[q] = c.constr_dsq[k];
+                rx[q] = c.rvec[k]; ry[q] = c.rvec[ncst + k]; rz[q] = c.rvec[2 * ncst + k];
+                wq[q] = 2.0 * (inv_mi + inv_mj);
+            } else {
+                const int i = cen_i[q] ? cen : h, j = cen_i[q] ? h : cen;
+                rx[q] = pos[i] - pos[j];
+                ry[q] = pos[n + i] - pos[n + j];
+                rz[q] = pos[2 * n + i] - pos[2 * n + j];
+                const double rsq = rx[q] * rx[q] + ry[q] * ry[q] + rz[q] * rz[q];
+                wq[q] = (inv_mi + inv_mj) * rsq;
+                dsq[q] = 0.0;
+            }
+            acc[q] = 0.0;
+        }
+        const bool keep_sum = !RATTLE && c.lam_sum;
+        double lam[NC];
+        unsigned it;
+        double mx;
+        int worst;
+        bool apply_first = false;
+        if (!phase2) {
+            it = 0;
+            mx = 0.0;
+            worst = 0;
+            if (!RATTLE && c.lam0) {
+#pragma unroll
+                for (int q = 0; q < NC; q++) { acc[q] = c.lam0[kk[q]]; lam[q] = acc[q]; }
+                apply_first = true;
+            }
+        } else {
+            it = (unsigned)c.cl_iters[cl];
+            mx = c.cl_worst[cl];
+            worst = c.cl_worst_idx[cl];
+            if (keep_sum)
+#pragma unroll
+                for (int q = 0; q < NC; q++) acc[q] = c.lam_sum[kk[q]];
+        }
+        bool ok = false;
+        const unsigned stop = phase2 ? T : c.max_iter;
+        while (true) {
+            if (!apply_first) {
+                if (it >= stop) break;
+                double m_ = 0.0;
+                int w_ = kk[0];
+#pragma unroll
+                for (int q = 0; q < NC; q++) {
+                    // the constraint's i minus its j
+                    const double xi = cen_i[q] ? cx : hx[q], yi = cen_i[q] ? cy : hy[q], zi = cen_i[q] ? cz : hz[q];
+                    const double xj = cen_i[q] ? hx[q] : cx, yj = cen_i[q] ? hy[q] : cy, zj = cen_i[q] ? hz[q] : cz;
+                    double l_;
+                    if (RATTLE) {
+                        const double dvx = xi - xj;
+                        const double dvy = yi - yj;
+                        const double dvz = zi - zj;
+                        const double rel_vel = dvx * rx[q] + dvy * ry[q] + dvz * rz[q];
+                        l_ = wq[q] == 0.0 ? 0.0 : rel_vel / wq[q];
+                    } else {
+                        const double dx = xi - xj;
+                        const double dy = yi - yj;
+                        const double dz = zi - zj;
+                        const double diff = dx * dx + dy * dy + dz * dz - dsq[q];
+                        const double dot_new_old = dx * rx[q] + dy * ry[q] + dz * rz[q];
+                        const double denom = wq[q] * dot_new_old;
+                        l_ = denom == 0.0 ? 0.0 : diff / denom;
+                        if (keep_sum) acc[q] += l_;
+                    }
+                    lam[q] = l_;
+                    const double la = fabs(l_);
+                    if (la > m_) { m_ = la; w_ = kk[q]; }
+                }
+                mx = m_;
+                worst = w_;
+            }
+            // atoms: the centre over its constraints in ascending order, then each H
+            double ddx = 0.0, ddy = 0.0, ddz = 0.0;
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                const double w = lam[q] * inv_c;
+                const double tx = w * rx[q], ty = w * ry[q], tz = w * rz[q];
+                if (cen_i[q]) { ddx -= tx; ddy -= ty; ddz -= tz; }
+                else { ddx += tx; ddy += ty; ddz += tz; }
+            }
+            cx += ddx; cy += ddy; cz += ddz;
+#pragma unroll
+            for (int q = 0; q < NC; q++) {
+                const double w = lam[q] * inv_h[q];
+                const double tx = w * rx[q], ty = w * ry[q], tz = w * rz[q];
+                double ex = 0.0, ey = 0.0, ez = 0.0;
+                if (cen_i[q]) { ex += tx; ey += ty; ez += tz; }
+                else { ex -= tx; ey -= ty; ez -= tz; }
+                hx[q] += ex; hy[q] += ey; hz[q] += ez;
+            }
+            if (apply_first) { apply_first = false; continue; }
+            it++;
+            if (!phase2 && mx < c.tol) { ok = true; break; }
+        }
+        v[cen] = cx; v[n + cen] = cy; v[2 * n + cen] = cz;
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            const int h = hq[q];
+            v[h] = hx[q]; v[n + h] = hy[q]; v[2 * n + h] = hz[q];
+            if (keep_sum) c.lam_sum[kk[q]] = acc[q];
+        }
+        c.cl_iters[cl] = (int)it;
+        c.cl_worst[cl] = mx;
+        c.cl_worst_idx[cl] = worst;
+        if (!phase2) {
+            if (!ok) {
+                atomicOr(&c.status->error, RATTLE ? (unsigned)GM_DEV_RATTLE_FAIL : (unsigned)GM_DEV_SHAKE_FAIL);
+                atomicMin(&c.status->fail_step, c.status->step);
+            }
+            atomicMax(RATTLE ? &c.status->rattle_T : &c.status->shake_T, it);
+        } else if (!(mx < c.tol) && T < c.max_iter) {
+            atomicOr(&c.status->error, (unsigned)GM_DEV_ITER_MISMATCH);
+        }
+    }
+}
+
+template <bool RATTLE>
+__device__ void cluster_star_any(const ClusterArgs &c, int cl, double *pos, double *vel, int n, bool phase2) {
+    switch (c.cl_cstart[cl + 1] - c.cl_cstart[cl]) {
+        case 2: cluster_star<RATTLE, 2>(c, cl, pos, vel, n, phase2); break;
+        case 3: cluster_star<RATTLE, 3>(c, cl, pos, vel, n, phase2); break;
+        case 4: cluster_star<RATTLE, 4>(c, cl, pos, vel, n, phase2); break;
+        case 5: cluster_star<RATTLE, 5>(c, cl, pos, vel, n, phase2); break;
+        case 6: cluster_star<RATTLE, 6>(c, cl, pos, vel, n, phase2); break;
+        case 7: cluster_star<RATTLE, 7>(c, cl, pos, vel, n, phase2); break;
+        default: cluster_star<RATTLE, 8>(c, cl, pos, vel, n, phase2); break;
+    }
+}
+
 // Clusters of 2-32 constraints on at most 32 atoms (a heavy atom with its H
 // atoms): one warp per cluster.  Lane a keeps atom a's coordinates and its
 // constraint list in registers, lane q keeps constraint q's bond vector and
@@ -498,23 +675,63 @@ __device__ void cluster_single(const ClusterArgs &c, int cl, double *pos, double
 // update of a Jacobi sweep (per-atom deltas over the atom's constraints in
 // ascending order from 0.0, then added), before the unchanged iterations.
 // The multiplier totals start from lam0.
-// Clusters come in three ranges: [0, n_single) single constraints, one per
-// thread; [n_single, n_warp_end) 2-32 constraints, one per warp; the rest one
-// per thread through global memory.  Launched with 32-thread blocks.
-__device__ __forceinline__ int big_cluster(const ClusterArgs &c, int block) {
-    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
-    return c.n_warp_end + (block - b_single - b_warp) * 32 + (int)threadIdx.x;
+// Clusters come in four ranges, launched with 32-thread blocks:
+// [0, n_single) one constraint, one per thread; [n_single, n_star_end)
+// stars of 2-8 constraints, one per thread; [n_star_end, n_warp_end) other
+// clusters of 2-32 constraints, one per warp; the rest one per thread
+// through global memory.
+struct ClusterBlocks {
+    int single, star, warp, big;
+};
+
+__host__ __device__ __forceinline__ ClusterBlocks cluster_block_ranges(const ClusterArgs &c) {
+    ClusterBlocks b;
+    b.single = (c.n_single + 31) / 32;
+    b.star = (c.n_star_end - c.n_single + 31) / 32;
+    b.warp = c.n_warp_end - c.n_star_end;
+    b.big = (c.n_clusters - c.n_warp_end + 31) / 32;
+    return b;
 }
 
 int cluster_blocks(const ClusterArgs &c) {
-    return (c.n_single + 31) / 32 + (c.n_warp_end - c.n_single) + (c.n_clusters - c.n_warp_end + 31) / 32;
+    const ClusterBlocks b = cluster_block_ranges(c);
+    return b.single + b.star + b.warp + b.big;
+}
+
+// Runs the cluster of this thread (or warp) by its class; false for the
+// global-memory class, which the caller handles, with *cl set.
+template <bool RATTLE>
+__device__ __forceinline__ bool cluster_dispatch(const ClusterArgs &c, double *pos, double *vel, int n, bool phase2,
+                                                 int *cl) {
+    const ClusterBlocks b = cluster_block_ranges(c);
+    int blk = blockIdx.x;
+    if (blk < b.single) {
+        const int q = blk * 32 + threadIdx.x;
+        if (q < c.n_single) cluster_single<RATTLE>(c, q, pos, vel, n, phase2);
+        return true;
+    }
+    blk -= b.single;
+    if (blk < b.star) {
+        const int q = c.n_single + blk * 32 + threadIdx.x;
+        if (q < c.n_star_end) cluster_star_any<RATTLE>(c, q, pos, vel, n, phase2);
+        return true;
+    }
+    blk -= b.star;
+    if (blk < b.warp) {
+        cluster_warp<RATTLE>(c, c.n_star_end + blk, pos, vel, n, phase2);
+        return true;
+    }
+    blk -= b.warp;
+    *cl = c.n_warp_end + blk * 32 + threadIdx.x;
+    return false;
 }
 
 __global__ void warm_start_apply(ClusterArgs c, double *pos, int n_atoms) {
     // big clusters only: the other paths apply the warm start themselves
-    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
-    if ((int)blockIdx.x < b_single + b_warp) return;
-    const int cl = big_cluster(c, blockIdx.x);
+    const ClusterBlocks b = cluster_block_ranges(c);
+    const int blk = (int)blockIdx.x - b.single - b.star - b.warp;
+    if (blk < 0) return;
+    const int cl = c.n_warp_end + blk * 32 + threadIdx.x;
     if (cl >= c.n_clusters || c.status->error) return;
     const int nc = c.n_constr;
     if (c.lam_sum)
@@ -539,17 +756,8 @@ __global__ void warm_start_apply(ClusterArgs c, double *pos, int n_atoms) {
 
 template <bool RATTLE>
 __global__ void cluster_phase1(ClusterArgs c, double *pos, double *vel, int n_atoms) {
-    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
-    if ((int)blockIdx.x < b_single) {
-        const int cl = blockIdx.x * 32 + threadIdx.x;
-        if (cl < c.n_single) cluster_single<RATTLE>(c, cl, pos, vel, n_atoms, false);
-        return;
-    }
-    if ((int)blockIdx.x < b_single + b_warp) {
-        cluster_warp<RATTLE>(c, c.n_single + (blockIdx.x - b_single), pos, vel, n_atoms, false);
-        return;
-    }
-    const int cl = big_cluster(c, blockIdx.x);
+    int cl = 0;
+    if (cluster_dispatch<RATTLE>(c, pos, vel, n_atoms, false, &cl)) return;
     if (cl >= c.n_clusters) return;
     if (c.status->error) return;
     double mx = 0.0;
@@ -574,17 +782,8 @@ __global__ void cluster_phase1(ClusterArgs c, double *pos, double *vel, int n_at
 
 template <bool RATTLE>
 __global__ void cluster_phase2(ClusterArgs c, double *pos, double *vel, int n_atoms) {
-    const int b_single = (c.n_single + 31) / 32, b_warp = c.n_warp_end - c.n_single;
-    if ((int)blockIdx.x < b_single) {
-        const int cl = blockIdx.x * 32 + threadIdx.x;
-        if (cl < c.n_single) cluster_single<RATTLE>(c, cl, pos, vel, n_atoms, true);
-        return;
-    }
-    if ((int)blockIdx.x < b_single + b_warp) {
-        cluster_warp<RATTLE>(c, c.n_single + (blockIdx.x - b_single), pos, vel, n_atoms, true);
-        return;
-    }
-    const int cl = big_cluster(c, blockIdx.x);
+    int cl = 0;
+    if (cluster_dispatch<RATTLE>(c, pos, vel, n_atoms, true, &cl)) return;
     if (cl >= c.n_clusters) return;
     const unsigned T = RATTLE ? c.status->rattle_T : c.status->shake_T;
     if ((c.status->error & ~(unsigned)(GM_DEV_SHAKE_FAIL | GM_DEV_RATTLE_FAIL)) != 0) return;

@@ -206,7 +206,8 @@ int gm_bonded_blocks(int n_bonds, int n_angles, int n_diheds);
 struct ClusterArgs {
     int n_clusters;
     int n_single;                         // clusters [0, n_single): one constraint on two atoms
-    int n_warp_end;                       // clusters [n_single, n_warp_end): 2-32 constraints, <= 32 atoms
+    int n_star_end;                       // [n_single, n_star_end): 2-8 constraints sharing one centre atom
+    int n_warp_end;                       // [n_star_end, n_warp_end): other clusters, 2-32 constraints, <= 32 atoms
     const int *cl_cstart, *cl_cons;       // cluster -> constraints (ascending)
     const int *cl_astart, *cl_atoms;      // cluster -> atoms
     const int *cl_acstart, *cl_acons;     // cluster-atom slot -> signed constraint refs (ascending)
