@@ -32,6 +32,7 @@ struct DevBuf {
 struct gm_ctx {
     int device = 0;
     cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // bonded/1-4 branch beside the pair kernel
     gm_params p{};
     int n = 0;
     bool fp64 = false;
@@ -104,6 +105,7 @@ struct gm_ctx {
     // energy
     double *d_epart = nullptr, *d_energy = nullptr, *d_kin_part = nullptr, *d_ke = nullptr;
     int n_epart = 0;
+    bool energy_stale = false;  // epart holds the last forces' partials, d_energy not yet their sum
     // status
     DevStatus *d_status = nullptr;
     DevStatus *h_status = nullptr;  // pinned
@@ -363,16 +365,40 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
     return (all ? 1 : 0) + 12 + (a.periodic || a.n > 0 ? 1 : 0);
 }
 
-int seq_forces(gm_ctx *c, cudaStream_t s) {
+// Force evaluation at the resident positions.  With a branch stream the
+// bonded and 1-4 kernels run on it beside the pair kernel: every force and
+// per-system energy sum is an integer sum and every energy partial has its own
+// slot, so the order in which the branches add changes no bit.  Without
+// `energy` the partials stay unsummed (energy_stale) until refresh_energy.
+int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr) {
     ListArgs la = list_args(c);
     if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);
     gm_launch_pack(la, c->fp64, s);
     ForceArgs fa = force_args(c);
-    gm_launch_bonded(fa, c->fp64, s);
+    const bool fork = branch && (c->bonded_blocks || c->blocks14);
+    const cudaStream_t sb = fork ? branch : s;
+    if (fork) {
+        cudaEventRecord(c->ev_fork, s);
+        cudaStreamWaitEvent(branch, c->ev_fork, 0);
+    }
+    gm_launch_bonded(fa, c->fp64, sb);
+    gm_launch_pair14(fa, sb);
     gm_launch_pair(fa, c->fp64, s);
-    gm_launch_pair14(fa, s);
-    gm_launch_energy(fa, s);
-    return 1 + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + 1;
+    if (fork) {
+        cudaEventRecord(c->ev_join, branch);
+        cudaStreamWaitEvent(s, c->ev_join, 0);
+    }
+    if (energy) gm_launch_energy(fa, s);
+    c->energy_stale = !energy;
+    return 1 + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + (energy ? 1 : 0);
+}
+
+// Sum the energy partials of the last force evaluation into d_energy.
+void refresh_energy(gm_ctx *c) {
+    if (!c->energy_stale) return;
+    gm_launch_energy(force_args(c), c->stream);
+    c->launches++;
+    c->energy_stale = false;
 }
 
 int check_status(gm_ctx *c, gm_convergence *conv);
@@ -561,13 +587,17 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
     long long k = 0;
     const int n = c->n;
     const bool constrained = c->n_clusters > 0;
-    gm_launch_half_kick(n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
-    gm_launch_drift(n, c->d_pos, c->d_vel, c->d_dref, dt, !constrained, c->d_status, s); k++;
-    if (constrained) {
-        k += issue_shake(c, s, true);
-        gm_launch_resync(n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, s); k++;
-    }
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
+    if (!constrained) {
+        gm_launch_kick_drift_check(n, c->d_pos, c->d_vel, c->d_dref, c->d_force, c->d_inv_mass, dt / 2.0, dt, c->d_ref,
+                                   half_skin * half_skin, c->d_status, cond, c->d_atom_sys, c->d_sys_flag, s);
+        *count += 1;
+        return GM_OK;
+    }
+    gm_launch_half_kick(n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+    gm_launch_drift(n, c->d_pos, c->d_vel, c->d_dref, dt, false, c->d_status, s); k++;
+    k += issue_shake(c, s, true);
+    gm_launch_resync(n, c->d_pos, c->d_vel, c->d_dref, dt, c->d_status, s); k++;
     gm_launch_check(n, c->d_pos, c->d_ref, half_skin * half_skin, c->d_status, cond, gm_check_blocks(n), c->d_atom_sys,
                     c->d_sys_flag, s);
     k++;
@@ -576,9 +606,14 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
 }
 
 int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
-    long long k = seq_forces(c, s);
+    long long k = seq_forces(c, s, false, c->side);
+    if (!c->n_clusters) {
+        gm_launch_kick_step(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+        *count += k;
+        return GM_OK;
+    }
     gm_launch_half_kick(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
-    if (c->n_clusters) { gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, s); k += 3; }
+    gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, s); k += 3;
     gm_launch_step(c->d_status, s); k++;
     *count += k;
     return GM_OK;
@@ -954,6 +989,9 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     if (cudaSetDevice(c->device) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        return bail(GM_ERR_DEVICE);
     int rc;
 #define TRY(x) do { rc = (x); if (rc) return bail(rc); } while (0)
     // ---- atoms: deduplicate (sigma, epsilon) into types, per system (the
@@ -1259,6 +1297,8 @@ int32_t gm_destroy(gm_ctx *c) {
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return GM_OK;
 }
@@ -1629,7 +1669,10 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
         c->launches++;
         rc2 = download3(c, c->d_fout, fx, fy, fz);
     }
-    if (!rc2 && energy) GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (!rc2 && energy) {
+        refresh_energy(c);
+        GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     return rc ? rc : rc2;
 }
@@ -1838,6 +1881,8 @@ int32_t gm_ensemble_energies(gm_ctx *c, double *e_pot, double *e_kin) {
     if (e_pot) {
         if (!c->forces_current) return fail(c, GM_ERR_NOT_BUILT, "no forces evaluated at the current positions");
         if (c->n_sys == 1) {
+            refresh_energy(c);
+            GM_CUDA(c, cudaStreamSynchronize(c->stream));
             GM_CUDA(c, cudaMemcpy(e_pot, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost));
         } else {
             std::vector<long long> q((size_t)c->n_sys);

@@ -854,6 +854,71 @@ __global__ void forces_out_kernel(int n3, const long long *force, double *out) {
 
 }  // namespace
 
+// half_kick_kernel, drift_kernel (resync) and check_kernel fused for systems
+// without constraints: one atom per thread, the same operations in the same
+// order.  A block that finds a non-finite position marks bad_pending instead of
+// error, and the last block moves it to error, so every block of the launch
+// reads the error word as it stood before the launch (as the separate kick and
+// drift kernels do).
+__global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double *dref, const long long *force,
+                                        const double *inv_mass, double dt_half, double dt, const double *ref,
+                                        double thr_sq, DevStatus *st, unsigned long long cond, const int *atom_sys,
+                                        unsigned int *sys_flag) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int need = 0, bad = 0;
+    if (i < n) {
+        double np[3];
+        if (!st->error) {
+            const double inv_m = inv_mass[i];
+            for (int d = 0; d < 3; d++) {
+                const double f = (double)force[d * n + i] * GM_FIX_INV;
+                const double v = vel[d * n + i] + dt_half * f * inv_m * kForceToAccel;
+                const double p = pos[d * n + i];
+                dref[d * n + i] = p;
+                np[d] = p + dt * v;
+                pos[d * n + i] = np[d];
+                vel[d * n + i] = (np[d] - p) / dt;
+            }
+        } else {
+            for (int d = 0; d < 3; d++) np[d] = pos[d * n + i];
+        }
+        bad = !(isfinite(np[0]) && isfinite(np[1]) && isfinite(np[2]));
+        const double dx = np[0] - ref[i], dy = np[1] - ref[n + i], dz = np[2] - ref[2 * n + i];
+        need = dx * dx + dy * dy + dz * dz > thr_sq;
+        if (need) sys_flag[atom_sys[i]] = 1u;
+    }
+    need = __syncthreads_or(need);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        if (need) atomicOr(&st->rebuild, 1u);
+        if (bad) atomicOr(&st->bad_pending, 1u);
+        __threadfence();
+        const unsigned done = atomicAdd(&st->blocks_done, 1u);
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            const unsigned r = atomicOr(&st->rebuild, 0u);
+            st->blocks_done = 0;
+            if (atomicExch(&st->bad_pending, 0u)) atomicOr(&st->error, (unsigned)GM_DEV_NONFINITE_POS);
+            const unsigned e = atomicOr(&st->error, 0u);
+            if (cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (r && !e) ? 1u : 0u);
+        }
+    }
+}
+// half_kick_kernel + step_kernel for systems without constraints (the step
+// counter is the only work step_kernel does for them)
+__global__ void kick_step_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                                 DevStatus *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool err = st->error != 0;
+    if (i < n && !err) {
+        const double inv_m = inv_mass[i];
+        for (int d = 0; d < 3; d++) {
+            const double f = (double)force[d * n + i] * GM_FIX_INV;
+            vel[d * n + i] += dt_half * f * inv_m * kForceToAccel;
+        }
+    }
+    if (i == 0 && !err) st->step += 1;
+}
 int gm_check_blocks(int n) { return n > 0 ? (n + 255) / 256 : 1; }
 
 void gm_launch_half_kick(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
@@ -877,6 +942,17 @@ void gm_launch_resync(int n, const double *pos, double *vel, const double *dref,
 }
 
 void gm_launch_step(DevStatus *st, cudaStream_t s) { step_kernel<<<1, 1, 0, s>>>(st); }
+void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, const long long *force,
+                                const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
+                                DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
+                                cudaStream_t s) {
+    kick_drift_check_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, pos, vel, dref, force, inv_mass, dt_half, dt, ref,
+                                                              thr_sq, st, cond, atom_sys, sys_flag);
+}
+void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                         DevStatus *st, cudaStream_t s) {
+    kick_step_kernel<<<n > 0 ? (n + 255) / 256 : 1, 256, 0, s>>>(n, vel, force, inv_mass, dt_half, st);
+}
 
 void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
                      unsigned long long cond, int blocks, const int *atom_sys, unsigned int *sys_flag, cudaStream_t s) {

@@ -58,6 +58,8 @@ struct DevStatus {
     unsigned long long shake_sum;  // sum of their SHAKE iteration counts
     unsigned long long rattle_sum; // sum of their RATTLE iteration counts
     unsigned int rec_n;            // warm-start samples recorded (in solves)
+    unsigned int bad_pending;      // non-finite positions seen by the fused step kernel, moved to
+                                   // error by its last block
 };
 
 struct GridInfo {
@@ -246,6 +248,15 @@ void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dr
 int gm_launch_shake_solve(const ClusterArgs &c, int n_atoms, double *pos, cudaStream_t s);
 void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s);
 void gm_launch_step(DevStatus *st, cudaStream_t s);
+// Unconstrained step: half-kick + drift (with the velocity resync) + rebuild
+// check in one launch, and half-kick + step counter in one launch.  Each atom
+// gets the same operations in the same order as the separate kernels.
+void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, const long long *force,
+                                const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
+                                DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
+                                cudaStream_t s);
+void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                         DevStatus *st, cudaStream_t s);
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,
                        cudaStream_t s);
 void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s);
