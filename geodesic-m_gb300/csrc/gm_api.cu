@@ -70,10 +70,10 @@ struct gm_ctx {
     double *d_bbox = nullptr;
     int bbox_blocks = 0;
     // list
-    int cap = 0, n_groups = 0;
+    int cap = 0, cap_seg = 0, n_groups = 0;  // list entries per atom; staging entries per atom and z layer
     int split = 1;                   // warps per group in the FP32 pair kernel
     int pair_warps = 4, pair_grid = 0;  // FP32 pair kernel block size and grid (0: one item per warp)
-    int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr;
+    int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr, *d_stage = nullptr;
     bool built = false;
     // exclusions
     int *d_excl_start = nullptr, *d_excl = nullptr;
@@ -191,6 +191,8 @@ ListArgs list_args(gm_ctx *c) {
     a.n_slots = c->n_slots;
     a.n_sys = c->n_sys;
     a.cap = c->cap;
+    a.cap_seg = c->cap_seg;
+    a.stage = c->d_stage;
     a.pos = c->d_pos;
     a.hi = c->d_hi;
     a.lo = c->d_lo;
@@ -501,21 +503,36 @@ int check_status(gm_ctx *c, gm_convergence *conv) {
     return fail(c, GM_ERR_DEVICE, "device status 0x%x", e);
 }
 
-int ensure_list_buffers(gm_ctx *c, int cap) {
-    if (cap == c->cap && c->d_list) return GM_OK;
-    dfree(c, c->d_list);
-    c->d_list = nullptr;
-    c->cap = cap;
-    size_t entries = (size_t)c->n_groups * 32 * (size_t)cap;
-    int rc = dalloc(c, &c->d_list, entries);
-    if (rc) return rc;
+// The list (cap entries per atom) and the list build's staging area (GM_NSEG
+// z layers of cap_seg entries per atom).
+int ensure_list_buffers(gm_ctx *c, int cap, int cap_seg) {
+    if (cap == c->cap && cap_seg == c->cap_seg && c->d_list && c->d_stage) return GM_OK;
+    if (cap != c->cap || !c->d_list) {
+        dfree(c, c->d_list);
+        c->d_list = nullptr;
+        c->cap = cap;
+        int rc = dalloc(c, &c->d_list, (size_t)c->n_groups * 32 * (size_t)cap);
+        if (rc) return rc;
+    }
+    if (cap_seg != c->cap_seg || !c->d_stage) {
+        dfree(c, c->d_stage);
+        c->d_stage = nullptr;
+        c->cap_seg = cap_seg;
+        int rc = dalloc(c, &c->d_stage, (size_t)c->n_groups * GM_NSEG * 32 * (size_t)cap_seg);
+        if (rc) return rc;
+    }
     // captured graphs hold the old pointer
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
     return GM_OK;
 }
 
-int estimate_cap(gm_ctx *c, const double *px, const double *py, const double *pz) {
+int round32(double x) { return std::max(((int)std::ceil(x) + 31) / 32 * 32, 32); }
+
+// List capacity from the densest system's mean density, and the staging
+// capacity of one z layer: a layer of cells about half the list radius thick
+// through the middle of the sphere holds ~37 % of it.
+int ensure_estimated_buffers(gm_ctx *c, const double *px, const double *py, const double *pz) {
     // densest system: its atoms over its bounding box (or the periodic box)
     double est = 32.0;
     const double rl = c->p.r_skin;
@@ -536,25 +553,42 @@ int estimate_cap(gm_ctx *c, const double *px, const double *py, const double *pz
         e = std::min(e, (double)(a1 - a0) + 32.0);
         est = std::max(est, e);
     }
-    int cap = ((int)std::ceil(est) + 31) / 32 * 32;
-    return std::max(cap, 32);
+    return ensure_list_buffers(c, round32(est), round32(0.45 * (est - 48.0) + 48.0));
 }
 
 int do_build(gm_ctx *c, bool all = true) {
     // list build on the resident positions (every system, or the flagged
     // ones), growing the capacity on overflow (then rebuilding every system)
+    unsigned long long r0 = 0, counted = 0;
     for (int attempt = 0; attempt < 6; attempt++) {
         int rc = reset_status(c);
         if (rc) return rc;
+        if (attempt == 0) r0 = c->h_status->n_rebuilds;
         c->launches += seq_rebuild(c, c->stream, all || attempt > 0);
         rc = check_status(c, nullptr);
-        if (rc == GM_ERR_LIST_OVERFLOW) {
-            int newcap = ((int)(c->cap * 1.5) + 31) / 32 * 32;
-            rc = ensure_list_buffers(c, newcap);
+        if (attempt == 0) counted = c->h_status->n_rebuilds - r0;
+        // the build records the longest list and staged layer it met: on an
+        // overflow, or (when every system was built) within 20 % of a
+        // capacity, since a resident run cannot grow the list, grow that
+        // capacity to a third above the need
+        const int need = (int)c->h_status->max_count, need_l = (int)c->h_status->max_layer;
+        const bool over = rc == GM_ERR_LIST_OVERFLOW;
+        const bool room = !rc && (all || attempt > 0);
+        const bool grow = need > (over ? c->cap : c->cap - c->cap / 5);
+        const bool grow_l = need_l > (over ? c->cap_seg : c->cap_seg - c->cap_seg / 5);
+        if ((over || room) && (grow || grow_l)) {
+            rc = ensure_list_buffers(c, grow ? round32(std::max(need + need / 3 + 32, c->cap + 32)) : c->cap,
+                                     grow_l ? round32(std::max(need_l + need_l / 3 + 32, c->cap_seg + 32)) : c->cap_seg);
             if (rc) return rc;
             continue;
         }
         if (rc) return rc;
+        if (attempt > 0) {
+            // capacity rebuilds are not list rebuilds: count the first attempt's
+            c->h_status->n_rebuilds = r0 + counted;
+            rc = st_write(c);
+            if (rc) return rc;
+        }
         c->built = true;
         c->forces_current = false;
         return GM_OK;
@@ -1317,7 +1351,7 @@ int32_t gm_build_list(gm_ctx *c, double *px, double *py, double *pz) {
     GM_CUDA(c, cudaSetDevice(c->device));
     if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position passed to build_neighbor_list");
     if (!c->d_list) {
-        int rc = ensure_list_buffers(c, estimate_cap(c, px, py, pz));
+        int rc = ensure_estimated_buffers(c, px, py, pz);
         if (rc) return rc;
     }
     int rc = upload3(c, c->d_pos, px, py, pz);
@@ -1488,7 +1522,7 @@ int32_t gm_upload_state(gm_ctx *c, const double *px, const double *py, const dou
     GM_CUDA(c, cudaSetDevice(c->device));
     if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position");
     if (!c->d_list) {
-        int rc = ensure_list_buffers(c, estimate_cap(c, px, py, pz));
+        int rc = ensure_estimated_buffers(c, px, py, pz);
         if (rc) return rc;
     }
     int rc;

@@ -30,6 +30,12 @@
 #define GM_MAX_TYPES 64
 #define GM_WARP 32
 #define GM_MAX_SPLIT 16      // largest number of warps per 32-atom group
+// The list build runs GM_NSEG warps per 32-atom group, one per z layer of the
+// 5 x 5 x (span + 4) cell box the group's candidates come from (cells are at
+// least half the list radius wide).  Each warp fills its own staging segment;
+// the block then concatenates the segments, layer by layer, into each lane's
+// list column.
+#define GM_NSEG 5
 
 // Device status bits (DevStatus::error).
 enum : unsigned int {
@@ -60,6 +66,8 @@ struct DevStatus {
     unsigned int rec_n;            // warm-start samples recorded (in solves)
     unsigned int bad_pending;      // non-finite positions seen by the fused step kernel, moved to
                                    // error by its last block
+    unsigned int max_count;        // largest list length the list build met (sizes a regrowth)
+    unsigned int max_layer;        // largest staging (one z layer) length it met
 };
 
 struct GridInfo {
@@ -118,6 +126,7 @@ struct ListArgs {
     int n_slots;             // sorted slots: each system's atoms padded to a multiple of 32
     int n_sys;               // systems in the context
     int cap;                 // list entries per atom
+    int cap_seg;             // staging entries per atom and z layer
     const double *pos;       // FP64 x|y|z rows of n atoms, caller order
     float4 *hi, *lo;         // per slot
     double4 *pos64s;         // per slot FP64 copy (FP64 mode) or nullptr
@@ -132,6 +141,7 @@ struct ListArgs {
     const double *charge64;  // caller order (FP64 mode)
     const int *excl_start, *excl;   // caller-order CSR (both directions, sorted)
     int *list, *count, *gmax;
+    int *stage;              // [group][layer][entry][lane], cap_seg entries per layer
     double *ref;             // FP64 x|y|z copy at each system's build
     long long *force;        // zeroed with the pack
     GridInfo *grid;          // one per system

@@ -11,8 +11,10 @@
 // range of sorted slots (padding slots have perm = -1 and no list), a range
 // of cells and its own grid; perm and the list entries hold global indices.
 // The list build gives each warp 32 consecutive cell-sorted atoms of one
-// system; the warp streams the candidates of each cell row its atoms occupy
-// through shared memory and each lane tests them against its own atom.  The
+// system and one z layer of their candidate cell box (five warps per group,
+// each filling its own list segment); the warp streams the candidates of
+// each cell row of its layer through shared memory and each lane tests them
+// against its own atom.  The
 // test runs in FP32 on hi+lo coordinates; candidates within `margin` of the
 // list radius are re-decided with the reference's exact FP64 expression
 // (min-image, then dx*dx + dy*dy + dz*dz, no fused multiply-add), so the pair
@@ -25,7 +27,6 @@
 
 namespace {
 
-constexpr int kBuildWarps = 4;
 
 __device__ __forceinline__ double exact_min_image(double d, double L) {
     // neighbor.rs:74-76: d - L * round(d / L), no contraction
@@ -397,16 +398,25 @@ __device__ __forceinline__ Range dim_range(int mn, int mx, int nc, int periodic,
 
 __device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c >= nc ? c - nc : c); }
 
-__global__ void __launch_bounds__(kBuildWarps * 32)
+// One block per group, one warp per z layer: warp `seg` tests the candidates
+// of z layer `seg` of each row box its lanes need and stages them; the block
+// then concatenates the layers into each lane's list column.
+__global__ void __launch_bounds__(GM_NSEG * 32)
 build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
-    __shared__ float4 s_hi[kBuildWarps][32];
-    __shared__ float4 s_lo[kBuildWarps][32];
-    __shared__ int s_orig[kBuildWarps][32];
+    __shared__ float4 s_hi[GM_NSEG][32];
+    __shared__ float4 s_lo[GM_NSEG][32];
+    __shared__ int s_orig[GM_NSEG][32];
+    __shared__ int s_cnt[GM_NSEG][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int group = blockIdx.x * kBuildWarps + wib;
+    const int group = blockIdx.x, seg = wib;
+    const int gseg = group * GM_NSEG + seg;
     if (group * 32 >= a.n_slots) return;
     const int sys = a.group_sys[group];
-    if (!a.sys_flag[sys]) return;  // warp-uniform: the system keeps its list
+    if (!a.sys_flag[sys]) return;  // block-uniform: the system keeps its list
+    // the unrolled candidate loop below reads all 32 staging entries
+    s_hi[wib][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s_lo[wib][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s_orig[wib][lane] = 0;
     const int soff = a.sys_slot_off[sys], coff = a.sys_cell_off[sys];
     const int ns = a.sys_atom_off[sys + 1] - a.sys_atom_off[sys];
     const int s = group * 32 + lane;
@@ -435,10 +445,12 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     // straddles the end of a row.  Sweeping each row's own 5 x 5 x (span + 4)
     // box keeps the regions tight (one box over both rows would cover the
     // whole row); a lane tests only the candidates of its own row's box, so
-    // it never meets a candidate twice.
+    // it never meets a candidate twice.  This warp takes z layer `seg` of
+    // each box.
     const int cx = my_cell % g.nc[0], cy = (my_cell / g.nc[0]) % g.nc[1], cz = my_cell / (g.nc[0] * g.nc[1]);
     const int row_id = valid ? cz * g.nc[1] + cy : -1;
-    int *my_list = a.list + (size_t)group * 32 * cap + lane;
+    const int cap_seg = a.cap_seg;
+    int *my_stage = a.stage + (size_t)gseg * 32 * cap_seg + lane;
     int cnt = 0;
     const double bx[3] = {a.box[0], a.box[1], a.box[2]};
     unsigned remaining = __ballot_sync(0xffffffffu, valid);
@@ -453,34 +465,40 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
         Range rx = dim_range(xmin, xmax, g.nc[0], g.periodic, g.full[0]);
         Range ry = dim_range(yR, yR, g.nc[1], g.periodic, g.full[1]);
         Range rz = dim_range(zR, zR, g.nc[2], g.periodic, g.full[2]);
-        for (int zz = rz.lo; zz <= rz.hi; zz++) {
-            const int z = rz.wrap ? wrapi(zz, g.nc[2]) : zz;
-            for (int yy = ry.lo; yy <= ry.hi; yy++) {
-                const int y = ry.wrap ? wrapi(yy, g.nc[1]) : yy;
-                // the x extent as one or two runs of consecutive cells
-                int seg_lo[2], seg_hi[2], nseg;
-                if (!rx.wrap) { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
-                else if (rx.lo < 0) { seg_lo[0] = rx.lo + g.nc[0]; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi; nseg = 2; }
-                else if (rx.hi >= g.nc[0]) { seg_lo[0] = rx.lo; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi - g.nc[0]; nseg = 2; }
-                else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nseg = 1; }
-                for (int sg = 0; sg < nseg; sg++) {
-                    const int row = (z * g.nc[1] + y) * g.nc[0];
-                    // the system's slots, made global
-                    const int b0 = soff + cell_start[row + seg_lo[sg]], b1 = soff + cell_start[row + seg_hi[sg] + 1];
-                    for (int base = b0; base < b1; base += 32) {
-                        const int t = base + lane;
-                        __syncwarp();
-                        if (t < b1) {
-                            s_hi[wib][lane] = a.hi[t];
-                            s_lo[wib][lane] = a.lo[t];
-                            s_orig[wib][lane] = a.perm[t];
-                        }
-                        __syncwarp();
-                        if (!mine) continue;
-                        const int m = min(32, b1 - base);
-                        for (int k = 0; k < m; k++) {
-                            const int j = base + k;
-                            if (j == s) continue;
+        const int zz = rz.lo + seg;
+        if (zz > rz.hi) continue;  // warp-uniform
+        const int z = rz.wrap ? wrapi(zz, g.nc[2]) : zz;
+        for (int yy = ry.lo; yy <= ry.hi; yy++) {
+            const int y = ry.wrap ? wrapi(yy, g.nc[1]) : yy;
+            // the x extent as one or two runs of consecutive cells
+            int seg_lo[2], seg_hi[2], nrun;
+            if (!rx.wrap) { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nrun = 1; }
+            else if (rx.lo < 0) { seg_lo[0] = rx.lo + g.nc[0]; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi; nrun = 2; }
+            else if (rx.hi >= g.nc[0]) { seg_lo[0] = rx.lo; seg_hi[0] = g.nc[0] - 1; seg_lo[1] = 0; seg_hi[1] = rx.hi - g.nc[0]; nrun = 2; }
+            else { seg_lo[0] = rx.lo; seg_hi[0] = rx.hi; nrun = 1; }
+            for (int sg = 0; sg < nrun; sg++) {
+                const int row = (z * g.nc[1] + y) * g.nc[0];
+                // the system's slots, made global
+                const int b0 = soff + cell_start[row + seg_lo[sg]], b1 = soff + cell_start[row + seg_hi[sg] + 1];
+                for (int base = b0; base < b1; base += 32) {
+                    const int t = base + lane;
+                    __syncwarp();
+                    if (t < b1) {
+                        s_hi[wib][lane] = a.hi[t];
+                        s_lo[wib][lane] = a.lo[t];
+                        s_orig[wib][lane] = a.perm[t];
+                    }
+                    __syncwarp();
+                    if (!mine) continue;
+                    const int m = min(32, b1 - base);
+                    // four candidates at a time: the distance tests are
+                    // independent, the rare accepted ones are handled in order
+                    for (int k0 = 0; k0 < m; k0 += 4) {
+                        float r2v[4];
+                        unsigned hit = 0;
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const int k = k0 + u;
                             const float4 ch = s_hi[wib][k], cl = s_lo[wib][k];
                             float dx = (ch.x - mh.x) + (cl.x - ml.x);
                             float dy = (ch.y - mh.y) + (cl.y - ml.y);
@@ -490,10 +508,17 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                                 dy -= g.box[1] * rintf(dy * g.inv_box[1]);
                                 dz -= g.box[2] * rintf(dz * g.inv_box[2]);
                             }
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 > rl2_hi) continue;
+                            r2v[u] = dx * dx + dy * dy + dz * dz;
+                            if (k < m && base + k != s && r2v[u] <= rl2_hi) hit |= 1u << u;
+                        }
+                        if (!hit) continue;
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            if (!((hit >> u) & 1u)) continue;
+                            const int k = k0 + u;
+                            const int j = base + k;
                             const int jo = s_orig[wib][k];
-                            bool in = r2 <= rl2_lo;
+                            bool in = r2v[u] <= rl2_lo;
                             if (!in) {
                                 // the reference's own FP64 decision
                                 double ex_ = exact_min_image(__dsub_rn(a.pos[jo], a.pos[my_orig]), bx[0]);
@@ -509,7 +534,7 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                             if (ne > 8)
                                 for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
                             if (excluded) continue;
-                            if (cnt < cap) my_list[(size_t)cnt * 32] = j;
+                            if (cnt < cap_seg) my_stage[(size_t)cnt * 32] = j;
                             cnt++;
                         }
                     }
@@ -517,13 +542,42 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
             }
         }
     }
-    if (valid) {
-        a.count[s] = cnt < cap ? cnt : cap;
-        if (cnt > cap) atomicOr(&a.status->error, (unsigned)GM_DEV_LIST_OVERFLOW);
+    // concatenate the layers: lane l's layer k goes after its layers < k
+    int lmax = cnt;
+    for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if (lane == 0) atomicMax(&a.status->max_layer, (unsigned)lmax);
+    const int staged = cnt < cap_seg ? cnt : cap_seg;
+    s_cnt[seg][lane] = staged;
+    __syncthreads();
+    int off = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < GM_NSEG; k++) {
+        const int ck = s_cnt[k][lane];
+        off += k < seg ? ck : 0;
+        total += ck;
     }
-    int c = valid ? (cnt < cap ? cnt : cap) : 0;
-    for (int o = 16; o > 0; o >>= 1) c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
-    if (lane == 0) a.gmax[group] = c;
+    int smax = staged;
+    for (int o = 16; o > 0; o >>= 1) smax = max(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    int *my_list = a.list + (size_t)group * 32 * cap + lane;
+    for (int e = 0; e < smax; e++) {
+        if (e < staged && off + e < cap) my_list[(size_t)(off + e) * 32] = my_stage[(size_t)e * 32];
+    }
+    if (seg == 0) {
+        if (valid) a.count[s] = total < cap ? total : cap;
+        if (valid && (cnt > cap_seg || total > cap)) atomicOr(&a.status->error, (unsigned)GM_DEV_LIST_OVERFLOW);
+        int c = valid ? (total < cap ? total : cap) : 0;
+        int tm = valid ? total : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            c = max(c, __shfl_xor_sync(0xffffffffu, c, o));
+            tm = max(tm, __shfl_xor_sync(0xffffffffu, tm, o));
+        }
+        if (lane == 0) {
+            a.gmax[group] = c;
+            atomicMax(&a.status->max_count, (unsigned)tm);
+        }
+    } else if (valid && cnt > cap_seg) {
+        atomicOr(&a.status->error, (unsigned)GM_DEV_LIST_OVERFLOW);
+    }
 }
 
 // Per-system launch shape: x covers the largest system, y the systems.
@@ -572,6 +626,6 @@ void gm_launch_build(const ListArgs &a, cudaStream_t s) {
     const int groups = a.n_slots / 32;
     const double rl2 = a.r_list * a.r_list;  // neighbor.rs:25
     const double margin = 1e-3 * (rl2 > 144.0 ? rl2 / 144.0 : 1.0);
-    build_kernel<<<(groups + kBuildWarps - 1) / kBuildWarps, kBuildWarps * 32, 0, s>>>(
+    build_kernel<<<groups, GM_NSEG * 32, 0, s>>>(
         a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
 }
