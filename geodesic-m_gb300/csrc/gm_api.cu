@@ -52,7 +52,7 @@ struct gm_ctx {
            *d_host_f = nullptr;
     long long *d_force = nullptr;
     // sorted / cells
-    float4 *d_hi = nullptr, *d_lo = nullptr;
+    float4 *d_coord = nullptr;  // two float4 per slot (hi, lo)
     double4 *d_pos64s = nullptr;
     int *d_type_sorted = nullptr;
     int *d_perm = nullptr, *d_cell_of = nullptr, *d_cell_sorted = nullptr, *d_cell_count = nullptr,
@@ -194,8 +194,7 @@ ListArgs list_args(gm_ctx *c) {
     a.cap_seg = c->cap_seg;
     a.stage = c->d_stage;
     a.pos = c->d_pos;
-    a.hi = c->d_hi;
-    a.lo = c->d_lo;
+    a.coord = c->d_coord;
     a.pos64s = c->d_pos64s;
     a.type_sorted = c->d_type_sorted;
     a.perm = c->d_perm;
@@ -246,8 +245,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.split = c->fp64 ? 1 : c->split;
     a.pair_warps = c->pair_warps;
     a.pair_grid = c->pair_grid;
-    a.hi = c->d_hi;
-    a.lo = c->d_lo;
+    a.coord = c->d_coord;
     a.pos64s = c->d_pos64s;
     a.type_sorted = c->d_type_sorted;
     a.perm = c->d_perm;
@@ -1261,10 +1259,8 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         cudaMemset(c->d_e_sys, 0, sizeof(long long) * (size_t)n_sys);
     }
     const size_t ns_ = (size_t)c->n_slots;
-    TRY(dalloc(c, &c->d_hi, ns_));
-    TRY(dalloc(c, &c->d_lo, ns_));
-    cudaMemset(c->d_hi, 0, sizeof(float4) * ns_);
-    cudaMemset(c->d_lo, 0, sizeof(float4) * ns_);
+    TRY(dalloc(c, &c->d_coord, 2 * ns_));
+    cudaMemset(c->d_coord, 0, sizeof(float4) * 2 * ns_);
     if (c->fp64) {
         TRY(dalloc(c, &c->d_pos64s, ns_));
         TRY(dalloc(c, &c->d_type_sorted, ns_));

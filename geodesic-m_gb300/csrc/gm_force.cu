@@ -2,7 +2,9 @@
 //
 // Nonbonded (force/nonbonded.rs:20-82 physics): one lane per cell-sorted atom
 // i walks its own column of the symmetric neighbour list, gathers each j's
-// float4 pair (hi, lo) through the read-only path and accumulates the force
+// float4 pair (hi, lo), one 32-byte sector, with one 256-bit load through the
+// read-only path (four entries' gathers in flight before their arithmetic) and
+// accumulates the force
 // on i only, so no atomics are needed and every atom's sum has a fixed order.
 // In mixed precision the pair arithmetic is FP32; per-lane partial sums over
 // chunks of 32 entries are folded into int64 fixed point (2^-40 kcal/mol/A),
@@ -16,6 +18,7 @@ namespace {
 
 constexpr int kPairWarps = 4;
 constexpr int kChunk = 32;
+constexpr int kBatch = 4;  // list entries gathered together in the FP32 pair kernel
 constexpr float kCoulomb = 332.0522173f;
 constexpr double kCoulomb64 = 332.0522173;
 
@@ -28,7 +31,7 @@ constexpr double kCoulomb64 = 332.0522173;
 // read through L1); a single system keeps its table in shared memory.
 template <bool PERIODIC, bool COULOMB, bool BATCH, int W>
 __global__ void __launch_bounds__(W * 32)
-pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict__ coord,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
                 const int *__restrict__ gmax, int ntypes, const float2 *__restrict__ tab, float rc2, float rsw,
                 float inv_wsw, float bx, float by, float bz, float ibx, float iby, float ibz,
@@ -50,7 +53,7 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
     const bool valid = atom >= 0;
     float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
     int cnt = 0;
-    if (valid) { mh = hi[s]; ml = lo[s]; cnt = count[s]; }
+    if (valid) { mh = coord[2 * s]; ml = coord[2 * s + 1]; cnt = count[s]; }
     const float2 *trow = (BATCH ? tab + (size_t)group_sys[group] * ntypes * ntypes : s_tab) +
                          (valid ? __float_as_int(mh.w) : 0) * ntypes;
     const float qi = ml.w * kCoulomb;
@@ -65,12 +68,21 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
     for (int e0 = e_begin; e0 < e_end; e0 += kChunk) {
         float fx = 0.f, fy = 0.f, fz = 0.f, ev = 0.f;
         const int e1 = min(e0 + kChunk, e_end);
-#pragma unroll 4
-        for (int e = e0; e < e1; e++) {
-            // lanes past their own count gather their own atom: r2 == 0 drops it
-            const int j = e < cnt ? __ldg(L + (size_t)e * 32) : self;
-            const float4 jh = __ldg(hi + j);
-            const float4 jl = __ldg(lo + j);
+        for (int e = e0; e < e1; e += kBatch) {
+            // lanes past their own count (or the chunk) gather their own
+            // atom: r2 == 0 drops it
+            int jj[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++)
+                jj[u] = (e + u < cnt && e + u < e1) ? __ldg(L + (size_t)(e + u) * 32) : self;
+            float4 jhv[kBatch], jlv[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                gm_ld_coord(coord + 2 * jj[u], jhv[u], jlv[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+            const float4 jh = jhv[u], jl = jlv[u];
             float dx = (jh.x - mh.x) + (jl.x - ml.x);
             float dy = (jh.y - mh.y) + (jl.y - ml.y);
             float dz = (jh.z - mh.z) + (jl.z - ml.z);
@@ -99,10 +111,10 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
                 }
                 const float r = r2 * rinv;
                 if (r > rsw) {
-                    const float u = (r - rsw) * inv_wsw;
-                    const float u2 = u * u;
-                    const float sw = 1.f + u2 * u * (-10.f + u * (15.f - 6.f * u));
-                    const float dsw = -30.f * u2 * (1.f - u) * (1.f - u) * inv_wsw;
+                    const float u_ = (r - rsw) * inv_wsw;
+                    const float u2 = u_ * u_;
+                    const float sw = 1.f + u2 * u_ * (-10.f + u_ * (15.f - 6.f * u_));
+                    const float dsw = -30.f * u2 * (1.f - u_) * (1.f - u_) * inv_wsw;
                     fr = fr * sw - v * dsw * rinv;
                     v *= sw;
                 }
@@ -110,6 +122,7 @@ pair_kernel_f32(int n, int n_slots, int cap, int split, const float4 *__restrict
                 fy -= fr * dy;
                 fz -= fr * dz;
                 ev += v;
+            }
             }
         }
         ax += gm_to_fix_checked(fx, bad);
@@ -417,7 +430,7 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
         const size_t smem = batch ? 0 : sizeof(float2) * (size_t)a.ntypes * a.ntypes;
 #define GM_PAIR32W(P, Q, B, WW)                                                                              \
     pair_kernel_f32<P, Q, B, WW><<<blocks32, WW * 32, smem, s>>>(                                            \
-        a.n, a.n_slots, a.cap, a.split, a.hi, a.lo, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, \
+        a.n, a.n_slots, a.cap, a.split, a.coord, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab32, a.rc2, a.rsw, \
         a.inv_wsw, a.box[0], a.box[1], a.box[2], a.inv_box[0], a.inv_box[1], a.inv_box[2], a.force, a.epart, a.status, \
         a.group_sys, a.e_sys)
 #define GM_PAIR32(P, Q, B) { if (W == 2) GM_PAIR32W(P, Q, B, 2); else if (W == 8) GM_PAIR32W(P, Q, B, 8); \

@@ -119,6 +119,14 @@ __device__ __forceinline__ void gm_add_sys_energy(long long *e_sys, int sy, doub
     }
 }
 
+// Both float4 of a slot's (hi, lo) coordinate pair in one 256-bit load
+// through the read-only path (the pair is 32-byte aligned).
+__device__ __forceinline__ void gm_ld_coord(const float4 *p, float4 &h, float4 &l) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
+        : "l"(p));
+}
+
 // ------------------------------------------------------- launcher exports
 
 struct ListArgs {
@@ -128,7 +136,7 @@ struct ListArgs {
     int cap;                 // list entries per atom
     int cap_seg;             // staging entries per atom and z layer
     const double *pos;       // FP64 x|y|z rows of n atoms, caller order
-    float4 *hi, *lo;         // per slot
+    float4 *coord;           // per slot two float4: (hi x, y, z, type bits), (lo x, y, z, charge)
     double4 *pos64s;         // per slot FP64 copy (FP64 mode) or nullptr
     int *type_sorted;        // per slot types (FP64 mode)
     int *perm;               // slot -> atom (global index), -1 on padding slots
@@ -175,7 +183,7 @@ struct ForceArgs {
     int split;               // warps per 32-atom group in the FP32 pair kernel
     int pair_warps;          // warps per block of the FP32 pair kernel (2, 4, 8)
     int pair_grid;           // blocks of the FP32 pair kernel (0: one work item per warp; fewer: persistent)
-    const float4 *hi, *lo;
+    const float4 *coord;     // per slot (hi, lo) pairs: one 32-byte sector per gathered atom
     const double4 *pos64s;
     const int *type_sorted;  // FP64 mode
     const int *perm;

@@ -366,8 +366,8 @@ __global__ void pack_kernel(ListArgs a, bool fp64) {
     const double x = a.pos[at], y = a.pos[n + at], z = a.pos[2 * n + at];
     const double dx = x - g->origin[0], dy = y - g->origin[1], dz = z - g->origin[2];
     const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
-    a.hi[s] = make_float4(hx, hy, hz, __int_as_float(a.type[at]));
-    a.lo[s] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), a.charge[at]);
+    a.coord[2 * s] = make_float4(hx, hy, hz, __int_as_float(a.type[at]));
+    a.coord[2 * s + 1] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), a.charge[at]);
     if (fp64) {
         a.pos64s[s] = make_double4(x, y, z, a.charge64[at]);
         a.type_sorted[s] = a.type[at];
@@ -428,8 +428,8 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
     int my_orig = -1, my_cell = 0;
     if (valid) {
-        mh = a.hi[s];
-        ml = a.lo[s];
+        mh = a.coord[2 * s];
+        ml = a.coord[2 * s + 1];
         my_orig = a.perm[s];
         my_cell = a.cell_sorted[s];
     }
@@ -440,6 +440,9 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     const int ne = e1 - e0;
 #pragma unroll
     for (int k = 0; k < 8; k++) ex[k] = (k < ne) ? a.excl[e0 + k] : -1;
+    // the exclusions span [ex_lo, ex_hi] in caller index: candidates outside
+    // skip the scan
+    const int ex_lo = ne > 0 ? ex[0] : INT_MAX, ex_hi = ne > 0 ? a.excl[e1 - 1] : INT_MIN;
     // Candidate regions, one per distinct cell row (cy, cz) among the lanes:
     // a group of 32 sorted atoms usually lies in one row of cells, sometimes
     // straddles the end of a row.  Sweeping each row's own 5 x 5 x (span + 4)
@@ -484,8 +487,8 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                     const int t = base + lane;
                     __syncwarp();
                     if (t < b1) {
-                        s_hi[wib][lane] = a.hi[t];
-                        s_lo[wib][lane] = a.lo[t];
+                        s_hi[wib][lane] = a.coord[2 * t];
+                        s_lo[wib][lane] = a.coord[2 * t + 1];
                         s_orig[wib][lane] = a.perm[t];
                     }
                     __syncwarp();
@@ -528,12 +531,14 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                                 in = rr <= rl2_64;
                             }
                             if (!in) continue;
-                            bool excluded = false;
+                            if (jo >= ex_lo && jo <= ex_hi) {
+                                bool excluded = false;
 #pragma unroll
-                            for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
-                            if (ne > 8)
-                                for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
-                            if (excluded) continue;
+                                for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
+                                if (ne > 8)
+                                    for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
+                                if (excluded) continue;
+                            }
                             if (cnt < cap_seg) my_stage[(size_t)cnt * 32] = j;
                             cnt++;
                         }
