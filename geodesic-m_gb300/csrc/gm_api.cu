@@ -86,6 +86,8 @@ struct gm_ctx {
     // 1-4
     int n14 = 0, blocks14 = 0;
     int *d_p14i = nullptr, *d_p14j = nullptr;
+    float4 *d_p14par = nullptr;
+    double2 *d_acs = nullptr;
     // constraints
     int n_constr = 0, n_clusters = 0, n_single = 0, n_star_end = 0, n_warp_end = 0;
     int *d_ci = nullptr, *d_cj = nullptr, *d_cl_cstart = nullptr, *d_cl_cons = nullptr, *d_cl_astart = nullptr,
@@ -280,6 +282,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.n_diheds = c->n_diheds;
     a.bond_i = c->d_bi; a.bond_j = c->d_bj; a.bond_k = c->d_bk; a.bond_r0 = c->d_br0;
     a.angle_i = c->d_ai; a.angle_j = c->d_aj; a.angle_k = c->d_ak; a.angle_kth = c->d_akth; a.angle_th0 = c->d_ath0;
+    a.angle_cs = c->d_acs;
     a.dihed_i = c->d_di; a.dihed_j = c->d_dj; a.dihed_k = c->d_dk; a.dihed_l = c->d_dl; a.dihed_kphi = c->d_dkphi;
     a.dihed_n = c->d_dn; a.dihed_delta = c->d_ddelta;
     a.bonded_blocks = c->bonded_blocks;
@@ -288,6 +291,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.n14 = c->n14; a.p14_i = c->d_p14i; a.p14_j = c->d_p14j;
     a.scale14_lj = c->p.scale14_lj; a.scale14_coul = c->p.scale14_coul;
     a.sigma = c->d_sigma; a.epsilon = c->d_eps; a.charge64 = c->d_charge64;
+    a.p14par = c->d_p14par;
     a.blocks14 = c->blocks14;
     a.epart14 = c->d_epart + pair_parts + c->bonded_blocks;
     a.energy = c->d_energy;
@@ -382,7 +386,7 @@ int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branc
         cudaStreamWaitEvent(branch, c->ev_fork, 0);
     }
     gm_launch_bonded(fa, c->fp64, sb);
-    gm_launch_pair14(fa, sb);
+    gm_launch_pair14(fa, c->fp64, sb);
     gm_launch_pair(fa, c->fp64, s);
     if (fork) {
         cudaEventRecord(c->ev_join, branch);
@@ -1127,6 +1131,11 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dupload(c, &c->d_ak, v(t->angle_k, t->n_angles).data(), (size_t)t->n_angles));
     TRY(dupload(c, &c->d_akth, t->angle_kth, (size_t)t->n_angles));
     TRY(dupload(c, &c->d_ath0, t->angle_th0, (size_t)t->n_angles));
+    {
+        std::vector<double2> cs((size_t)t->n_angles);
+        for (int64_t q = 0; q < t->n_angles; q++) cs[(size_t)q] = make_double2(std::cos(t->angle_th0[q]), std::sin(t->angle_th0[q]));
+        TRY(dupload(c, &c->d_acs, cs.data(), cs.size()));
+    }
     TRY(dupload(c, &c->d_di, v(t->dihed_i, t->n_diheds).data(), (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_dj, v(t->dihed_j, t->n_diheds).data(), (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_dk, v(t->dihed_k, t->n_diheds).data(), (size_t)t->n_diheds));
@@ -1158,6 +1167,16 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         c->blocks14 = (c->n14 + 255) / 256;
         TRY(dupload(c, &c->d_p14i, a.data(), a.size()));
         TRY(dupload(c, &c->d_p14j, b.data(), b.size()));
+        // FP32 parameters of the mixed path (force/nonbonded.rs:20-82 mixing)
+        std::vector<float4> par(p14.size());
+        for (size_t k = 0; k < p14.size(); k++) {
+            const int i = a[k], j = b[k];
+            const double sg = 0.5 * (atoms->sigma[i] + atoms->sigma[j]);
+            const double ep = std::sqrt(atoms->epsilon[i] * atoms->epsilon[j]);
+            const double qq = p.coulomb ? 332.0522173 * charge64[(size_t)i] * charge64[(size_t)j] : 0.0;
+            par[k] = make_float4((float)(sg * sg), (float)(p.scale14_lj * 4.0 * ep), (float)(p.scale14_coul * qq), 0.f);
+        }
+        TRY(dupload(c, &c->d_p14par, par.data(), par.size()));
     }
     // ---- constraints as independent clusters
     c->n_constr = (int)t->n_constr;
@@ -1575,6 +1594,8 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
                 if (c->use_graph) cudaGraphLaunch(c->graph_exec, c->stream);
                 else run_direct(c, dt, 1);
                 break;
+            case 5: seq_forces(c, c->stream, false, c->side); break;
+            case 6: gm_launch_pair14(fa, c->fp64, c->stream); break;
             default: gm_launch_pack(la, c->fp64, c->stream); break;
         }
         cudaEventRecord(e1, c->stream);

@@ -255,6 +255,7 @@ __device__ __forceinline__ double gm_atan2(double y, double x) { return atan2(y,
 
 template <typename T>
 __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
+    constexpr bool kMixed = sizeof(T) == sizeof(float);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
     double e = 0.0;
@@ -270,7 +271,25 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
         const double k = a.bond_k[t], r0 = a.bond_r0[t];
         const double r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 > 0.0) {
+        bool done = false;
+        if (kMixed && r2 > 0.0) {
+            // mixed path: r - r0 = (r^2 - r0^2) / (r + r0), the cancelling
+            // difference r^2 - r0^2 in FP64 and the rest in FP32 (the FP64
+            // pipe is the bottleneck of this kernel); a bond stretched by
+            // half an angstrom or more takes the FP64 branch below
+            const float r = sqrtf((float)r2);
+            const float dr = (float)fma(-r0, r0, r2) / (r + (float)r0);
+            if (fabsf(dr) < 0.5f && r > 1e-3f) {
+                const float kf = (float)k;
+                e = (double)(kf * dr * dr);
+                const float g = 2.f * kf * dr / r;
+                const float fx = g * (float)dx, fy = g * (float)dy, fz = g * (float)dz;
+                add_force<float>(a.force, n, i, fx, fy, fz, bad);
+                add_force<float>(a.force, n, j, -fx, -fy, -fz, bad);
+                done = true;
+            }
+        }
+        if (!done && r2 > 0.0) {
             const double r = sqrt(r2);
             const double dr = r - r0;
             e = k * dr * dr;
@@ -285,7 +304,38 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         first = i;
         const V3<T> b1 = diff<T>(a.pos, n, i, j), b2 = diff<T>(a.pos, n, kk, j);
         const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
-        if (r1 != (T)0 && r2 != (T)0) {
+        if (kMixed && r1 != (T)0 && r2 != (T)0) {
+            // mixed path: theta - theta0 = atan2(sin(theta - theta0),
+            // cos(theta - theta0)), both from FP64 products
+            //   |d1||d2| sin(theta - theta0) = |d1 x d2| cos theta0 - (d1 . d2) sin theta0
+            //   |d1||d2| cos(theta - theta0) = (d1 . d2) cos theta0 + |d1 x d2| sin theta0
+            // with |d1 x d2| from an FP32 square root and one Newton step in
+            // FP64; no FP64 acos, square root or division
+            const V3<double> d1 = diff<double>(a.pos, n, i, j), d2 = diff<double>(a.pos, n, kk, j);
+            const double dd = dot(d1, d2);
+            const V3<double> cr = cross(d1, d2);
+            const double q2 = dot(cr, cr);
+            const float s32 = sqrtf((float)q2);
+            double sx = (double)s32;
+            if (s32 > 0.f) sx = fma(fma(-sx, sx, q2), (double)(0.5f / s32), sx);
+            const double2 cs0 = a.angle_cs[q];
+            const double y = sx * cs0.x - dd * cs0.y, x = dd * cs0.x + sx * cs0.y;
+            const float dth = atan2f((float)y, (float)x);
+            const float k = (float)a.angle_kth[q];
+            e = (double)(k * dth * dth);
+            const float ir12 = 1.f / (float)(r1 * r2), ir11 = 1.f / (float)(r1 * r1), ir22 = 1.f / (float)(r2 * r2);
+            const float c = (float)dd * ir12;
+            float sn = (float)sx * ir12;
+            sn = sn > 1e-8f ? sn : 1e-8f;
+            const float aa = 2.f * k * dth / sn;
+            const V3<float> fi = {aa * ((float)b2.x * ir12 - c * (float)b1.x * ir11), aa * ((float)b2.y * ir12 - c * (float)b1.y * ir11),
+                                  aa * ((float)b2.z * ir12 - c * (float)b1.z * ir11)};
+            const V3<float> fk = {aa * ((float)b1.x * ir12 - c * (float)b2.x * ir22), aa * ((float)b1.y * ir12 - c * (float)b2.y * ir22),
+                                  aa * ((float)b1.z * ir12 - c * (float)b2.z * ir22)};
+            add_force<float>(a.force, n, i, fi.x, fi.y, fi.z, bad);
+            add_force<float>(a.force, n, kk, fk.x, fk.y, fk.z, bad);
+            add_force<float>(a.force, n, j, -(fi.x + fk.x), -(fi.y + fk.y), -(fi.z + fk.z), bad);
+        } else if (r1 != (T)0 && r2 != (T)0) {
             // theta - theta0 in FP64 in both paths: an FP32 acos is off by
             // ~1e-7 rad, i.e. ~1e-5 kcal/mol/A at k = 50, which a structure
             // near equilibrium cannot absorb
@@ -353,13 +403,41 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
 
 // Scaled 1-4 pairs (beyond the reference): unswitched, no cutoff; LJ scaled by
 // scale14_lj, Coulomb by scale14_coul.  FP64 arithmetic, few pairs.
+template <bool MIXED>
 __global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = a.n;
     double e = 0.0;
     unsigned bad = 0;
     int first = -1;
-    if (t < a.n14) {
+    if (MIXED && t < a.n14) {
+        // FP32 pair arithmetic as in the pair kernel, on the FP64 difference
+        const int i = a.p14_i[t], j = a.p14_j[t];
+        first = i;
+        const float dx = (float)(a.pos[j] - a.pos[i]), dy = (float)(a.pos[n + j] - a.pos[n + i]),
+                    dz = (float)(a.pos[2 * n + j] - a.pos[2 * n + i]);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 > 0.f) {
+            const float4 p = a.p14par[t];
+            float rinv = rsqrtf(r2);
+            rinv = fmaf(0.5f * rinv, fmaf(-r2 * rinv, rinv, 1.0f), rinv);
+            const float rinv2 = rinv * rinv;
+            float v = 0.f, g = 0.f;  // g = F_r / r
+            if (p.y != 0.f) {
+                const float s2 = p.x * rinv2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+                v += p.y * (s12 - s6);
+                g += 6.f * p.y * (2.f * s12 - s6) * rinv2;
+            }
+            if (p.z != 0.f) {
+                const float vc = p.z * rinv;
+                v += vc;
+                g += vc * rinv2;
+            }
+            e = (double)v;
+            add_force<float>(a.force, n, i, -g * dx, -g * dy, -g * dz, bad);
+            add_force<float>(a.force, n, j, g * dx, g * dy, g * dz, bad);
+        }
+    } else if (!MIXED && t < a.n14) {
         const int i = a.p14_i[t], j = a.p14_j[t];
         first = i;
         const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
@@ -462,9 +540,10 @@ void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s) {
     else bonded_kernel<float><<<a.bonded_blocks, 256, 0, s>>>(a);
 }
 
-void gm_launch_pair14(const ForceArgs &a, cudaStream_t s) {
+void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.blocks14 == 0) return;
-    pair14_kernel<<<a.blocks14, 256, 0, s>>>(a);
+    if (fp64) pair14_kernel<false><<<a.blocks14, 256, 0, s>>>(a);
+    else pair14_kernel<true><<<a.blocks14, 256, 0, s>>>(a);
 }
 
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s) {

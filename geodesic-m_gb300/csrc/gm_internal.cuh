@@ -205,6 +205,7 @@ struct ForceArgs {
     int n_bonds, n_angles, n_diheds;
     const int *bond_i, *bond_j; const double *bond_k, *bond_r0;
     const int *angle_i, *angle_j, *angle_k; const double *angle_kth, *angle_th0;
+    const double2 *angle_cs;  // (cos theta0, sin theta0) per angle
     const int *dihed_i, *dihed_j, *dihed_k, *dihed_l; const double *dihed_kphi; const int *dihed_n;
     const double *dihed_delta;
     double *epart_bonded;    // per block
@@ -212,6 +213,7 @@ struct ForceArgs {
     // scaled 1-4 pairs
     int n14; const int *p14_i, *p14_j; double scale14_lj, scale14_coul;
     const double *sigma, *epsilon, *charge64;
+    const float4 *p14par;     // per 1-4 pair: (sigma_ij^2, 4 eps_ij * scale_lj, k_C q_i q_j * scale_coul, 0)
     double *epart14; int blocks14;
     double *energy;          // total
     int n_epart_total;       // n_groups * split + bonded_blocks + blocks14 entries
@@ -219,7 +221,7 @@ struct ForceArgs {
 
 void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s);
 void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s);
-void gm_launch_pair14(const ForceArgs &a, cudaStream_t s);
+void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s);
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s);
 int gm_bonded_blocks(int n_bonds, int n_angles, int n_diheds);
 
