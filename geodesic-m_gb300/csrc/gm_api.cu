@@ -56,7 +56,7 @@ struct gm_ctx {
     double4 *d_pos64s = nullptr;
     int *d_type_sorted = nullptr;
     int *d_perm = nullptr, *d_cell_of = nullptr, *d_cell_sorted = nullptr, *d_cell_count = nullptr,
-        *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr;
+        *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr, *d_slot_of = nullptr;
     long long total_cells = 0;     // cell budget of all systems
     // systems of a batch (one for a plain context)
     int n_sys = 1, n_slots = 0, scan_blocks = 0, max_sys_atoms = 0;
@@ -200,6 +200,7 @@ ListArgs list_args(gm_ctx *c) {
     a.pos64s = c->d_pos64s;
     a.type_sorted = c->d_type_sorted;
     a.perm = c->d_perm;
+    a.slot_of = c->d_slot_of;
     a.cell_of = c->d_cell_of;
     a.cell_sorted = c->d_cell_sorted;
     a.cell_count = c->d_cell_count;
@@ -248,6 +249,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.pair_warps = c->pair_warps;
     a.pair_grid = c->pair_grid;
     a.coord = c->d_coord;
+    a.slot_of = c->d_slot_of;
     a.pos64s = c->d_pos64s;
     a.type_sorted = c->d_type_sorted;
     a.perm = c->d_perm;
@@ -374,10 +376,11 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
 // per-system energy sum is an integer sum and every energy partial has its own
 // slot, so the order in which the branches add changes no bit.  Without
 // `energy` the partials stay unsummed (energy_stale) until refresh_energy.
-int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr) {
+// `packed`: the step kernel before it already packed the coordinates.
+int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr, bool packed = false) {
     ListArgs la = list_args(c);
     if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);
-    gm_launch_pack(la, c->fp64, s);
+    if (!packed) gm_launch_pack(la, c->fp64, s);
     ForceArgs fa = force_args(c);
     const bool fork = branch && (c->bonded_blocks || c->blocks14);
     const cudaStream_t sb = fork ? branch : s;
@@ -394,7 +397,21 @@ int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branc
     }
     if (energy) gm_launch_energy(fa, s);
     c->energy_stale = !energy;
-    return 1 + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + (energy ? 1 : 0);
+    return (packed ? 0 : 1) + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + (energy ? 1 : 0);
+}
+
+PackArgs pack_args(gm_ctx *c) {
+    PackArgs p{};
+    p.coord = c->d_coord;
+    p.pos64s = c->d_pos64s;
+    p.type_sorted = c->d_type_sorted;
+    p.slot_of = c->d_slot_of;
+    p.grid = c->d_grid;
+    p.type = c->d_type;
+    p.charge = c->d_charge;
+    p.charge64 = c->d_charge64;
+    p.fp64 = c->fp64 ? 1 : 0;
+    return p;
 }
 
 // Sum the energy partials of the last force evaluation into d_energy.
@@ -626,7 +643,8 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
     if (!constrained) {
         gm_launch_kick_drift_check(n, c->d_pos, c->d_vel, c->d_dref, c->d_force, c->d_inv_mass, dt / 2.0, dt, c->d_ref,
-                                   half_skin * half_skin, c->d_status, cond, c->d_atom_sys, c->d_sys_flag, s);
+                                   half_skin * half_skin, c->d_status, cond, c->d_atom_sys, c->d_sys_flag,
+                                   pack_args(c), s);
         *count += 1;
         return GM_OK;
     }
@@ -642,7 +660,7 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
 }
 
 int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
-    long long k = seq_forces(c, s, false, c->side);
+    long long k = seq_forces(c, s, false, c->side, c->n_clusters == 0);
     if (!c->n_clusters) {
         gm_launch_kick_step(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
         *count += k;
@@ -1288,6 +1306,7 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     }
     TRY(dalloc(c, &c->d_perm, ns_));
     cudaMemset(c->d_perm, 0xFF, sizeof(int) * ns_);  // -1: padding until a build fills the slot
+    TRY(dalloc(c, &c->d_slot_of, (size_t)std::max(n, 1)));
     TRY(dalloc(c, &c->d_cell_of, (size_t)n));
     TRY(dalloc(c, &c->d_cell_sorted, ns_));
     TRY(dalloc(c, &c->d_tmp_atom, ns_));

@@ -234,6 +234,14 @@ __device__ __forceinline__ V3<T> diff(const double *pos, int n, int a, int b) {
     // pos[a] - pos[b], differenced in FP64 before any narrowing
     return {(T)(pos[a] - pos[b]), (T)(pos[n + a] - pos[n + b]), (T)(pos[2 * n + a] - pos[2 * n + b])};
 }
+// FP32 difference of two atoms of one system from their (hi, lo) slot copies
+// (relative to the same grid origin): the rounded FP64 difference within an ulp
+__device__ __forceinline__ V3<float> fdiff(const ForceArgs &a, int ia, int ib) {
+    float4 ha, la, hb, lb;
+    gm_ld_coord(a.coord + 2 * a.slot_of[ia], ha, la);
+    gm_ld_coord(a.coord + 2 * a.slot_of[ib], hb, lb);
+    return {(ha.x - hb.x) + (la.x - lb.x), (ha.y - hb.y) + (la.y - lb.y), (ha.z - hb.z) + (la.z - lb.z)};
+}
 template <typename T>
 __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
@@ -302,7 +310,9 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         const int q = t - a.n_bonds;
         const int i = a.angle_i[q], j = a.angle_j[q], kk = a.angle_k[q];
         first = i;
-        const V3<T> b1 = diff<T>(a.pos, n, i, j), b2 = diff<T>(a.pos, n, kk, j);
+        V3<T> b1, b2;
+        if constexpr (kMixed) { b1 = fdiff(a, i, j); b2 = fdiff(a, kk, j); }
+        else { b1 = diff<T>(a.pos, n, i, j); b2 = diff<T>(a.pos, n, kk, j); }
         const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
         if (kMixed && r1 != (T)0 && r2 != (T)0) {
             // mixed path: theta - theta0 = atan2(sin(theta - theta0),
@@ -364,7 +374,9 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         const int q = t - a.n_bonds - a.n_angles;
         const int i = a.dihed_i[q], j = a.dihed_j[q], k = a.dihed_k[q], l = a.dihed_l[q];
         first = i;
-        const V3<T> b1 = diff<T>(a.pos, n, j, i), b2 = diff<T>(a.pos, n, k, j), b3 = diff<T>(a.pos, n, l, k);
+        V3<T> b1, b2, b3;
+        if constexpr (kMixed) { b1 = fdiff(a, j, i); b2 = fdiff(a, k, j); b3 = fdiff(a, l, k); }
+        else { b1 = diff<T>(a.pos, n, j, i); b2 = diff<T>(a.pos, n, k, j); b3 = diff<T>(a.pos, n, l, k); }
         const V3<T> m = cross(b1, b2), nv = cross(b2, b3);
         const T m2 = dot(m, m), n2 = dot(nv, nv), b2l = sqrt(dot(b2, b2));
         if (m2 != (T)0 && n2 != (T)0 && b2l != (T)0) {
@@ -414,8 +426,8 @@ __global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
         // FP32 pair arithmetic as in the pair kernel, on the FP64 difference
         const int i = a.p14_i[t], j = a.p14_j[t];
         first = i;
-        const float dx = (float)(a.pos[j] - a.pos[i]), dy = (float)(a.pos[n + j] - a.pos[n + i]),
-                    dz = (float)(a.pos[2 * n + j] - a.pos[2 * n + i]);
+        const V3<float> d = fdiff(a, j, i);
+        const float dx = d.x, dy = d.y, dz = d.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 > 0.f) {
             const float4 p = a.p14par[t];

@@ -854,16 +854,17 @@ __global__ void forces_out_kernel(int n3, const long long *force, double *out) {
 
 }  // namespace
 
-// half_kick_kernel, drift_kernel (resync) and check_kernel fused for systems
-// without constraints: one atom per thread, the same operations in the same
-// order.  A block that finds a non-finite position marks bad_pending instead of
+// half_kick_kernel, drift_kernel (resync), check_kernel and pack_kernel's
+// per-atom work fused for systems without constraints: one atom per thread,
+// the same operations in the same order (a rebuild that the check triggers
+// packs again with the new grid).  A block that finds a non-finite position marks bad_pending instead of
 // error, and the last block moves it to error, so every block of the launch
 // reads the error word as it stood before the launch (as the separate kick and
 // drift kernels do).
-__global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double *dref, const long long *force,
+__global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double *dref, long long *force,
                                         const double *inv_mass, double dt_half, double dt, const double *ref,
                                         double thr_sq, DevStatus *st, unsigned long long cond, const int *atom_sys,
-                                        unsigned int *sys_flag) {
+                                        unsigned int *sys_flag, PackArgs pk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int need = 0, bad = 0;
     if (i < n) {
@@ -882,6 +883,19 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
         } else {
             for (int d = 0; d < 3; d++) np[d] = pos[d * n + i];
         }
+        // pack_kernel's work for this atom, from the same FP64 position
+        const int sl = pk.slot_of[i];
+        const GridInfo *g = pk.grid + atom_sys[i];
+        const double ox = np[0] - g->origin[0], oy = np[1] - g->origin[1], oz = np[2] - g->origin[2];
+        const float hx = (float)ox, hy = (float)oy, hz = (float)oz;
+        pk.coord[2 * sl] = make_float4(hx, hy, hz, __int_as_float(pk.type[i]));
+        pk.coord[2 * sl + 1] = make_float4((float)(ox - (double)hx), (float)(oy - (double)hy), (float)(oz - (double)hz),
+                                           pk.charge[i]);
+        if (pk.fp64) {
+            pk.pos64s[sl] = make_double4(np[0], np[1], np[2], pk.charge64[i]);
+            pk.type_sorted[sl] = pk.type[i];
+        }
+        for (int d = 0; d < 3; d++) force[d * n + i] = 0;
         bad = !(isfinite(np[0]) && isfinite(np[1]) && isfinite(np[2]));
         const double dx = np[0] - ref[i], dy = np[1] - ref[n + i], dz = np[2] - ref[2 * n + i];
         need = dx * dx + dy * dy + dz * dz > thr_sq;
@@ -942,12 +956,12 @@ void gm_launch_resync(int n, const double *pos, double *vel, const double *dref,
 }
 
 void gm_launch_step(DevStatus *st, cudaStream_t s) { step_kernel<<<1, 1, 0, s>>>(st); }
-void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, const long long *force,
+void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, long long *force,
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
-                                cudaStream_t s) {
+                                const PackArgs &pk, cudaStream_t s) {
     kick_drift_check_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, pos, vel, dref, force, inv_mass, dt_half, dt, ref,
-                                                              thr_sq, st, cond, atom_sys, sys_flag);
+                                                              thr_sq, st, cond, atom_sys, sys_flag, pk);
 }
 void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s) {

@@ -86,10 +86,30 @@ struct GridInfo {
 __device__ __forceinline__ long long gm_to_fix(double v) { return __double2ll_rn(v * GM_FIX_SCALE); }
 
 // A float force contribution to fixed point; flags non-finite / overflow.
+// round(v * 2^40) to the nearest integer, ties to even, for |v| < 2^22, from
+// the bits of v with integer operations only (the same value as
+// __float2ll_rn(v * 2^40); a 64-bit conversion instruction is slow here)
+__device__ __forceinline__ long long gm_f2fix(float v) {
+    const unsigned b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xffu);
+    const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+    const int sh = e - 150 + 40;  // |v| * 2^40 = m * 2^sh (normal v)
+    long long r;
+    if (e == 0 || sh < -25) {
+        r = 0;  // below 2^-41: rounds to zero
+    } else if (sh >= 0) {
+        r = m << sh;
+    } else {
+        const int s = -sh;
+        const long long q = m >> s, rem = m & ((1ll << s) - 1), half = 1ll << (s - 1);
+        r = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    }
+    return (b >> 31) ? -r : r;
+}
 __device__ __forceinline__ long long gm_to_fix_checked(float v, unsigned int &bad) {
-    if (!isfinite(v)) bad |= GM_DEV_NONFINITE_FORCE;
-    else if (fabsf(v) >= (float)GM_FIX_LIMIT) bad |= GM_DEV_FIX_OVERFLOW;
-    return __float2ll_rn(v * GM_FIX_SCALE_F);
+    if (!isfinite(v)) { bad |= GM_DEV_NONFINITE_FORCE; return 0; }
+    if (fabsf(v) >= (float)GM_FIX_LIMIT) { bad |= GM_DEV_FIX_OVERFLOW; return 0; }
+    return gm_f2fix(v);
 }
 __device__ __forceinline__ long long gm_to_fix_checked(double v, unsigned int &bad) {
     if (!isfinite(v)) bad |= GM_DEV_NONFINITE_FORCE;
@@ -140,6 +160,7 @@ struct ListArgs {
     double4 *pos64s;         // per slot FP64 copy (FP64 mode) or nullptr
     int *type_sorted;        // per slot types (FP64 mode)
     int *perm;               // slot -> atom (global index), -1 on padding slots
+    int *slot_of;            // atom -> slot (or nullptr)
     int *cell_of;            // atom -> cell of its system
     int *cell_sorted;        // slot -> cell of its system
     int *cell_count, *cell_start, *cell_cursor;  // system s at sys_cell_off[s] (cell_start: ncell + 1 entries)
@@ -184,6 +205,7 @@ struct ForceArgs {
     int pair_warps;          // warps per block of the FP32 pair kernel (2, 4, 8)
     int pair_grid;           // blocks of the FP32 pair kernel (0: one work item per warp; fewer: persistent)
     const float4 *coord;     // per slot (hi, lo) pairs: one 32-byte sector per gathered atom
+    const int *slot_of;      // atom -> slot
     const double4 *pos64s;
     const int *type_sorted;  // FP64 mode
     const int *perm;
@@ -271,10 +293,24 @@ void gm_launch_step(DevStatus *st, cudaStream_t s);
 // Unconstrained step: half-kick + drift (with the velocity resync) + rebuild
 // check in one launch, and half-kick + step counter in one launch.  Each atom
 // gets the same operations in the same order as the separate kernels.
-void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, const long long *force,
+// The pack kernel's per-atom work (FP32 (hi, lo) copies relative to the
+// system's grid origin, FP64 copies in FP64 mode, forces cleared), done by the
+// fused step kernel for the force evaluation that follows it.
+struct PackArgs {
+    float4 *coord;
+    double4 *pos64s;
+    int *type_sorted;
+    const int *slot_of;
+    const GridInfo *grid;
+    const int *type;
+    const float *charge;
+    const double *charge64;
+    int fp64;
+};
+void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, long long *force,
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
-                                cudaStream_t s);
+                                const PackArgs &pk, cudaStream_t s);
 void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s);
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,

@@ -345,12 +345,14 @@ __global__ void rank_kernel(ListArgs a) {
             atomicOr(&a.status->error, (unsigned)GM_DEV_CELL_OVERFLOW);
             a.perm[soff + k] = a0 + at;
             a.cell_sorted[soff + k] = c;
+            if (a.slot_of) a.slot_of[a0 + at] = soff + k;
             continue;
         }
         int rank = 0;
         for (int m = s0; m < s1; m++) rank += a.tmp_atom[soff + m] < at;
         a.perm[soff + s0 + rank] = a0 + at;
         a.cell_sorted[soff + s0 + rank] = c;
+        if (a.slot_of) a.slot_of[a0 + at] = soff + s0 + rank;
     }
 }
 
