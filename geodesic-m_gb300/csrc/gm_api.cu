@@ -1615,6 +1615,11 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
                 break;
             case 5: seq_forces(c, c->stream, false, c->side); break;
             case 6: gm_launch_pair14(fa, c->fp64, c->stream); break;
+            case 7:  // the list build kernel alone, every system
+                gm_launch_flags(la, true, c->stream);
+                gm_launch_build(la, c->stream);
+                gm_launch_flags(la, false, c->stream);
+                break;
             default: gm_launch_pack(la, c->fp64, c->stream); break;
         }
         cudaEventRecord(e1, c->stream);

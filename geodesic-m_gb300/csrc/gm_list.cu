@@ -403,10 +403,14 @@ __device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c
 // One block per group, one warp per z layer: warp `seg` tests the candidates
 // of z layer `seg` of each row box its lanes need and stages them; the block
 // then concatenates the layers into each lane's list column.
+template <bool PERIODIC>
 __global__ void __launch_bounds__(GM_NSEG * 32)
 build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
-    __shared__ float4 s_hi[GM_NSEG][32];
-    __shared__ float4 s_lo[GM_NSEG][32];
+    // candidates of the current batch: coordinates relative to the group's
+    // first atom (FP32; the rounding, under 1e-5 A for candidates within a
+    // few list radii, stays far inside the FP64 re-decision margin) and
+    // caller indices
+    __shared__ float4 s_rel[GM_NSEG][32];
     __shared__ int s_orig[GM_NSEG][32];
     __shared__ int s_cnt[GM_NSEG][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -416,8 +420,7 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     const int sys = a.group_sys[group];
     if (!a.sys_flag[sys]) return;  // block-uniform: the system keeps its list
     // the unrolled candidate loop below reads all 32 staging entries
-    s_hi[wib][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-    s_lo[wib][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s_rel[wib][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
     s_orig[wib][lane] = 0;
     const int soff = a.sys_slot_off[sys], coff = a.sys_cell_off[sys];
     const int ns = a.sys_atom_off[sys + 1] - a.sys_atom_off[sys];
@@ -427,11 +430,18 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     const int n = a.n;
     const int cap = a.cap;
     const int *__restrict__ cell_start = a.cell_start + coff;
-    float4 mh = make_float4(0.f, 0.f, 0.f, 0.f), ml = mh;
+    // the reference point: the group's first slot (always an atom: systems
+    // start on a group boundary)
+    float4 rh, rl;
+    gm_ld_coord(a.coord + 2 * group * 32, rh, rl);
+    float mx = 0.f, my = 0.f, mz = 0.f;
     int my_orig = -1, my_cell = 0;
     if (valid) {
-        mh = a.coord[2 * s];
-        ml = a.coord[2 * s + 1];
+        float4 mh, ml;
+        gm_ld_coord(a.coord + 2 * s, mh, ml);
+        mx = (mh.x - rh.x) + (ml.x - rl.x);
+        my = (mh.y - rh.y) + (ml.y - rl.y);
+        mz = (mh.z - rh.z) + (ml.z - rl.z);
         my_orig = a.perm[s];
         my_cell = a.cell_sorted[s];
     }
@@ -489,61 +499,60 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                     const int t = base + lane;
                     __syncwarp();
                     if (t < b1) {
-                        s_hi[wib][lane] = a.coord[2 * t];
-                        s_lo[wib][lane] = a.coord[2 * t + 1];
+                        float4 ch, cl;
+                        gm_ld_coord(a.coord + 2 * t, ch, cl);
+                        s_rel[wib][lane] = make_float4((ch.x - rh.x) + (cl.x - rl.x), (ch.y - rh.y) + (cl.y - rl.y),
+                                                       (ch.z - rh.z) + (cl.z - rl.z), 0.f);
                         s_orig[wib][lane] = a.perm[t];
                     }
                     __syncwarp();
                     if (!mine) continue;
                     const int m = min(32, b1 - base);
-                    // four candidates at a time: the distance tests are
-                    // independent, the rare accepted ones are handled in order
-                    for (int k0 = 0; k0 < m; k0 += 4) {
-                        float r2v[4];
-                        unsigned hit = 0;
+                    // distance tests of all 32 staged candidates: bit k of
+                    // `near` within the list radius plus the margin, of `sure`
+                    // within it minus the margin
+                    unsigned near = 0, sure = 0;
 #pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            const int k = k0 + u;
-                            const float4 ch = s_hi[wib][k], cl = s_lo[wib][k];
-                            float dx = (ch.x - mh.x) + (cl.x - ml.x);
-                            float dy = (ch.y - mh.y) + (cl.y - ml.y);
-                            float dz = (ch.z - mh.z) + (cl.z - ml.z);
-                            if (g.periodic) {
-                                dx -= g.box[0] * rintf(dx * g.inv_box[0]);
-                                dy -= g.box[1] * rintf(dy * g.inv_box[1]);
-                                dz -= g.box[2] * rintf(dz * g.inv_box[2]);
-                            }
-                            r2v[u] = dx * dx + dy * dy + dz * dz;
-                            if (k < m && base + k != s && r2v[u] <= rl2_hi) hit |= 1u << u;
+                    for (int k = 0; k < 32; k++) {
+                        const float4 c = s_rel[wib][k];
+                        float dx = c.x - mx, dy = c.y - my, dz = c.z - mz;
+                        if (PERIODIC) {
+                            dx -= g.box[0] * rintf(dx * g.inv_box[0]);
+                            dy -= g.box[1] * rintf(dy * g.inv_box[1]);
+                            dz -= g.box[2] * rintf(dz * g.inv_box[2]);
                         }
-                        if (!hit) continue;
-#pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            if (!((hit >> u) & 1u)) continue;
-                            const int k = k0 + u;
-                            const int j = base + k;
-                            const int jo = s_orig[wib][k];
-                            bool in = r2v[u] <= rl2_lo;
-                            if (!in) {
-                                // the reference's own FP64 decision
-                                double ex_ = exact_min_image(__dsub_rn(a.pos[jo], a.pos[my_orig]), bx[0]);
-                                double ey_ = exact_min_image(__dsub_rn(a.pos[n + jo], a.pos[n + my_orig]), bx[1]);
-                                double ez_ = exact_min_image(__dsub_rn(a.pos[2 * n + jo], a.pos[2 * n + my_orig]), bx[2]);
-                                double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
-                                in = rr <= rl2_64;
-                            }
-                            if (!in) continue;
-                            if (jo >= ex_lo && jo <= ex_hi) {
-                                bool excluded = false;
-#pragma unroll
-                                for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
-                                if (ne > 8)
-                                    for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
-                                if (excluded) continue;
-                            }
-                            if (cnt < cap_seg) my_stage[(size_t)cnt * 32] = j;
-                            cnt++;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        near |= (r2 <= rl2_hi ? 1u : 0u) << k;
+                        sure |= (r2 <= rl2_lo ? 1u : 0u) << k;
+                    }
+                    near &= m < 32 ? (1u << m) - 1u : 0xffffffffu;
+                    const int self = s - base;
+                    if (self >= 0 && self < 32) near &= ~(1u << self);
+                    // the accepted candidates, in order
+                    while (near) {
+                        const int k = __ffs(near) - 1;
+                        near &= near - 1;
+                        const int jo = s_orig[wib][k];
+                        bool in = (sure >> k) & 1u;
+                        if (!in) {
+                            // the reference's own FP64 decision
+                            double ex_ = exact_min_image(__dsub_rn(a.pos[jo], a.pos[my_orig]), bx[0]);
+                            double ey_ = exact_min_image(__dsub_rn(a.pos[n + jo], a.pos[n + my_orig]), bx[1]);
+                            double ez_ = exact_min_image(__dsub_rn(a.pos[2 * n + jo], a.pos[2 * n + my_orig]), bx[2]);
+                            double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex_, ex_), __dmul_rn(ey_, ey_)), __dmul_rn(ez_, ez_));
+                            in = rr <= rl2_64;
                         }
+                        if (!in) continue;
+                        if (jo >= ex_lo && jo <= ex_hi) {
+                            bool excluded = false;
+#pragma unroll
+                            for (int q = 0; q < 8; q++) excluded |= (ex[q] == jo);
+                            if (ne > 8)
+                                for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
+                            if (excluded) continue;
+                        }
+                        if (cnt < cap_seg) my_stage[(size_t)cnt * 32] = base + k;
+                        cnt++;
                     }
                 }
             }
@@ -633,6 +642,8 @@ void gm_launch_build(const ListArgs &a, cudaStream_t s) {
     const int groups = a.n_slots / 32;
     const double rl2 = a.r_list * a.r_list;  // neighbor.rs:25
     const double margin = 1e-3 * (rl2 > 144.0 ? rl2 / 144.0 : 1.0);
-    build_kernel<<<groups, GM_NSEG * 32, 0, s>>>(
-        a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
+    if (a.periodic)
+        build_kernel<true><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
+    else
+        build_kernel<false><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
 }

@@ -400,7 +400,7 @@ class CudaBackend:
 
     def profile(self, which: str, n_iter: int = 20, dt: float = 0.002) -> float:
         """Average device milliseconds of one launch (CUDA events)."""
-        code = {"pair": 0, "bonded": 1, "rebuild": 2, "step": 3, "pack": 4, "forces": 5, "pair14": 6}[which]
+        code = {"pair": 0, "bonded": 1, "rebuild": 2, "step": 3, "pack": 4, "forces": 5, "pair14": 6, "build": 7}[which]
         ms = C.c_double()
         self._check(lib().gm_profile(self._h, code, n_iter, dt, C.byref(ms)))
         return ms.value

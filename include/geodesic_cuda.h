@@ -168,7 +168,8 @@ int32_t gm_synchronize(gm_ctx *ctx, gm_convergence *err);
  * launch of: which = 0 the pair kernel, 1 the bonded kernel, 2 the list
  * rebuild sequence, 3 one captured BAB step of length dt, 4 the pack kernel,
  * 5 the force evaluation of a step (pack, then the pair kernel beside the
- * bonded and 1-4 kernels), 6 the 1-4 kernel.  Runs on the resident state
+ * bonded and 1-4 kernels), 6 the 1-4 kernel, 7 the list build kernel (with
+ * its flag set/clear launches).  Runs on the resident state
  * (which = 3 advances it); forces are recomputed afterwards. */
 int32_t gm_profile(gm_ctx *ctx, int32_t which, int32_t n_iter, double dt, double *avg_ms);
 /* Runs n_steps resident BAB steps, each bracketed by CUDA events; with
