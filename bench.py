@@ -39,9 +39,9 @@ PHYS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0,
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 # DRAM bytes (read + write) per launch of the FP32 pair kernel per half-list
 # pair, from one ncu capture of the 50k workload at its minimised start
-# (96,405,504 B for 10,067,070 pairs, profiles/pair_kernel_f32_50k_lattice.md);
-# traffic grows with the pair count, so the bench scales it to its own count
-PAIR_TRAFFIC_PER_PAIR = 96_405_504 / 10_067_070
+# (93,724,416 + 3,199,744 B for 10,067,070 pairs); traffic grows with the
+# pair count, so the bench scales it to its own count
+PAIR_TRAFFIC_PER_PAIR = 96_924_160 / 10_067_070
 
 
 def ns_per_day(steps, seconds):
@@ -185,6 +185,12 @@ def run_cuda(args, rank, world):
     t_pair = be.profile("pair", 30) / 1e3
     t_bonded = be.profile("bonded", 30) / 1e3
     t_rebuild = be.profile("rebuild", 5) / 1e3
+    # the other pieces of a step (CUDA events, warm): the 1-4 kernel, the list
+    # build kernel alone, and the whole force evaluation (pack, then the pair
+    # kernel beside the bonded and 1-4 kernels)
+    t_pair14 = be.profile("pair14", 30) / 1e3
+    t_build = be.profile("build", 5) / 1e3
+    t_forces = be.profile("forces", 30) / 1e3
     alg_bytes = 4 * pairs + 52 * N_ATOMS
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_pair / 1e9
@@ -261,7 +267,8 @@ def run_cuda(args, rank, world):
         "steady_state_ns_per_day": round(ns_per_day(min(args.steps, 2000), t_bb), 3),
         "errors_vs_fp64_oracle": errs,
         "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
-                      "list_rebuild": round(t_rebuild * 1e3, 4)},
+                      "pair14": round(t_pair14 * 1e3, 5), "forces": round(t_forces * 1e3, 5),
+                      "list_rebuild": round(t_rebuild * 1e3, 4), "build_kernel": round(t_build * 1e3, 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
                      "peak_source": peak_kind,
