@@ -627,7 +627,7 @@ def main():
         from geodesic_cuda import backend
         if args.config == "ensemble":
             if not args.steps_given:
-                args.steps = 1000
+                args.steps = 5000  # the batched-ensemble workload's own step count
             line = run_ensemble(args)
         elif args.config == "warm_start":
             if not args.steps_given:
