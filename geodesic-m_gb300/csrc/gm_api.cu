@@ -662,7 +662,8 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
 int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
     long long k = seq_forces(c, s, false, c->side, c->n_clusters == 0);
     if (!c->n_clusters) {
-        gm_launch_kick_step(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+        // the closing half-kick is done by the next step's first kernel, or
+        // by finish_steps after the last step
         *count += k;
         return GM_OK;
     }
@@ -709,6 +710,16 @@ int capture_graph(gm_ctx *c, double dt) {
     c->graph_dt = dt;
     c->graph_cap = c->cap;
     c->launches_per_step = count;
+    return GM_OK;
+}
+
+// After the last resident step of a call: the closing half-kick that the
+// unconstrained step leaves to the next step (nothing pending otherwise).
+int finish_steps(gm_ctx *c, double dt) {
+    if (c->n_clusters) return GM_OK;
+    gm_launch_kick_tail(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, c->stream);
+    c->launches++;
+    GM_CUDA(c, cudaGetLastError());
     return GM_OK;
 }
 
@@ -1627,6 +1638,10 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         total += ms;
+        if (which == 3) {
+            rc = finish_steps(c, dt);  // outside the timed span, as after a run
+            if (rc) return rc;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1668,12 +1683,15 @@ int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_ste
     if (rc) return rc;
     rc = ensure_forces(c);
     if (rc) return rc;
-    if (!c->use_graph) return run_direct(c, dt, n_steps);
+    if (!c->use_graph) {
+        rc = run_direct(c, dt, n_steps);
+        return rc ? rc : finish_steps(c, dt);
+    }
     rc = capture_graph(c, dt);
     if (rc) return rc;
     for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
     c->launches += c->launches_per_step * n_steps;
-    return GM_OK;
+    return finish_steps(c, dt);
 }
 
 int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps, void *flush_buf,
@@ -1703,6 +1721,8 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
             GM_CUDA(c, cudaMemsetAsync(flush_buf, (int)((k + 1) & 0xff), (size_t)flush_bytes, c->stream));
     }
     if (c->use_graph) c->launches += c->launches_per_step * n_steps;
+    rc = finish_steps(c, dt);
+    if (rc) return rc;
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     double total = 0.0;
     for (int64_t k = 0; k < n_steps; k++) {

@@ -867,13 +867,21 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
                                         unsigned int *sys_flag, PackArgs pk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int need = 0, bad = 0;
+    // read by every block before the last block updates them
+    const bool err0 = st->error != 0, tail0 = st->tail_pending != 0;
     if (i < n) {
         double np[3];
-        if (!st->error) {
+        if (!err0) {
             const double inv_m = inv_mass[i];
             for (int d = 0; d < 3; d++) {
                 const double f = (double)force[d * n + i] * GM_FIX_INV;
-                const double v = vel[d * n + i] + dt_half * f * inv_m * kForceToAccel;
+                // the previous step's closing half-kick (same forces) when it
+                // is pending, then this step's opening one: two additions in
+                // the order of the separate kernels
+                const double kick = dt_half * f * inv_m * kForceToAccel;
+                double v = vel[d * n + i];
+                if (tail0) v = v + kick;
+                v = v + kick;
                 const double p = pos[d * n + i];
                 dref[d * n + i] = p;
                 np[d] = p + dt * v;
@@ -915,6 +923,37 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
             if (atomicExch(&st->bad_pending, 0u)) atomicOr(&st->error, (unsigned)GM_DEV_NONFINITE_POS);
             const unsigned e = atomicOr(&st->error, 0u);
             if (cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (r && !e) ? 1u : 0u);
+            // the previous step is complete; this one's closing half-kick is
+            // left to the next step's kernel or the finalizer
+            if (!err0) {
+                if (tail0) st->step += 1;
+                st->tail_pending = 1u;
+            }
+        }
+    }
+}
+// The closing half-kick of the last unconstrained resident step and its step
+// count, when pending; the last block clears the flag after every block has
+// read it.
+__global__ void kick_tail_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                                 DevStatus *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool go = st->tail_pending != 0 && st->error == 0;
+    if (i < n && go) {
+        const double inv_m = inv_mass[i];
+        for (int d = 0; d < 3; d++) {
+            const double f = (double)force[d * n + i] * GM_FIX_INV;
+            vel[d * n + i] += dt_half * f * inv_m * kForceToAccel;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(&st->blocks_done, 1u);
+        if (done == gridDim.x - 1) {
+            st->blocks_done = 0;
+            if (go) st->step += 1;
+            st->tail_pending = 0u;
         }
     }
 }
@@ -962,6 +1001,10 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
                                 const PackArgs &pk, cudaStream_t s) {
     kick_drift_check_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, pos, vel, dref, force, inv_mass, dt_half, dt, ref,
                                                               thr_sq, st, cond, atom_sys, sys_flag, pk);
+}
+void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                         DevStatus *st, cudaStream_t s) {
+    kick_tail_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, vel, force, inv_mass, dt_half, st);
 }
 void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s) {

@@ -68,6 +68,8 @@ struct DevStatus {
                                    // error by its last block
     unsigned int max_count;        // largest list length the list build met (sizes a regrowth)
     unsigned int max_layer;        // largest staging (one z layer) length it met
+    unsigned int tail_pending;     // unconstrained resident steps: the last step's closing half-kick
+                                   // is still to do (the next step's first kernel or the finalizer)
 };
 
 struct GridInfo {
@@ -312,6 +314,10 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
                                 const PackArgs &pk, cudaStream_t s);
 void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
+                         DevStatus *st, cudaStream_t s);
+// The closing half-kick and step count of the last unconstrained resident
+// step, when one is pending (a no-op otherwise).
+void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s);
 void gm_launch_kinetic(int n, const double *vel, const double *mass, double *partials, int blocks, double *out,
                        cudaStream_t s);

@@ -376,3 +376,37 @@ def test_resident_runs_bit_identical():
         assert np.array_equal(pos.view(np.uint64), res[0][0].view(np.uint64))
         assert np.array_equal(vel.view(np.uint64), res[0][1].view(np.uint64))
         assert e == res[0][2] and nreb == res[0][3]
+
+
+@pytest.mark.parametrize("precision", [backend.PRECISION_MIXED, backend.PRECISION_FP64])
+def test_resident_unconstrained_steps_equal_trait_loop(precision):
+    """Without constraints the resident step folds each step's closing
+    half-kick into the next step's first kernel (two additions with the same
+    forces, in the same order) and finishes the last one after the loop.
+    The result must equal, bit for bit, the loop of lib.rs:292-323 driven
+    through the trait-level entry points, list rebuilds included."""
+    atoms, topo, state, _ = synth.generate(2000, seed=23, temperature=600.0, relax_iters=200)
+    p = backend.SimParams(precision=precision, box_size=(1000.0,) * 3, periodic=False, r_cutoff=10.0,
+                          r_skin=10.6, r_switch=8.0)
+    dt, n = 0.002, 60
+    res = backend.CudaBackend(atoms, topo, p)
+    pr = np.ascontiguousarray(state.pos.copy())
+    vr = np.ascontiguousarray(state.vel.copy())
+    _, n_reb, _ = res.steps(pr, vr, dt, n)
+    assert n_reb >= 2, n_reb  # the comparison covers rebuilds inside the graph
+    res.close()
+    be = backend.CudaBackend(atoms, topo, p)
+    pos = np.ascontiguousarray(state.pos.copy())
+    vel = np.ascontiguousarray(state.vel.copy())
+    be.build_neighbor_list(pos)
+    f = be.compute_forces(pos).copy()
+    for step in range(n):
+        be.half_kick(vel, f, dt / 2.0)
+        be.geodesic_drift(pos, vel, dt, step)
+        if be.needs_rebuild(pos):
+            be.build_neighbor_list(pos)
+        f = be.compute_forces(pos).copy()
+        be.half_kick(vel, f, dt / 2.0)
+    be.close()
+    assert np.array_equal(pr.view(np.uint64), pos.view(np.uint64))
+    assert np.array_equal(vr.view(np.uint64), vel.view(np.uint64))
