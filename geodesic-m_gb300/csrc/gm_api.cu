@@ -451,6 +451,7 @@ int reset_status(gm_ctx *c) {
     z.shake_sum = c->h_status->shake_sum;
     z.rattle_sum = c->h_status->rattle_sum;
     z.rec_n = c->h_status->rec_n;
+    z.rebuild_base = c->h_status->rebuild_base;
     *c->h_status = z;
     return st_write(c);
 }
@@ -494,11 +495,9 @@ int fill_convergence(gm_ctx *c, bool rattle, gm_convergence *conv) {
                 (unsigned long long)(conv ? conv->step : 0), best, c->p.max_constr_iter);
 }
 
-int check_status(gm_ctx *c, gm_convergence *conv) {
-    GM_CUDA(c, cudaStreamSynchronize(c->stream));
-    GM_CUDA(c, cudaGetLastError());
-    int rc0 = st_read(c);
-    if (rc0) return rc0;
+// The status word as the stream left it, read by the caller into h_status:
+// the reference's error for the first device failure it records.
+int status_result(gm_ctx *c, gm_convergence *conv) {
     const unsigned e = c->h_status->error;
     c->last_shake_T = c->h_status->shake_T;
     c->last_rattle_T = c->h_status->rattle_T;
@@ -520,6 +519,14 @@ int check_status(gm_ctx *c, gm_convergence *conv) {
     if (e & GM_DEV_ITER_MISMATCH)
         return fail(c, GM_ERR_UNSUPPORTED, "constraint cluster iteration counts disagree with the global stop rule");
     return fail(c, GM_ERR_DEVICE, "device status 0x%x", e);
+}
+
+int check_status(gm_ctx *c, gm_convergence *conv) {
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    GM_CUDA(c, cudaGetLastError());
+    int rc0 = st_read(c);
+    if (rc0) return rc0;
+    return status_result(c, conv);
 }
 
 // The list (cap entries per atom) and the list build's staging area (GM_NSEG
@@ -720,6 +727,43 @@ int finish_steps(gm_ctx *c, double dt) {
     gm_launch_kick_tail(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, c->stream);
     c->launches++;
     GM_CUDA(c, cudaGetLastError());
+    return GM_OK;
+}
+
+int run_direct(gm_ctx *c, double dt, int64_t n_steps);
+
+// n resident steps (one graph launch each, or direct launches), then the
+// closing half-kick; nothing waits for the device.
+int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
+    if (!c->use_graph) {
+        int rc = run_direct(c, dt, n_steps);
+        return rc ? rc : finish_steps(c, dt);
+    }
+    int rc = capture_graph(c, dt);
+    if (rc) return rc;
+    for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+    c->launches += c->launches_per_step * n_steps;
+    return finish_steps(c, dt);
+}
+
+// Caller positions into the context.  When the resident forces are current
+// and the caller hands back the resident positions (bit for bit), the forces
+// stay valid; one read of the device's comparison decides.
+int stage_positions(gm_ctx *c, const double *px, const double *py, const double *pz) {
+    if (!c->forces_current) return upload3(c, c->d_pos, px, py, pz);
+    int rc = upload3(c, c->d_dref, px, py, pz);
+    if (rc) return rc;
+    GM_CUDA(c, cudaMemsetAsync(&c->d_status->differs, 0, sizeof(unsigned int), c->stream));
+    gm_launch_differs(c->n, c->d_dref, c->d_pos, &c->d_status->differs, c->stream);
+    c->launches++;
+    GM_CUDA(c, cudaMemcpyAsync(&c->h_status->differs, &c->d_status->differs, sizeof(unsigned int),
+                               cudaMemcpyDeviceToHost, c->stream));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->h_status->differs) {
+        c->forces_current = false;
+        GM_CUDA(c, cudaMemcpyAsync(c->d_pos, c->d_dref, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    }
     return GM_OK;
 }
 
@@ -1683,15 +1727,7 @@ int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_ste
     if (rc) return rc;
     rc = ensure_forces(c);
     if (rc) return rc;
-    if (!c->use_graph) {
-        rc = run_direct(c, dt, n_steps);
-        return rc ? rc : finish_steps(c, dt);
-    }
-    rc = capture_graph(c, dt);
-    if (rc) return rc;
-    for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
-    c->launches += c->launches_per_step * n_steps;
-    return finish_steps(c, dt);
+    return launch_steps(c, dt, n_steps);
 }
 
 int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps, void *flush_buf,
@@ -1746,30 +1782,41 @@ void *gm_stream(gm_ctx *c) { return c ? (void *)c->stream : nullptr; }
 int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double dt,
                  uint64_t first_step, int64_t n_steps, double *fx, double *fy, double *fz, double *energy,
                  int64_t *n_rebuilds, gm_convergence *err) {
-    if (!c) return GM_ERR_INVALID_ARGUMENT;
-    int rc = gm_upload_state(c, px, py, pz, vx, vy, vz);
+    // Two host synchronisations per call: the check whether the caller's
+    // positions are the resident ones (forces stay valid), and the results
+    // with the status word at the end.  The status reset, the step number and
+    // the call's rebuild base are set on the device.
+    if (!c || !(dt > 0) || n_steps < 0) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position");
+    if (!c->d_list) {
+        int rc = ensure_estimated_buffers(c, px, py, pz);
+        if (rc) return rc;
+    }
+    gm_launch_status_reset(c->d_status, 1, first_step, c->stream);
+    c->launches++;
+    int rc = stage_positions(c, px, py, pz);
+    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
+    if (!rc) rc = ensure_forces(c);
+    if (!rc) rc = launch_steps(c, dt, n_steps);
     if (rc) return rc;
-    rc = st_read(c);
-    if (rc) return rc;
-    const unsigned long long r0 = c->h_status->n_rebuilds;
-    rc = gm_run_resident(c, dt, first_step, n_steps);
-    if (rc) return rc;
-    rc = check_status(c, err);
-    const unsigned long long r1 = c->h_status->n_rebuilds;
-    if (n_rebuilds) *n_rebuilds = (int64_t)(r1 - r0);
-    int rc2 = download3(c, c->d_pos, px, py, pz);
-    if (!rc2) rc2 = download3(c, c->d_vel, vx, vy, vz);
-    if (!rc2 && (fx || fy || fz)) {
+    rc = download3(c, c->d_pos, px, py, pz);
+    if (!rc) rc = download3(c, c->d_vel, vx, vy, vz);
+    if (!rc && (fx || fy || fz)) {
         gm_launch_forces_out(c->n, c->d_force, c->d_fout, c->stream);
         c->launches++;
-        rc2 = download3(c, c->d_fout, fx, fy, fz);
+        rc = download3(c, c->d_fout, fx, fy, fz);
     }
-    if (!rc2 && energy) {
+    if (!rc && energy) {
         refresh_energy(c);
         GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
+    GM_CUDA(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
-    return rc ? rc : rc2;
+    GM_CUDA(c, cudaGetLastError());
+    if (n_rebuilds) *n_rebuilds = (int64_t)(c->h_status->n_rebuilds - c->h_status->rebuild_base);
+    const int rs = status_result(c, err);
+    return rs ? rs : rc;
 }
 
 int32_t gm_counters(const gm_ctx *cc, int64_t *out, int64_t n) {

@@ -847,6 +847,19 @@ __global__ void differs_kernel(int n3, const double *a, const double *b, unsigne
     if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(flag, 1u);
 }
 
+__global__ void status_reset_kernel(DevStatus *st, int set_step, unsigned long long step) {
+    DevStatus z{};
+    z.fail_step = ~0ull;
+    z.n_rebuilds = st->n_rebuilds;
+    z.step = set_step ? step : st->step;
+    z.c_steps = st->c_steps;
+    z.shake_sum = st->shake_sum;
+    z.rattle_sum = st->rattle_sum;
+    z.rec_n = st->rec_n;
+    z.rebuild_base = st->n_rebuilds;
+    *st = z;
+}
+
 __global__ void forces_out_kernel(int n3, const long long *force, double *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n3) out[i] = (double)force[i] * GM_FIX_INV;
@@ -1053,6 +1066,9 @@ void gm_launch_kinetic(int n, const double *vel, const double *mass, double *par
     kinetic_final<<<1, 32, 0, s>>>(partials, blocks, out);
 }
 
+void gm_launch_status_reset(DevStatus *st, int set_step, unsigned long long step, cudaStream_t s) {
+    status_reset_kernel<<<1, 1, 0, s>>>(st, set_step, step);
+}
 void gm_launch_differs(int n, const double *a, const double *b, unsigned int *flag, cudaStream_t s) {
     if (n) differs_kernel<<<(3 * n + 255) / 256, 256, 0, s>>>(3 * n, a, b, flag);
 }

@@ -70,6 +70,7 @@ struct DevStatus {
     unsigned int max_layer;        // largest staging (one z layer) length it met
     unsigned int tail_pending;     // unconstrained resident steps: the last step's closing half-kick
                                    // is still to do (the next step's first kernel or the finalizer)
+    unsigned long long rebuild_base;  // n_rebuilds when the current call's status was reset
 };
 
 struct GridInfo {
@@ -323,6 +324,9 @@ void gm_launch_kinetic(int n, const double *vel, const double *mass, double *par
                        cudaStream_t s);
 void gm_launch_forces_out(int n, const long long *force, double *out, cudaStream_t s);
 void gm_launch_differs(int n, const double *a, const double *b, unsigned int *flag, cudaStream_t s);
+// The per-call status reset on the device: counters kept, per-call fields
+// cleared, the step set when set_step, n_rebuilds noted as the call's base.
+void gm_launch_status_reset(DevStatus *st, int set_step, unsigned long long step, cudaStream_t s);
 int gm_check_blocks(int n);
 
 // ---- constraint warm start (gm_mlp.cu) -----------------------------------
