@@ -359,6 +359,7 @@ struct WsFeatureArgs {
     float *feat;                 // [n_constr][12] raw features
     double *scale;               // 2 (1/m_i + 1/m_j) per constraint
     double *t1;                  // first Jacobi step of a cold solve, times scale
+    float4 *unit;                // reference bond direction per constraint (FP32), for the coupling pass
 };
 void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s);
 // lam0[k] = (t1[k] + y_k * t_scale + t_mean) / scale[k] from the raw features

@@ -73,6 +73,9 @@ __global__ void ws_features_kernel(WsFeatureArgs a) {
     f[5] = (float)(a.atom_cstart[i + 1] - a.atom_cstart[i]);
     f[6] = (float)(a.atom_cstart[j + 1] - a.atom_cstart[j]);
     f[7] = (float)t1;
+    float ux, uy, uz;
+    ref_unit(a, k, ux, uy, uz);
+    a.unit[k] = make_float4(ux, uy, uz, 0.f);
 }
 
 // Pass 2: coupling to the other constraints on the constraint's two atoms
@@ -83,8 +86,8 @@ __global__ void ws_coupling_kernel(WsFeatureArgs a) {
     if (k >= a.n_constr) return;
     const int ends[2] = {a.constr_i[k], a.constr_j[k]};
     const float wk = __fadd_rn((float)a.inv_mass[ends[0]], (float)a.inv_mass[ends[1]]);
-    float ux, uy, uz;
-    ref_unit(a, k, ux, uy, uz);
+    const float4 uk = a.unit[k];
+    const float ux = uk.x, uy = uk.y, uz = uk.z;
     float c1 = 0.0f, c2 = 0.0f, cmax = 0.0f, ct = 0.0f;
     for (int e = 0; e < 2; e++) {
         const int at = ends[e];
@@ -95,9 +98,8 @@ __global__ void ws_coupling_kernel(WsFeatureArgs a) {
             const int l = ref >= 0 ? ref : -ref - 1;
             if (l == k) continue;
             const float sl = ref >= 0 ? 1.0f : -1.0f;
-            float vx, vy, vz;
-            ref_unit(a, l, vx, vy, vz);
-            const float cs = dot3f(ux, uy, uz, vx, vy, vz);
+            const float4 ul = a.unit[l];
+            const float cs = dot3f(ux, uy, uz, ul.x, ul.y, ul.z);
             const float wl = __fadd_rn((float)a.inv_mass[a.constr_i[l]], (float)a.inv_mass[a.constr_j[l]]);
             const float coup = __fmul_rn(__fmul_rn(__fdiv_rn(inv_a, wk), cs), __fmul_rn(sk, sl));
             const float tl = (float)a.t1[l];
@@ -115,45 +117,112 @@ __global__ void ws_coupling_kernel(WsFeatureArgs a) {
 }
 
 // Weights into shared memory: matmul weights BF16-rounded, biases as is.
+// 128-bit loads, four in flight per thread before their stores (every block
+// loads the 20 KB, so the latency of one load at a time would dominate a
+// short kernel).  The sections start on 16-byte boundaries (offsets are
+// multiples of four floats), and so do the shared arrays.
+__device__ __forceinline__ float4 bf4(float4 v) { return make_float4(bf(v.x), bf(v.y), bf(v.z), bf(v.w)); }
+__device__ __forceinline__ void store_weight4(int o, float4 v, float *sW1, float *sb1, float *sW2, float *sb2,
+                                              float *sw3) {
+    if (o < GM_WS_OFF_B1) *reinterpret_cast<float4 *>(sW1 + o) = bf4(v);
+    else if (o < GM_WS_OFF_W2) *reinterpret_cast<float4 *>(sb1 + o - GM_WS_OFF_B1) = v;
+    else if (o < GM_WS_OFF_B2) *reinterpret_cast<float4 *>(sW2 + o - GM_WS_OFF_W2) = bf4(v);
+    else if (o < GM_WS_OFF_W3) *reinterpret_cast<float4 *>(sb2 + o - GM_WS_OFF_B2) = v;
+    else *reinterpret_cast<float4 *>(sw3 + o - GM_WS_OFF_W3) = bf4(v);
+}
 __device__ void load_weights(const float *P, float *sW1, float *sb1, float *sW2, float *sb2, float *sw3, float *sb3) {
-    for (int t = threadIdx.x; t < kIn * kH; t += blockDim.x) sW1[t] = bf(P[GM_WS_OFF_W1 + t]);
-    for (int t = threadIdx.x; t < kH * kH; t += blockDim.x) sW2[t] = bf(P[GM_WS_OFF_W2 + t]);
-    for (int t = threadIdx.x; t < kH; t += blockDim.x) {
-        sb1[t] = P[GM_WS_OFF_B1 + t];
-        sb2[t] = P[GM_WS_OFF_B2 + t];
-        sw3[t] = bf(P[GM_WS_OFF_W3 + t]);
+    const float4 *P4 = reinterpret_cast<const float4 *>(P);
+    constexpr int kW4 = GM_WS_OFF_B3 / 4;
+    for (int t0 = threadIdx.x; t0 < kW4; t0 += 4 * blockDim.x) {
+        float4 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int t = t0 + r * (int)blockDim.x;
+            v[r] = t < kW4 ? __ldg(P4 + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int t = t0 + r * (int)blockDim.x;
+            if (t < kW4) store_weight4(4 * t, v[r], sW1, sb1, sW2, sb2, sw3);
+        }
     }
     if (threadIdx.x == 0) *sb3 = P[GM_WS_OFF_B3];
 }
 
+// Inference: four threads per constraint (a quad), thread q owning hidden
+// units [16q, 16q + 16) of both layers.  Weights are read from shared memory
+// 16 at a time (four 128-bit loads) into 16 independent accumulations; the
+// first layer's activations reach the other threads of the quad by shuffles.
+// Every sum keeps the ascending order of the one-thread form (each unit over
+// its inputs in index order; the output over the units in index order, passed
+// along the quad), so the result equals it.
 __global__ void __launch_bounds__(128) ws_infer_kernel(int n, const float *__restrict__ feat,
                                                        const float *__restrict__ P, const float *__restrict__ norm,
                                                        const double *__restrict__ scale,
                                                        const double *__restrict__ t1, double *lam0, float *y_out) {
-    __shared__ float sW1[kIn * kH], sW2[kH * kH], sb1[kH], sb2[kH], sw3[kH], sb3, snorm[GM_WS_NNORM];
+    __shared__ __align__(16) float sW1[kIn * kH];
+    __shared__ __align__(16) float sW2[kH * kH];
+    __shared__ __align__(16) float sb1[kH];
+    __shared__ __align__(16) float sb2[kH];
+    __shared__ __align__(16) float sw3[kH];
+    __shared__ float sb3, snorm[GM_WS_NNORM];
     load_weights(P, sW1, sb1, sW2, sb2, sw3, &sb3);
     if (threadIdx.x < GM_WS_NNORM) snorm[threadIdx.x] = norm[threadIdx.x];
     __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    const int q = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
+    const int k = blockIdx.x * (blockDim.x / 4) + (threadIdx.x >> 2);
+    const bool live = k < n;  // the quad of a constraint past n still joins the shuffles
+    const int o0 = 16 * q;
     float x[kIn];
 #pragma unroll
-    for (int f = 0; f < kIn; f++) x[f] = bf((feat[(size_t)k * kIn + f] - snorm[f]) / snorm[kIn + f]);
-    float a1[kH];
+    for (int f = 0; f < kIn; f++) x[f] = live ? bf((feat[(size_t)k * kIn + f] - snorm[f]) / snorm[kIn + f]) : 0.f;
+    float z[16];
 #pragma unroll
-    for (int o = 0; o < kH; o++) {
-        float z = sb1[o];
+    for (int j = 0; j < 16; j++) z[j] = sb1[o0 + j];
 #pragma unroll
-        for (int f = 0; f < kIn; f++) z = fmaf(x[f], sW1[f * kH + o], z);
-        a1[o] = bf(z * sigmoid(z));
+    for (int f = 0; f < kIn; f++) {
+        const float4 *w = reinterpret_cast<const float4 *>(sW1 + f * kH + o0);
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const float4 w4 = w[v];
+            z[4 * v] = fmaf(x[f], w4.x, z[4 * v]);
+            z[4 * v + 1] = fmaf(x[f], w4.y, z[4 * v + 1]);
+            z[4 * v + 2] = fmaf(x[f], w4.z, z[4 * v + 2]);
+            z[4 * v + 3] = fmaf(x[f], w4.w, z[4 * v + 3]);
+        }
     }
+    float a1[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) a1[j] = bf(z[j] * sigmoid(z[j]));
+#pragma unroll
+    for (int j = 0; j < 16; j++) z[j] = sb2[o0 + j];
+#pragma unroll
+    for (int src = 0; src < 4; src++) {
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+            const float a = __shfl_sync(0xffffffffu, a1[jj], base + src);  // unit 16 src + jj
+            const float4 *w = reinterpret_cast<const float4 *>(sW2 + (16 * src + jj) * kH + o0);
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const float4 w4 = w[v];
+                z[4 * v] = fmaf(a, w4.x, z[4 * v]);
+                z[4 * v + 1] = fmaf(a, w4.y, z[4 * v + 1]);
+                z[4 * v + 2] = fmaf(a, w4.z, z[4 * v + 2]);
+                z[4 * v + 3] = fmaf(a, w4.w, z[4 * v + 3]);
+            }
+        }
+    }
+    // the output: units 0..63 in order, thread 0's sixteen, then thread 1's, ...
     float y = sb3;
-    for (int o = 0; o < kH; o++) {
-        float z = sb2[o];
 #pragma unroll
-        for (int q = 0; q < kH; q++) z = fmaf(a1[q], sW2[q * kH + o], z);
-        y = fmaf(bf(z * sigmoid(z)), sw3[o], y);
+    for (int src = 0; src < 4; src++) {
+        if (q == src) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) y = fmaf(bf(z[j] * sigmoid(z[j])), sw3[o0 + j], y);
+        }
+        y = __shfl_sync(0xffffffffu, y, base + src);
     }
+    if (!live || q != 0) return;
     if (y_out) y_out[k] = y;
     if (lam0) lam0[k] = (t1[k] + ((double)y * (double)snorm[25] + (double)snorm[24])) / scale[k];
 }
@@ -373,7 +442,7 @@ void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s) {
 void gm_launch_ws_infer(int n, const float *feat, const float *params, const float *norm, const double *scale,
                         const double *t1, double *lam0, float *y_out, cudaStream_t s) {
     if (n == 0) return;
-    ws_infer_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, feat, params, norm, scale, t1, lam0, y_out);
+    ws_infer_kernel<<<(n + 31) / 32, 128, 0, s>>>(n, feat, params, norm, scale, t1, lam0, y_out);
 }
 
 void gm_launch_ws_record(int n_constr, const float *feat, const double *lam_sum, const double *scale, const double *t1,
