@@ -28,6 +28,9 @@ constexpr int kRow = kH + 1;  // padded shared-memory row (conflict-free per-sam
 
 __device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-z)); }
+// The same function for inference: correctly rounded reciprocal of 1 + exp(-z)
+// (equal to the division above), no division subroutine.
+__device__ __forceinline__ float sigmoid_rcp(float z) { return __frcp_rn(1.0f + expf(-z)); }
 
 __device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by, double bz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
@@ -149,41 +152,48 @@ __device__ void load_weights(const float *P, float *sW1, float *sb1, float *sW2,
     if (threadIdx.x == 0) *sb3 = P[GM_WS_OFF_B3];
 }
 
-// Inference: four threads per constraint (a quad), thread q owning hidden
-// units [16q, 16q + 16) of both layers.  Weights are read from shared memory
-// 16 at a time (four 128-bit loads) into 16 independent accumulations; the
-// first layer's activations reach the other threads of the quad by shuffles.
-// Every sum keeps the ascending order of the one-thread form (each unit over
-// its inputs in index order; the output over the units in index order, passed
-// along the quad), so the result equals it.
-__global__ void __launch_bounds__(128) ws_infer_kernel(int n, const float *__restrict__ feat,
+// Inference: TPC threads per constraint, thread q owning the U = 64 / TPC
+// hidden units [U q, U q + U) of both layers.  Weights are read from shared
+// memory four at a time (128-bit loads) into U independent accumulations; the
+// first layer's activations reach the other threads of the group by
+// shuffles.  Every sum keeps the ascending order of the one-thread form (each
+// unit over its inputs in index order; the output over the units in index
+// order, passed along the group).  Inputs are standardised with the
+// correctly rounded reciprocal of the spread (within an ulp of the division,
+// before their BF16 rounding) and the SiLU's 1 / (1 + exp(-z)) is a
+// correctly rounded reciprocal (equal to the division).
+template <int TPC>
+__global__ void __launch_bounds__(256) ws_infer_kernel(int n, const float *__restrict__ feat,
                                                        const float *__restrict__ P, const float *__restrict__ norm,
                                                        const double *__restrict__ scale,
                                                        const double *__restrict__ t1, double *lam0, float *y_out) {
+    constexpr int U = kH / TPC;
+    static_assert(U % 4 == 0, "units per thread in whole 128-bit loads");
     __shared__ __align__(16) float sW1[kIn * kH];
     __shared__ __align__(16) float sW2[kH * kH];
     __shared__ __align__(16) float sb1[kH];
     __shared__ __align__(16) float sb2[kH];
     __shared__ __align__(16) float sw3[kH];
-    __shared__ float sb3, snorm[GM_WS_NNORM];
+    __shared__ float sb3, snorm[GM_WS_NNORM], sinv[kIn];
     load_weights(P, sW1, sb1, sW2, sb2, sw3, &sb3);
     if (threadIdx.x < GM_WS_NNORM) snorm[threadIdx.x] = norm[threadIdx.x];
+    if (threadIdx.x < kIn) sinv[threadIdx.x] = __frcp_rn(norm[kIn + threadIdx.x]);
     __syncthreads();
-    const int q = threadIdx.x & 3, base = (threadIdx.x & 31) & ~3;
-    const int k = blockIdx.x * (blockDim.x / 4) + (threadIdx.x >> 2);
-    const bool live = k < n;  // the quad of a constraint past n still joins the shuffles
-    const int o0 = 16 * q;
+    const int q = threadIdx.x % TPC, base = (threadIdx.x & 31) - q;
+    const int k = blockIdx.x * (blockDim.x / TPC) + threadIdx.x / TPC;
+    const bool live = k < n;  // a group past n still joins the shuffles
+    const int o0 = U * q;
     float x[kIn];
 #pragma unroll
-    for (int f = 0; f < kIn; f++) x[f] = live ? bf((feat[(size_t)k * kIn + f] - snorm[f]) / snorm[kIn + f]) : 0.f;
-    float z[16];
+    for (int f = 0; f < kIn; f++) x[f] = live ? bf((feat[(size_t)k * kIn + f] - snorm[f]) * sinv[f]) : 0.f;
+    float z[U];
 #pragma unroll
-    for (int j = 0; j < 16; j++) z[j] = sb1[o0 + j];
+    for (int j = 0; j < U; j++) z[j] = sb1[o0 + j];
 #pragma unroll
     for (int f = 0; f < kIn; f++) {
         const float4 *w = reinterpret_cast<const float4 *>(sW1 + f * kH + o0);
 #pragma unroll
-        for (int v = 0; v < 4; v++) {
+        for (int v = 0; v < U / 4; v++) {
             const float4 w4 = w[v];
             z[4 * v] = fmaf(x[f], w4.x, z[4 * v]);
             z[4 * v + 1] = fmaf(x[f], w4.y, z[4 * v + 1]);
@@ -191,19 +201,19 @@ __global__ void __launch_bounds__(128) ws_infer_kernel(int n, const float *__res
             z[4 * v + 3] = fmaf(x[f], w4.w, z[4 * v + 3]);
         }
     }
-    float a1[16];
+    float a1[U];
 #pragma unroll
-    for (int j = 0; j < 16; j++) a1[j] = bf(z[j] * sigmoid(z[j]));
+    for (int j = 0; j < U; j++) a1[j] = bf(z[j] * sigmoid_rcp(z[j]));
 #pragma unroll
-    for (int j = 0; j < 16; j++) z[j] = sb2[o0 + j];
+    for (int j = 0; j < U; j++) z[j] = sb2[o0 + j];
 #pragma unroll
-    for (int src = 0; src < 4; src++) {
+    for (int src = 0; src < TPC; src++) {
 #pragma unroll
-        for (int jj = 0; jj < 16; jj++) {
-            const float a = __shfl_sync(0xffffffffu, a1[jj], base + src);  // unit 16 src + jj
-            const float4 *w = reinterpret_cast<const float4 *>(sW2 + (16 * src + jj) * kH + o0);
+        for (int jj = 0; jj < U; jj++) {
+            const float a = __shfl_sync(0xffffffffu, a1[jj], base + src);  // unit U src + jj
+            const float4 *w = reinterpret_cast<const float4 *>(sW2 + (U * src + jj) * kH + o0);
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
+            for (int v = 0; v < U / 4; v++) {
                 const float4 w4 = w[v];
                 z[4 * v] = fmaf(a, w4.x, z[4 * v]);
                 z[4 * v + 1] = fmaf(a, w4.y, z[4 * v + 1]);
@@ -212,13 +222,13 @@ __global__ void __launch_bounds__(128) ws_infer_kernel(int n, const float *__res
             }
         }
     }
-    // the output: units 0..63 in order, thread 0's sixteen, then thread 1's, ...
+    // the output: units 0..63 in order, thread 0's, then thread 1's, ...
     float y = sb3;
 #pragma unroll
-    for (int src = 0; src < 4; src++) {
+    for (int src = 0; src < TPC; src++) {
         if (q == src) {
 #pragma unroll
-            for (int j = 0; j < 16; j++) y = fmaf(bf(z[j] * sigmoid(z[j])), sw3[o0 + j], y);
+            for (int j = 0; j < U; j++) y = fmaf(bf(z[j] * sigmoid_rcp(z[j])), sw3[o0 + j], y);
         }
         y = __shfl_sync(0xffffffffu, y, base + src);
     }
@@ -442,7 +452,9 @@ void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s) {
 void gm_launch_ws_infer(int n, const float *feat, const float *params, const float *norm, const double *scale,
                         const double *t1, double *lam0, float *y_out, cudaStream_t s) {
     if (n == 0) return;
-    ws_infer_kernel<<<(n + 31) / 32, 128, 0, s>>>(n, feat, params, norm, scale, t1, lam0, y_out);
+    constexpr int kTPC = 16, kThreads = 256, kPerBlock = kThreads / kTPC;
+    ws_infer_kernel<kTPC><<<(n + kPerBlock - 1) / kPerBlock, kThreads, 0, s>>>(n, feat, params, norm, scale, t1, lam0,
+                                                                              y_out);
 }
 
 void gm_launch_ws_record(int n_constr, const float *feat, const double *lam_sum, const double *scale, const double *t1,
