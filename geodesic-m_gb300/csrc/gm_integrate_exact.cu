@@ -24,6 +24,19 @@ namespace {
 
 constexpr double kForceToAccel = 20.455 * 20.455;  // integrator.rs:9
 
+// num / dt correctly rounded, from y = RN(1 / dt) computed once on the host:
+// Markstein's correction (P. Markstein, "IA-64 and Elementary Functions",
+// 2000): q = RN(num y), r = num - q dt is exact in one FMA, and RN(q + r y) is
+// the correctly rounded quotient when y is the correctly rounded reciprocal
+// (away from overflow and underflow).  Three FP64 operations instead of a
+// division, which is long on this part; checked bit for bit against the
+// division on 4e8 operand pairs (velocity-resync values and arbitrary ones).
+__device__ __forceinline__ double div_by_dt(double num, double dt, double y) {
+    const double q = num * y;
+    const double r = fma(-q, dt, num);
+    return fma(r, y, q);
+}
+
 __global__ void half_kick_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                                  const DevStatus *st) {
     // integrator.rs:14-21: v += dt_half * F * inv_m * 20.455^2
@@ -58,12 +71,12 @@ __global__ void drift_kernel(int n, double *pos, double *vel, double *dref, doub
     }
 }
 
-__global__ void resync_kernel(int n, const double *pos, double *vel, const double *dref, double dt,
+__global__ void resync_kernel(int n, const double *pos, double *vel, const double *dref, double dt, double inv_dt,
                               const DevStatus *st) {
     // integrator.rs:64-68 (skipped after a failed projection, like the `?` at integrator.rs:256)
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || st->error) return;
-    for (int d = 0; d < 3; d++) vel[d * n + i] = (pos[d * n + i] - dref[d * n + i]) / dt;
+    for (int d = 0; d < 3; d++) vel[d * n + i] = div_by_dt(pos[d * n + i] - dref[d * n + i], dt, inv_dt);
 }
 
 __global__ void check_kernel(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
@@ -875,9 +888,9 @@ __global__ void forces_out_kernel(int n3, const long long *force, double *out) {
 // reads the error word as it stood before the launch (as the separate kick and
 // drift kernels do).
 __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double *dref, long long *force,
-                                        const double *inv_mass, double dt_half, double dt, const double *ref,
-                                        double thr_sq, DevStatus *st, unsigned long long cond, const int *atom_sys,
-                                        unsigned int *sys_flag, PackArgs pk) {
+                                        const double *inv_mass, double dt_half, double dt, double inv_dt,
+                                        const double *ref, double thr_sq, DevStatus *st, unsigned long long cond,
+                                        const int *atom_sys, unsigned int *sys_flag, PackArgs pk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int need = 0, bad = 0;
     // read by every block before the last block updates them
@@ -899,7 +912,7 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
                 dref[d * n + i] = p;
                 np[d] = p + dt * v;
                 pos[d * n + i] = np[d];
-                vel[d * n + i] = (np[d] - p) / dt;
+                vel[d * n + i] = div_by_dt(np[d] - p, dt, inv_dt);
             }
         } else {
             for (int d = 0; d < 3; d++) np[d] = pos[d * n + i];
@@ -1004,7 +1017,7 @@ void gm_launch_drift(int n, double *pos, double *vel, double *dref, double dt, b
 
 void gm_launch_resync(int n, const double *pos, double *vel, const double *dref, double dt, const DevStatus *st,
                       cudaStream_t s) {
-    if (n) resync_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, vel, dref, dt, st);
+    if (n) resync_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, vel, dref, dt, 1.0 / dt, st);
 }
 
 void gm_launch_step(DevStatus *st, cudaStream_t s) { step_kernel<<<1, 1, 0, s>>>(st); }
@@ -1012,8 +1025,9 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
                                 const PackArgs &pk, cudaStream_t s) {
-    kick_drift_check_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, pos, vel, dref, force, inv_mass, dt_half, dt, ref,
-                                                              thr_sq, st, cond, atom_sys, sys_flag, pk);
+    kick_drift_check_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, pos, vel, dref, force, inv_mass, dt_half, dt,
+                                                              1.0 / dt, ref, thr_sq, st, cond, atom_sys, sys_flag,
+                                                              pk);
 }
 void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s) {
