@@ -389,8 +389,7 @@ int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branc
         cudaEventRecord(c->ev_fork, s);
         cudaStreamWaitEvent(branch, c->ev_fork, 0);
     }
-    gm_launch_bonded(fa, c->fp64, sb);
-    gm_launch_pair14(fa, c->fp64, sb);
+    gm_launch_bonded_pair14(fa, c->fp64, sb);
     gm_launch_pair(fa, c->fp64, s);
     if (fork) {
         cudaEventRecord(c->ev_join, branch);
@@ -398,7 +397,7 @@ int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branc
     }
     if (energy) gm_launch_energy(fa, s);
     c->energy_stale = !energy;
-    return (packed ? 0 : 1) + (c->bonded_blocks ? 1 : 0) + 1 + (c->blocks14 ? 1 : 0) + (energy ? 1 : 0);
+    return (packed ? 0 : 1) + (c->bonded_blocks || c->blocks14 ? 1 : 0) + 1 + (energy ? 1 : 0);
 }
 
 PackArgs pack_args(gm_ctx *c) {
@@ -623,9 +622,15 @@ int do_build(gm_ctx *c, bool all = true) {
     return fail(c, GM_ERR_LIST_OVERFLOW, "neighbour list capacity could not be sized");
 }
 
+// Host rows in one contiguous x|y|z block (the caller's 3 x N array) go in
+// one copy; separate rows in three.
 int upload3(gm_ctx *c, double *dst, const double *x, const double *y, const double *z) {
     const size_t b = sizeof(double) * (size_t)c->n;
     if (!c->n) return GM_OK;
+    if (y == x + c->n && z == y + c->n) {
+        GM_CUDA(c, cudaMemcpyAsync(dst, x, 3 * b, cudaMemcpyHostToDevice, c->stream));
+        return GM_OK;
+    }
     GM_CUDA(c, cudaMemcpyAsync(dst, x, b, cudaMemcpyHostToDevice, c->stream));
     GM_CUDA(c, cudaMemcpyAsync(dst + c->n, y, b, cudaMemcpyHostToDevice, c->stream));
     GM_CUDA(c, cudaMemcpyAsync(dst + 2 * c->n, z, b, cudaMemcpyHostToDevice, c->stream));
@@ -635,6 +640,10 @@ int upload3(gm_ctx *c, double *dst, const double *x, const double *y, const doub
 int download3(gm_ctx *c, const double *src, double *x, double *y, double *z) {
     const size_t b = sizeof(double) * (size_t)c->n;
     if (!c->n) return GM_OK;
+    if (x && y == x + c->n && z == y + c->n) {
+        GM_CUDA(c, cudaMemcpyAsync(x, src, 3 * b, cudaMemcpyDeviceToHost, c->stream));
+        return GM_OK;
+    }
     if (x) GM_CUDA(c, cudaMemcpyAsync(x, src, b, cudaMemcpyDeviceToHost, c->stream));
     if (y) GM_CUDA(c, cudaMemcpyAsync(y, src + c->n, b, cudaMemcpyDeviceToHost, c->stream));
     if (z) GM_CUDA(c, cudaMemcpyAsync(z, src + 2 * c->n, b, cudaMemcpyDeviceToHost, c->stream));

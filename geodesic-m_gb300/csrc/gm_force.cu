@@ -262,9 +262,9 @@ __device__ __forceinline__ float gm_atan2(float y, float x) { return atan2f(y, x
 __device__ __forceinline__ double gm_atan2(double y, double x) { return atan2(y, x); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
+__device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
     constexpr bool kMixed = sizeof(T) == sizeof(float);
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blk * blockDim.x + threadIdx.x;
     const int n = a.n;
     double e = 0.0;
     unsigned bad = 0;
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
         if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.epart_bonded[blockIdx.x] = se[0];
+    if (threadIdx.x == 0) a.epart_bonded[blk] = se[0];
     if (a.e_sys) gm_add_sys_energy(a.e_sys, first >= 0 ? a.atom_sys[first] : -1, e);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
@@ -416,8 +416,8 @@ __global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) {
 // Scaled 1-4 pairs (beyond the reference): unswitched, no cutoff; LJ scaled by
 // scale14_lj, Coulomb by scale14_coul.  FP64 arithmetic, few pairs.
 template <bool MIXED>
-__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
+    const int t = blk * blockDim.x + threadIdx.x;
     const int n = a.n;
     double e = 0.0;
     unsigned bad = 0;
@@ -481,10 +481,22 @@ __global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) {
         if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.epart14[blockIdx.x] = se[0];
+    if (threadIdx.x == 0) a.epart14[blk] = se[0];
     if (a.e_sys) gm_add_sys_energy(a.e_sys, first >= 0 ? a.atom_sys[first] : -1, e);
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) { bonded_block<T>(a, blockIdx.x); }
+template <bool MIXED>
+__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) { pair14_block<MIXED>(a, blockIdx.x); }
+// Both in one launch: the first bonded_blocks blocks take the bonded terms,
+// the rest the 1-4 pairs (independent work; integer force sums).
+template <typename T, bool MIXED>
+__global__ void __launch_bounds__(256) bonded_pair14_kernel(ForceArgs a) {
+    if ((int)blockIdx.x < a.bonded_blocks) bonded_block<T>(a, blockIdx.x);
+    else pair14_block<MIXED>(a, blockIdx.x - a.bonded_blocks);
 }
 
 // Fixed-order sum of all energy partials (pair groups, bonded blocks, 1-4
@@ -550,6 +562,13 @@ void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.bonded_blocks == 0) return;
     if (fp64) bonded_kernel<double><<<a.bonded_blocks, 256, 0, s>>>(a);
     else bonded_kernel<float><<<a.bonded_blocks, 256, 0, s>>>(a);
+}
+
+void gm_launch_bonded_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {
+    const int blocks = a.bonded_blocks + a.blocks14;
+    if (blocks == 0) return;
+    if (fp64) bonded_pair14_kernel<double, false><<<blocks, 256, 0, s>>>(a);
+    else bonded_pair14_kernel<float, true><<<blocks, 256, 0, s>>>(a);
 }
 
 void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {

@@ -247,6 +247,8 @@ struct ForceArgs {
 void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s);
 void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s);
 void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s);
+// the bonded terms and the 1-4 pairs in one launch
+void gm_launch_bonded_pair14(const ForceArgs &a, bool fp64, cudaStream_t s);
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s);
 int gm_bonded_blocks(int n_bonds, int n_angles, int n_diheds);
 
