@@ -983,21 +983,6 @@ __global__ void kick_tail_kernel(int n, double *vel, const long long *force, con
         }
     }
 }
-// half_kick_kernel + step_kernel for systems without constraints (the step
-// counter is the only work step_kernel does for them)
-__global__ void kick_step_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
-                                 DevStatus *st) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool err = st->error != 0;
-    if (i < n && !err) {
-        const double inv_m = inv_mass[i];
-        for (int d = 0; d < 3; d++) {
-            const double f = (double)force[d * n + i] * GM_FIX_INV;
-            vel[d * n + i] += dt_half * f * inv_m * kForceToAccel;
-        }
-    }
-    if (i == 0 && !err) st->step += 1;
-}
 int gm_check_blocks(int n) { return n > 0 ? (n + 255) / 256 : 1; }
 
 void gm_launch_half_kick(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
@@ -1032,10 +1017,6 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
 void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          DevStatus *st, cudaStream_t s) {
     kick_tail_kernel<<<gm_check_blocks(n), 256, 0, s>>>(n, vel, force, inv_mass, dt_half, st);
-}
-void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
-                         DevStatus *st, cudaStream_t s) {
-    kick_step_kernel<<<n > 0 ? (n + 255) / 256 : 1, 256, 0, s>>>(n, vel, force, inv_mass, dt_half, st);
 }
 
 void gm_launch_check(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,

@@ -295,9 +295,10 @@ void gm_launch_shake_prepare(const ClusterArgs &c, int n_atoms, const double *dr
 int gm_launch_shake_solve(const ClusterArgs &c, int n_atoms, double *pos, cudaStream_t s);
 void gm_launch_rattle(const ClusterArgs &c, int n_atoms, const double *pos, double *vel, cudaStream_t s);
 void gm_launch_step(DevStatus *st, cudaStream_t s);
-// Unconstrained step: half-kick + drift (with the velocity resync) + rebuild
-// check in one launch, and half-kick + step counter in one launch.  Each atom
-// gets the same operations in the same order as the separate kernels.
+// Unconstrained step: half-kicks (the previous step's closing one and this
+// step's opening one) + drift (with the velocity resync) + rebuild check +
+// coordinate pack in one launch.  Each atom gets the same operations in the
+// same order as the separate kernels.
 // The pack kernel's per-atom work (FP32 (hi, lo) copies relative to the
 // system's grid origin, FP64 copies in FP64 mode, forces cleared), done by the
 // fused step kernel for the force evaluation that follows it.
@@ -316,8 +317,6 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
                                 const PackArgs &pk, cudaStream_t s);
-void gm_launch_kick_step(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
-                         DevStatus *st, cudaStream_t s);
 // The closing half-kick and step count of the last unconstrained resident
 // step, when one is pending (a no-op otherwise).
 void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
