@@ -134,8 +134,9 @@ def lib():
         L.gm_kinetic_energy.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.gm_n_threads.argtypes = [C.c_void_p]
         L.gm_get_pairs.argtypes = [C.c_void_p, C.c_int64, _u32p, _u32p, P(C.c_int64)]
-        L.gm_steps.argtypes = [C.c_void_p] + [_f64p] * 6 + [C.c_double, C.c_uint64, C.c_int64] + [_f64p] * 4 + [
-            P(C.c_int64), P(GmConvergence)]
+        # row pointers as plain addresses: a call per step stays cheap
+        L.gm_steps.argtypes = [C.c_void_p] + [C.c_void_p] * 6 + [C.c_double, C.c_uint64, C.c_int64] + [
+            C.c_void_p] * 3 + [_f64p, P(C.c_int64), P(GmConvergence)]
         L.gm_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_int64]
         L.gm_upload_state.argtypes = [C.c_void_p] + [_f64p] * 6
         L.gm_download_state.argtypes = [C.c_void_p] + [_f64p] * 6
@@ -193,6 +194,14 @@ def build_pairs_static(pos_ptr, n_atoms, excl_start_ptr, excl_ptr, params: SimPa
 
 def _p(a, ct=C.c_double):
     return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _row_addrs(a):
+    """Addresses of the three rows of a C-contiguous float64 (3, N) array."""
+    assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape[0] == 3, "expect C-contiguous float64 (3, N)"
+    base = a.__array_interface__["data"][0]
+    step = a.strides[0]
+    return base, base + step, base + 2 * step
 
 
 def _rows(a):
@@ -265,6 +274,7 @@ class CudaBackend:
             raise BackendError(st.value, "gm_create failed")
         self._forces = np.zeros((3, self.n))
         self._energy = 0.0
+        self._steps_out = None  # reused gm_steps out-parameters
 
     def autotune(self, reps=5):
         """Pick the FP32 pair kernel's split, block size and grid by timing
@@ -372,13 +382,17 @@ class CudaBackend:
     def steps(self, pos, vel, dt, n_steps, first_step=0, want_forces=False):
         """Device-resident BAB + RATTLE steps (lib.rs:292-323), state in place.
         Returns (potential energy, list rebuilds, forces or None)."""
-        conv = GmConvergence()
-        e = C.c_double()
-        nr = C.c_int64()
+        out = self._steps_out
+        if out is None:
+            e, nr, conv = C.c_double(), C.c_int64(), GmConvergence()
+            out = self._steps_out = (e, nr, conv, C.byref(e), C.byref(nr), C.byref(conv))
+        e, nr, conv, e_ref, nr_ref, conv_ref = out
         f = np.zeros((3, self.n)) if want_forces else None
-        fr = _rows(f) if want_forces else (None, None, None)
-        self._check(lib().gm_steps(self._h, *_rows(pos), *_rows(vel), dt, first_step, n_steps, *fr, C.byref(e),
-                                   C.byref(nr), C.byref(conv)), conv)
+        fr = _row_addrs(f) if want_forces else (None, None, None)
+        rc = lib().gm_steps(self._h, *_row_addrs(pos), *_row_addrs(vel), dt, first_step, n_steps, *fr, e_ref,
+                            nr_ref, conv_ref)
+        if rc != GM_OK:
+            self._check(rc, GmConvergence.from_buffer_copy(conv))
         self._energy = e.value
         return e.value, nr.value, f
 
