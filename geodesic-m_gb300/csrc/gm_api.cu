@@ -367,9 +367,9 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
     gm_launch_pack(a, c->fp64, s);
     gm_launch_build(a, s);
     gm_launch_flags(a, false, s);
-    // [flags], wrap or bbox, grid, clear cells, assign, 3 scan kernels,
-    // scatter, rank, pack, build, clear flags
-    return (all ? 1 : 0) + 12 + (a.periodic || a.n > 0 ? 1 : 0);
+    // [flags], wrap or bbox, grid (clears the cells), assign, scan, scatter,
+    // rank, pack, build, clear flags
+    return (all ? 1 : 0) + 9 + (a.periodic || a.n > 0 ? 1 : 0);
 }
 
 // Force evaluation at the resident positions.  With a branch stream the

@@ -129,6 +129,7 @@ __global__ void grid_kernel(ListArgs a, int blocks) {
         red[v][threadIdx.x] = acc;
     }
     __syncthreads();
+    __shared__ int s_ncell;
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
         if (threadIdx.x < k)
             for (int v = 0; v < 9; v++) {
@@ -138,7 +139,7 @@ __global__ void grid_kernel(ListArgs a, int blocks) {
             }
         __syncthreads();
     }
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x == 0) {
     GridInfo *g = a.grid + sys;
     const int n_atoms = a.sys_atom_off[sys + 1] - a.sys_atom_off[sys];
     const int max_cells = a.sys_cell_off[sys + 1] - a.sys_cell_off[sys] - 1;
@@ -199,6 +200,15 @@ __global__ void grid_kernel(ListArgs a, int blocks) {
     }
     g->ncell = nc[0] * nc[1] * nc[2];  // <= max_cells by construction
     atomicAdd(&a.status->n_rebuilds, 1ull);
+    s_ncell = min(g->ncell, max_cells);
+    }
+    // the cells the new grid uses (the only ones assign and the scan touch)
+    __syncthreads();
+    const int c0 = a.sys_cell_off[sys];
+    for (int c = c0 + threadIdx.x; c < c0 + s_ncell; c += blockDim.x) {
+        a.cell_count[c] = 0;
+        a.cell_cursor[c] = 0;
+    }
 }
 
 // Clears the cells the system's new grid uses (the only ones assign and the
@@ -277,6 +287,33 @@ __device__ __forceinline__ int sys_ncell(const ListArgs &a, int s) {
     return min(a.grid[s].ncell, max_cells);
 }
 
+// Exclusive scan of each system's cell counts into cell_start[0..ncell], one
+// block per system walking its cells in chunks of 4096 with a running carry
+// (a few chunks for the grids of these systems).
+__global__ void __launch_bounds__(1024) scan_cells_kernel(ListArgs a) {
+    __shared__ int warp_sums[32];
+    const int s = blockIdx.x;
+    if (!a.sys_flag[s]) return;
+    const int ncell = sys_ncell(a, s), coff = a.sys_cell_off[s];
+    int carry = 0;
+    for (int base = 0; base <= ncell; base += 4 * (int)blockDim.x) {
+        const int i0 = base + 4 * (int)threadIdx.x;
+        int v[4], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[k] = i0 + k < ncell ? a.cell_count[coff + i0 + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = carry + block_exclusive_scan(sum, warp_sums, total);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (i0 + k <= ncell) a.cell_start[coff + i0 + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+}
 __global__ void scan_local_kernel(ListArgs a) {
     __shared__ int warp_sums[32];
     const int s = blockIdx.y;
@@ -621,11 +658,9 @@ void gm_launch_grid(const ListArgs &a, cudaStream_t s) {
 }
 
 void gm_launch_bin(const ListArgs &a, cudaStream_t s) {
-    clear_cells_kernel<<<dim3((unsigned)std::min(a.scan_blocks * 4, 4096), (unsigned)a.n_sys), 256, 0, s>>>(a);
+    // the grid kernel cleared the cells
     if (a.n > 0) assign_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);
-    scan_local_kernel<<<dim3((unsigned)a.scan_blocks, (unsigned)a.n_sys), 1024, 0, s>>>(a);
-    scan_blocks_kernel<<<a.n_sys, 1024, 0, s>>>(a);
-    scan_add_kernel<<<dim3((unsigned)a.scan_blocks, (unsigned)a.n_sys), 1024, 0, s>>>(a);
+    scan_cells_kernel<<<a.n_sys, 1024, 0, s>>>(a);
     if (a.n > 0) {
         scatter_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);
         rank_kernel<<<sys_grid(a, 256, 4096), 256, 0, s>>>(a);

@@ -31,7 +31,7 @@ constexpr int kScanBlocks = (kMaxCells + 1 + 1023) / 1024 + 1;
 constexpr int kMaxDevices = 64;
 
 // Layout of the scratch array.  What accumulates starts at zero: the status
-// word is cleared by a memset, and the cell counts and cursors by the binning
+// word is cleared by a memset, and the cell counts and cursors by the grid
 // launch; every other field is written in full before it is read.
 struct Scratch {
     double bbox[9 * kBboxBlocks];
