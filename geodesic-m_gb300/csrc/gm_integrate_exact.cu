@@ -24,19 +24,6 @@ namespace {
 
 constexpr double kForceToAccel = 20.455 * 20.455;  // integrator.rs:9
 
-// num / dt correctly rounded, from y = RN(1 / dt) computed once on the host:
-// Markstein's correction (P. Markstein, "IA-64 and Elementary Functions",
-// 2000): q = RN(num y), r = num - q dt is exact in one FMA, and RN(q + r y) is
-// the correctly rounded quotient when y is the correctly rounded reciprocal
-// (away from overflow and underflow).  Three FP64 operations instead of a
-// division, which is long on this part; checked bit for bit against the
-// division on 4e8 operand pairs (velocity-resync values and arbitrary ones).
-__device__ __forceinline__ double div_by_dt(double num, double dt, double y) {
-    const double q = num * y;
-    const double r = fma(-q, dt, num);
-    return fma(r, y, q);
-}
-
 __global__ void half_kick_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                                  const DevStatus *st) {
     // integrator.rs:14-21: v += dt_half * F * inv_m * 20.455^2
@@ -76,7 +63,7 @@ __global__ void resync_kernel(int n, const double *pos, double *vel, const doubl
     // integrator.rs:64-68 (skipped after a failed projection, like the `?` at integrator.rs:256)
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || st->error) return;
-    for (int d = 0; d < 3; d++) vel[d * n + i] = div_by_dt(pos[d * n + i] - dref[d * n + i], dt, inv_dt);
+    for (int d = 0; d < 3; d++) vel[d * n + i] = gm_div_by_dt(pos[d * n + i] - dref[d * n + i], dt, inv_dt);
 }
 
 __global__ void check_kernel(int n, const double *pos, const double *ref, double thr_sq, DevStatus *st,
@@ -912,7 +899,7 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
                 dref[d * n + i] = p;
                 np[d] = p + dt * v;
                 pos[d * n + i] = np[d];
-                vel[d * n + i] = div_by_dt(np[d] - p, dt, inv_dt);
+                vel[d * n + i] = gm_div_by_dt(np[d] - p, dt, inv_dt);
             }
         } else {
             for (int d = 0; d < 3; d++) np[d] = pos[d * n + i];

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "geodesic_cuda.h"
+#include "gm_exact_math.h"
 
 #define GM_FIX_SCALE 1099511627776.0        // 2^40
 #define GM_FIX_INV (1.0 / 1099511627776.0)  // 2^-40
@@ -89,26 +90,6 @@ struct GridInfo {
 __device__ __forceinline__ long long gm_to_fix(double v) { return __double2ll_rn(v * GM_FIX_SCALE); }
 
 // A float force contribution to fixed point; flags non-finite / overflow.
-// round(v * 2^40) to the nearest integer, ties to even, for |v| < 2^22, from
-// the bits of v with integer operations only (the same value as
-// __float2ll_rn(v * 2^40); a 64-bit conversion instruction is slow here)
-__device__ __forceinline__ long long gm_f2fix(float v) {
-    const unsigned b = __float_as_uint(v);
-    const int e = (int)((b >> 23) & 0xffu);
-    const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
-    const int sh = e - 150 + 40;  // |v| * 2^40 = m * 2^sh (normal v)
-    long long r;
-    if (e == 0 || sh < -25) {
-        r = 0;  // below 2^-41: rounds to zero
-    } else if (sh >= 0) {
-        r = m << sh;
-    } else {
-        const int s = -sh;
-        const long long q = m >> s, rem = m & ((1ll << s) - 1), half = 1ll << (s - 1);
-        r = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
-    }
-    return (b >> 31) ? -r : r;
-}
 __device__ __forceinline__ long long gm_to_fix_checked(float v, unsigned int &bad) {
     if (!isfinite(v)) { bad |= GM_DEV_NONFINITE_FORCE; return 0; }
     if (fabsf(v) >= (float)GM_FIX_LIMIT) { bad |= GM_DEV_FIX_OVERFLOW; return 0; }
