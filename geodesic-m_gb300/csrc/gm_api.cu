@@ -109,6 +109,11 @@ struct gm_ctx {
     double *d_epart = nullptr, *d_energy = nullptr, *d_kin_part = nullptr, *d_ke = nullptr;
     int n_epart = 0;
     bool energy_stale = false;  // epart holds the last forces' partials, d_energy not yet their sum
+    // trajectory frames recorded during resident steps
+    int frame_interval = 0, frame_cap = 0;
+    float *d_frame_xyz = nullptr;
+    unsigned long long *d_frame_step = nullptr;
+    double *d_frame_energy = nullptr, *d_frame_part = nullptr;
     // status
     DevStatus *d_status = nullptr;
     DevStatus *h_status = nullptr;  // pinned
@@ -452,6 +457,8 @@ int reset_status(gm_ctx *c) {
     z.rattle_sum = c->h_status->rattle_sum;
     z.rec_n = c->h_status->rec_n;
     z.rebuild_base = c->h_status->rebuild_base;
+    z.frame_n = c->h_status->frame_n;
+    z.frame_lost = c->h_status->frame_lost;
     *c->h_status = z;
     return st_write(c);
 }
@@ -678,15 +685,28 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
 
 int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
     long long k = seq_forces(c, s, false, c->side, c->n_clusters == 0);
-    if (!c->n_clusters) {
-        // the closing half-kick is done by the next step's first kernel, or
-        // by finish_steps after the last step
-        *count += k;
-        return GM_OK;
+    if (c->n_clusters) {
+        gm_launch_half_kick(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
+        gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, s); k += 3;
+        gm_launch_step(c->d_status, s); k++;
     }
-    gm_launch_half_kick(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
-    gm_launch_rattle(cluster_args(c), c->n, c->d_pos, c->d_vel, s); k += 3;
-    gm_launch_step(c->d_status, s); k++;
+    // (without constraints the closing half-kick is done by the next step's
+    // first kernel, or by finish_steps after the last step)
+    if (c->frame_interval > 0) {
+        // the energy partials of this step's forces, summed by the frame kernel
+        ForceArgs fa = force_args(c);
+        FrameArgs f{};
+        f.interval = c->frame_interval;
+        f.cap = c->frame_cap;
+        f.xyz = c->d_frame_xyz;
+        f.step = c->d_frame_step;
+        f.energy = c->d_frame_energy;
+        f.partial = c->d_frame_part;
+        f.epart = fa.epart;
+        f.n_epart = fa.n_epart_total;
+        gm_launch_frame(c->n, c->d_pos, c->d_vel, c->d_force, c->d_inv_mass, c->d_mass, dt / 2.0, c->d_status, f, s);
+        k++;
+    }
     *count += k;
     return GM_OK;
 }
@@ -2020,6 +2040,74 @@ int32_t gm_ws_last(gm_ctx *c, float *feat, double *lam0, double *lam_sum) {
 }
 
 /* ---- batches of independent systems ----------------------------------- */
+
+/* ---- trajectory frames ------------------------------------------------- */
+
+int32_t gm_frames_enable(gm_ctx *c, int32_t frame_interval, int32_t capacity) {
+    if (!c || frame_interval < 0 || (frame_interval > 0 && capacity < 1)) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    dfree(c, c->d_frame_xyz);
+    dfree(c, c->d_frame_step);
+    dfree(c, c->d_frame_energy);
+    dfree(c, c->d_frame_part);
+    c->d_frame_xyz = nullptr;
+    c->d_frame_step = nullptr;
+    c->d_frame_energy = nullptr;
+    c->d_frame_part = nullptr;
+    c->frame_interval = 0;
+    c->frame_cap = 0;
+    if (frame_interval > 0) {
+        int rc = dalloc(c, &c->d_frame_xyz, (size_t)capacity * 3 * (size_t)std::max(c->n, 1));
+        if (!rc) rc = dalloc(c, &c->d_frame_step, (size_t)capacity);
+        if (!rc) rc = dalloc(c, &c->d_frame_energy, 2 * (size_t)capacity);
+        if (!rc) rc = dalloc(c, &c->d_frame_part, (size_t)GM_FRAME_BLOCKS);
+        if (rc) return rc;
+        c->frame_interval = frame_interval;
+        c->frame_cap = capacity;
+    }
+    // the step graph is captured with or without the frame kernel
+    drop_graph(c);
+    int rc = st_read(c);
+    if (rc) return rc;
+    c->h_status->frame_n = 0;
+    c->h_status->frame_lost = 0;
+    return st_write(c);
+}
+
+int32_t gm_frames_take(gm_ctx *c, int64_t max_frames, float *xyz, uint64_t *steps, double *e_pot, double *e_kin,
+                       int64_t *n_frames, int64_t *n_lost) {
+    if (!c || !n_frames) return GM_ERR_INVALID_ARGUMENT;
+    GM_CUDA(c, cudaSetDevice(c->device));
+    int rc = st_read(c);
+    if (rc) return rc;
+    const int64_t n = c->h_status->frame_n;
+    *n_frames = n;
+    if (n_lost) *n_lost = c->h_status->frame_lost;
+    if (n > max_frames) return fail(c, GM_ERR_INVALID_ARGUMENT, "%lld frames recorded, room for %lld",
+                                    (long long)n, (long long)max_frames);
+    if (n > 0) {
+        if (xyz)
+            GM_CUDA(c, cudaMemcpyAsync(xyz, c->d_frame_xyz, sizeof(float) * 3 * (size_t)c->n * (size_t)n,
+                                       cudaMemcpyDeviceToHost, c->stream));
+        if (steps)
+            GM_CUDA(c, cudaMemcpyAsync(steps, c->d_frame_step, sizeof(unsigned long long) * (size_t)n,
+                                       cudaMemcpyDeviceToHost, c->stream));
+        if (e_pot || e_kin) {
+            std::vector<double> e(2 * (size_t)n);
+            GM_CUDA(c, cudaMemcpyAsync(e.data(), c->d_frame_energy, sizeof(double) * e.size(),
+                                       cudaMemcpyDeviceToHost, c->stream));
+            GM_CUDA(c, cudaStreamSynchronize(c->stream));
+            for (int64_t k = 0; k < n; k++) {
+                if (e_pot) e_pot[k] = e[2 * (size_t)k];
+                if (e_kin) e_kin[k] = e[2 * (size_t)k + 1];
+            }
+        }
+    }
+    c->h_status->frame_n = 0;
+    c->h_status->frame_lost = 0;
+    return st_write(c);
+}
 
 int32_t gm_ensemble_info(const gm_ctx *c, int64_t *atom_offsets) {
     if (!c || !atom_offsets) return GM_ERR_INVALID_ARGUMENT;

@@ -501,17 +501,10 @@ __global__ void __launch_bounds__(256) bonded_pair14_kernel(ForceArgs a) {
 
 // Fixed-order sum of all energy partials (pair groups, bonded blocks, 1-4
 // blocks) into the FP64 total: deterministic for a given launch shape.
-__global__ void __launch_bounds__(1024) energy_kernel(const double *epart, int n, double *out) {
-    __shared__ double s[1024];
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += epart[i];
-    s[threadIdx.x] = acc;
-    __syncthreads();
-    for (int k = 512; k > 0; k >>= 1) {
-        if (threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *out = s[0];
+__global__ void __launch_bounds__(256) energy_kernel(const double *epart, int n, double *out) {
+    __shared__ double s[256];
+    const double e = gm_block_sum256(epart, n, s);
+    if (threadIdx.x == 0) *out = e;
 }
 
 }  // namespace
@@ -578,5 +571,5 @@ void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {
 }
 
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s) {
-    energy_kernel<<<1, 1024, 0, s>>>(a.epart, a.n_epart_total, a.energy);
+    energy_kernel<<<1, 256, 0, s>>>(a.epart, a.n_epart_total, a.energy);
 }

@@ -833,6 +833,64 @@ __global__ void kinetic_partial(int n, const double *vel, const double *mass, do
     if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
 }
 
+// Trajectory frame (see gm_launch_frame).  The completed step count is the
+// counter plus one while the unconstrained step's closing half-kick is still
+// pending; every block takes the same early exit.
+__global__ void __launch_bounds__(256) frame_kernel(int n, const double *pos, const double *vel,
+                                                    const long long *force, const double *inv_mass,
+                                                    const double *mass, double dt_half, DevStatus *st, FrameArgs f) {
+    const bool tail = st->tail_pending != 0;
+    const unsigned long long step = st->step + (tail ? 1ull : 0ull);
+    if (st->error || f.interval <= 0 || step % (unsigned long long)f.interval != 0) return;
+    const unsigned slot = st->frame_n;  // every block reads it before the last block advances it
+    const bool store = slot < (unsigned)f.cap;
+    float *fx = f.xyz + (size_t)(store ? slot : 0) * 3 * (size_t)n;
+    __shared__ double s[256];
+    __shared__ bool last;
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double v[3];
+        for (int d = 0; d < 3; d++) {
+            if (store) fx[(size_t)d * n + i] = (float)pos[d * n + i];
+            v[d] = vel[d * n + i];
+            if (tail) {
+                const double fd = (double)force[d * n + i] * GM_FIX_INV;
+                v[d] += dt_half * fd * inv_mass[i] * kForceToAccel;
+            }
+        }
+        acc += mass[i] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);  // kinetic_partial's order
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        f.partial[blockIdx.x] = s[0];
+        __threadfence();
+        last = atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double e_pot = gm_block_sum256(f.epart, f.n_epart, s);
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int b = 0; b < (int)gridDim.x; b++) sum += ((volatile double *)f.partial)[b];
+        const double e_kin = 0.5 * sum * (1.0 / (20.455 * 20.455));  // kinetic_final
+        st->blocks_done = 0;
+        if (store) {
+            f.step[slot] = step;
+            f.energy[2 * slot] = e_pot;
+            f.energy[2 * slot + 1] = e_kin;
+            st->frame_n = slot + 1;
+        } else {
+            st->frame_lost += 1;
+        }
+    }
+}
+
 __global__ void kinetic_final(const double *partial, int blocks, double *out) {
     if (threadIdx.x != 0) return;
     double sum = 0.0;
@@ -856,6 +914,8 @@ __global__ void status_reset_kernel(DevStatus *st, int set_step, unsigned long l
     z.shake_sum = st->shake_sum;
     z.rattle_sum = st->rattle_sum;
     z.rec_n = st->rec_n;
+    z.frame_n = st->frame_n;
+    z.frame_lost = st->frame_lost;
     z.rebuild_base = st->n_rebuilds;
     *st = z;
 }
@@ -1048,6 +1108,10 @@ void gm_launch_kinetic(int n, const double *vel, const double *mass, double *par
     kinetic_final<<<1, 32, 0, s>>>(partials, blocks, out);
 }
 
+void gm_launch_frame(int n, const double *pos, const double *vel, const long long *force, const double *inv_mass,
+                     const double *mass, double dt_half, DevStatus *st, const FrameArgs &f, cudaStream_t s) {
+    frame_kernel<<<GM_FRAME_BLOCKS, 256, 0, s>>>(n, pos, vel, force, inv_mass, mass, dt_half, st, f);
+}
 void gm_launch_status_reset(DevStatus *st, int set_step, unsigned long long step, cudaStream_t s) {
     status_reset_kernel<<<1, 1, 0, s>>>(st, set_step, step);
 }

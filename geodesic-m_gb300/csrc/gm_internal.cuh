@@ -72,6 +72,8 @@ struct DevStatus {
     unsigned int tail_pending;     // unconstrained resident steps: the last step's closing half-kick
                                    // is still to do (the next step's first kernel or the finalizer)
     unsigned long long rebuild_base;  // n_rebuilds when the current call's status was reset
+    unsigned int frame_n;          // trajectory frames recorded since they were last taken
+    unsigned int frame_lost;       // frames due while the ring was full
 };
 
 struct GridInfo {
@@ -121,6 +123,20 @@ __device__ __forceinline__ void gm_add_sys_energy(long long *e_sys, int sy, doub
     } else if (sy >= 0 && q != 0) {
         gm_atomic_fix_add(e_sys + sy, q);
     }
+}
+
+// Sum of x[0..n) by a block of 256 threads: per-thread strided partial sums,
+// then a tree over the block (fixed order; every caller gets the same bits).
+__device__ __forceinline__ double gm_block_sum256(const double *x, int n, double *s) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) acc += x[i];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    return s[0];
 }
 
 // Both float4 of a slot's (hi, lo) coordinate pair in one 256-bit load
@@ -298,6 +314,24 @@ void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, l
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,
                                 const PackArgs &pk, cudaStream_t s);
+// Trajectory frames recorded on the device during resident steps.
+struct FrameArgs {
+    int interval;                // a frame when the completed step count is a multiple (0: none)
+    int cap;                     // frames the ring holds
+    float *xyz;                  // [cap][3][n] positions as float32
+    unsigned long long *step;    // [cap] step of each frame
+    double *energy;              // [cap][2] potential and kinetic energy (kcal/mol)
+    double *partial;             // [kFrameBlocks] kinetic partial sums
+    const double *epart;         // energy partials of the last force evaluation
+    int n_epart;
+};
+constexpr int GM_FRAME_BLOCKS = 64;  // the kinetic reduction's grid (as gm_kinetic_energy's)
+// Records a frame when the step just completed is due: positions as float32,
+// the kinetic energy of the step's final velocities (its closing half-kick
+// applied when still pending, in the finalizer's arithmetic; the reduction of
+// gm_kinetic_energy) and the potential energy (the energy kernel's sum).
+void gm_launch_frame(int n, const double *pos, const double *vel, const long long *force, const double *inv_mass,
+                     const double *mass, double dt_half, DevStatus *st, const FrameArgs &f, cudaStream_t s);
 // The closing half-kick and step count of the last unconstrained resident
 // step, when one is pending (a no-op otherwise).
 void gm_launch_kick_tail(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,

@@ -22,6 +22,7 @@ import numpy as np
 from . import _build
 
 GM_OK = 0
+GM_ERR_INVALID_ARGUMENT = 1
 STATUS_NAMES = {
     1: "INVALID_ARGUMENT", 2: "NO_DEVICE", 3: "OUT_OF_MEMORY", 4: "DEVICE", 5: "CONVERGENCE", 6: "NONFINITE",
     7: "LIST_OVERFLOW", 8: "UNSUPPORTED", 9: "FIXED_POINT_OVERFLOW", 10: "NOT_BUILT",
@@ -138,6 +139,9 @@ def lib():
         L.gm_steps.argtypes = [C.c_void_p] + [C.c_void_p] * 6 + [C.c_double, C.c_uint64, C.c_int64] + [
             C.c_void_p] * 3 + [_f64p, P(C.c_int64), P(GmConvergence)]
         L.gm_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_int64]
+        L.gm_frames_enable.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.gm_frames_take.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     P(C.c_int64), P(C.c_int64)]
         L.gm_upload_state.argtypes = [C.c_void_p] + [_f64p] * 6
         L.gm_download_state.argtypes = [C.c_void_p] + [_f64p] * 6
         L.gm_run_resident.argtypes = [C.c_void_p, C.c_double, C.c_uint64, C.c_int64]
@@ -169,7 +173,8 @@ def lib():
                   "gm_ws_gradient", "gm_ws_last", "gm_build_pairs_static", "gm_destroy", "gm_build_list", "gm_compute_forces", "gm_needs_rebuild", "gm_geodesic_drift",
                   "gm_half_kick", "gm_constrain_velocities", "gm_kinetic_energy", "gm_n_threads", "gm_get_pairs",
                   "gm_steps", "gm_last_error", "gm_upload_state", "gm_download_state", "gm_run_resident",
-                  "gm_forces_resident", "gm_synchronize", "gm_counters", "gm_profile", "gm_time_steps"):
+                  "gm_forces_resident", "gm_synchronize", "gm_counters", "gm_profile", "gm_time_steps",
+                  "gm_frames_enable", "gm_frames_take"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -289,6 +294,34 @@ class CudaBackend:
         ek = np.zeros(self.n_sys)
         self._check(lib().gm_ensemble_energies(self._h, _p(ep), _p(ek)))
         return ep, ek
+
+    def frames_enable(self, frame_interval: int, capacity: int = 64):
+        """Record a trajectory frame every `frame_interval` resident steps into
+        a device ring of `capacity` frames (gm_frames_enable); 0 turns it off."""
+        self._check(lib().gm_frames_enable(self._h, int(frame_interval), int(capacity)))
+        self._frame_cap = int(capacity) if frame_interval > 0 else 0
+
+    def frames_take(self):
+        """The frames recorded since the last call (gm_frames_take): xyz
+        (n, 3, N) float32, step (n,) uint64, e_pot and e_kin (n,) float64."""
+        cap = getattr(self, "_frame_cap", 0)
+        xyz = np.zeros((cap, 3, self.n), dtype=np.float32)
+        steps = np.zeros(cap, dtype=np.uint64)
+        ep = np.zeros(cap)
+        ek = np.zeros(cap)
+        n, lost = C.c_int64(), C.c_int64()
+        self._check(lib().gm_frames_take(self._h, cap, xyz.ctypes.data, steps.ctypes.data, ep.ctypes.data,
+                                         ek.ctypes.data, C.byref(n), C.byref(lost)))
+        if lost.value:
+            raise BackendError(GM_ERR_INVALID_ARGUMENT, f"{lost.value} trajectory frames lost on a full ring")
+        k = n.value
+        return dict(xyz=xyz[:k], step=steps[:k], e_pot=ep[:k], e_kin=ek[:k])
+
+    def resident_energies(self):
+        """(potential, kinetic) energy of the resident state, summed over the
+        systems of a batch."""
+        ep, ek = self.ensemble_energies()
+        return float(ep.sum()), float(ek.sum())
 
     def close(self):
         if getattr(self, "_h", None):

@@ -209,6 +209,26 @@ int32_t gm_ensemble_info(const gm_ctx *ctx, int64_t *atom_offsets);
  * kinetic energy of the resident velocities (lib.rs:68-77); NULL skips. */
 int32_t gm_ensemble_energies(gm_ctx *ctx, double *e_pot, double *e_kin);
 
+/* ---- trajectory frames (the run loop's frame output, lib.rs:325-331,
+ * 347-361, recorded on the device) -------------------------------------
+ *
+ * With frame_interval > 0, every resident step (gm_run_resident, gm_steps,
+ * gm_time_steps) whose completed step count is a multiple of frame_interval
+ * records a frame into a device ring of `capacity` frames: the positions as
+ * float32 rows x|y|z (the run loop's f32 conversion), the potential energy of
+ * the step's force evaluation and the kinetic energy of its final velocities
+ * (the sums of potential_energy / gm_kinetic_energy).  Frames due while the
+ * ring is full are counted as lost.  0 turns recording off.  Changing the
+ * setting recaptures the step graph. */
+int32_t gm_frames_enable(gm_ctx *ctx, int32_t frame_interval, int32_t capacity);
+/* Copies the frames recorded since the last call, oldest first, and empties
+ * the ring: xyz [n][3][N] float32, steps [n], e_pot / e_kin [n] (kcal/mol);
+ * any pointer may be NULL.  *n_frames = n; GM_ERR_INVALID_ARGUMENT (nothing
+ * taken) when n > max_frames.  *n_lost (nullable): frames dropped on a full
+ * ring. */
+int32_t gm_frames_take(gm_ctx *ctx, int64_t max_frames, float *xyz, uint64_t *steps, double *e_pot, double *e_kin,
+                       int64_t *n_frames, int64_t *n_lost);
+
 /* ---- autotuner (no reference counterpart) ------------------------------
  *
  * Times the FP32 pair kernel on the current list (reps launches per

@@ -13,6 +13,7 @@ reference's golden trajectory `geodesic/tests/golden/ala_dipeptide_ref.dcd`
 `ala_dipeptide_ref_frames.npy` (float32, shape (100, 3, 22)) plus the DCD
 header fields in `ala_dipeptide_ref_header.json`.
 """
+import hashlib
 import json
 import os
 import struct
@@ -64,7 +65,13 @@ def main(ref_root):
         amber.save_npz(os.path.join(HERE, f"{name}.npz"), atoms, topo, state)
         print(f"{name}: {atoms.n} atoms, {len(topo.bond_i)} bonds, {len(topo.angle_i)} angles, "
               f"{len(topo.dihed_i)} dihedrals, {len(topo.excl_i)} exclusions")
-    header, frames = read_dcd(os.path.join(ref_root, "geodesic", "tests", "golden", "ala_dipeptide_ref.dcd"))
+    dcd_path = os.path.join(ref_root, "geodesic", "tests", "golden", "ala_dipeptide_ref.dcd")
+    header, frames = read_dcd(dcd_path)
+    with open(dcd_path, "rb") as f:
+        raw = f.read()
+    # the file's identity, so a writer given the decoded frames can be checked byte for byte
+    header["file_bytes"] = len(raw)
+    header["file_sha256"] = hashlib.sha256(raw).hexdigest()
     np.save(os.path.join(HERE, "ala_dipeptide_ref_frames.npy"), frames.astype(np.float32))
     with open(os.path.join(HERE, "ala_dipeptide_ref_header.json"), "w") as f:
         json.dump(header, f, indent=1)
