@@ -158,95 +158,157 @@ def infer_element(name: str) -> int:
     return ELEMENT_UNKNOWN
 
 
+def _field_bytes(sections: dict, flag: str, width: int, count: int):
+    """The `count` fixed-width fields of a section as a numpy byte-string
+    array, or None when the section is not plain ASCII (the per-field path
+    then keeps the reference's character positions)."""
+    if flag not in sections:
+        raise PrmtopError(f"missing required config key: %FLAG {flag}")
+    raw = sections[flag]
+    if not raw.isascii():
+        return None
+    need = width * count
+    # a field past the end of the data parses as blank (an error), a partly
+    # present one as its characters, as in the per-field path
+    b = raw[:need].encode("ascii").ljust(need)
+    return np.frombuffer(b, dtype=f"S{width}")
+
+
+def _ints_np(sections, flag, width, count) -> np.ndarray:
+    """`_ints` for whole sections at once; any field the vectorised parse
+    rejects goes through `_ints`, which raises the reference's error."""
+    f = _field_bytes(sections, flag, width, count)
+    try:
+        if f is not None:
+            return f.astype(np.int64)
+    except ValueError:
+        pass
+    return np.asarray(_ints(sections, flag, width, count), np.int64)
+
+
+def _floats_np(sections, flag, width, count) -> np.ndarray:
+    f = _field_bytes(sections, flag, width, count)
+    try:
+        if f is not None:
+            return f.astype(np.float64)
+    except ValueError:
+        pass
+    return np.asarray(_floats(sections, flag, width, count), np.float64)
+
+
+def _elements(names: np.ndarray) -> np.ndarray:
+    """`infer_element` for an (N,) array of 4-byte names: the first ASCII
+    letter decides."""
+    b = np.frombuffer(names.tobytes(), np.uint8).reshape(-1, 4) if len(names) else np.zeros((0, 4), np.uint8)
+    upper = b & 0xDF  # ASCII letters to upper case
+    alpha = ((b >= 65) & (b <= 90)) | ((b >= 97) & (b <= 122))
+    has = alpha.any(axis=1)
+    first = upper[np.arange(len(b)), alpha.argmax(axis=1)] if len(b) else np.zeros(0, np.uint8)
+    out = np.full(len(b), ELEMENT_UNKNOWN, np.uint8)
+    for ch, el in ((b"H", ELEMENT_H), (b"C", ELEMENT_C), (b"N", ELEMENT_N), (b"O", ELEMENT_O), (b"S", ELEMENT_S)):
+        out[has & (first == ch[0])] = el
+    return out
+
+
 def parse_prmtop(text: str) -> tuple:
-    """Returns (AtomData, BondedTopology) like `prmtop::parse` (`prmtop.rs:182`)."""
+    """Returns (AtomData, BondedTopology) like `prmtop::parse` (`prmtop.rs:182`).
+
+    Whole sections are parsed as numpy fixed-width arrays (a million-atom
+    file in seconds); the per-atom and per-term assembly is vectorised with
+    the reference's exact rules."""
     s = _sections(text)
     p = _ints(s, "POINTERS", 8, 20)
     natom, ntypes, nbonh, ntheth, nphih = p[0], p[1], p[2], p[4], p[6]
     nnb, nres, nbona, ntheta, nphia = p[10], p[11], p[12], p[13], p[14]
     numbnd, numang, nptra = p[15], p[16], p[17]
 
-    names = _fields(s, "ATOM_NAME", 4, natom)
-    charge = np.array(_floats(s, "CHARGE", 16, natom), np.float64) / AMBER_CHARGE_TO_ELEMENTARY
-    mass = np.array(_floats(s, "MASS", 16, natom), np.float64)
-    type_index = _ints(s, "ATOM_TYPE_INDEX", 8, natom)
-    n_excluded = _ints(s, "NUMBER_EXCLUDED_ATOMS", 8, natom)
-    nb_index = _ints(s, "NONBONDED_PARM_INDEX", 8, ntypes * ntypes)
+    names_b = _field_bytes(s, "ATOM_NAME", 4, natom)
+    if names_b is None:
+        names = _fields(s, "ATOM_NAME", 4, natom)
+        element = np.array([infer_element(n) for n in names], np.uint8)
+    else:
+        names = [n.decode("ascii") for n in names_b]
+        element = _elements(names_b)
+    charge = _floats_np(s, "CHARGE", 16, natom) / AMBER_CHARGE_TO_ELEMENTARY
+    mass = _floats_np(s, "MASS", 16, natom)
+    type_index = _ints_np(s, "ATOM_TYPE_INDEX", 8, natom)
+    n_excluded = _ints_np(s, "NUMBER_EXCLUDED_ATOMS", 8, natom)
+    nb_index = _ints_np(s, "NONBONDED_PARM_INDEX", 8, ntypes * ntypes)
     n_lj = ntypes * (ntypes + 1) // 2
-    acoef = _floats(s, "LENNARD_JONES_ACOEF", 16, n_lj)
-    bcoef = _floats(s, "LENNARD_JONES_BCOEF", 16, n_lj)
-    res_ptr = _ints(s, "RESIDUE_POINTER", 8, nres)
-    excl_list = _ints(s, "EXCLUDED_ATOMS_LIST", 8, nnb)
+    acoef = _floats_np(s, "LENNARD_JONES_ACOEF", 16, n_lj)
+    bcoef = _floats_np(s, "LENNARD_JONES_BCOEF", 16, n_lj)
+    res_ptr = _ints_np(s, "RESIDUE_POINTER", 8, nres)
+    excl_list = _ints_np(s, "EXCLUDED_ATOMS_LIST", 8, nnb)
 
-    sigma = np.zeros(natom)
-    epsilon = np.zeros(natom)
-    for i, ty in enumerate(type_index):
-        ico = nb_index[ntypes * (ty - 1) + ty - 1]
-        if ico <= 0:
-            raise PrmtopError(f"atom {i} uses a 10-12 H-bond LJ type (NONBONDED_PARM_INDEX={ico}); not supported")
-        a, b = acoef[ico - 1], bcoef[ico - 1]
+    # per type (prmtop.rs:216-237), then per atom; the first atom of a 10-12
+    # type is the one reported
+    ico = nb_index[ntypes * (type_index - 1) + type_index - 1] if natom else np.zeros(0, np.int64)
+    bad = np.nonzero(ico <= 0)[0]
+    if len(bad):
+        i = int(bad[0])
+        raise PrmtopError(f"atom {i} uses a 10-12 H-bond LJ type (NONBONDED_PARM_INDEX={int(ico[i])}); not supported")
+    sig_t, eps_t = {}, {}
+    for c in np.unique(ico):
+        a, b = float(acoef[c - 1]), float(bcoef[c - 1])
         if a == 0.0 or b == 0.0:
-            sigma[i] = epsilon[i] = 0.0
+            sig_t[c] = eps_t[c] = 0.0
         else:
-            sigma[i] = math.pow(a / b, 1.0 / 6.0)
-            epsilon[i] = (b * b) / (4.0 * a)
+            sig_t[c] = math.pow(a / b, 1.0 / 6.0)
+            eps_t[c] = (b * b) / (4.0 * a)
+    uniq, inv = np.unique(ico, return_inverse=True)
+    sigma = np.array([sig_t[c] for c in uniq], np.float64)[inv] if natom else np.zeros(0)
+    epsilon = np.array([eps_t[c] for c in uniq], np.float64)[inv] if natom else np.zeros(0)
 
-    element = np.array([infer_element(n) for n in names], np.uint8)
-    residue = np.zeros(natom, np.uint32)
-    for i in range(natom):
-        rid = 0
-        for r, start in enumerate(res_ptr):
-            if start <= i + 1:
-                rid = r
-            else:
-                break
-        residue[i] = rid
-    atoms = AtomData(sigma, epsilon, mass, charge, element, residue, [n.ljust(4) for n in names])
+    # residue of atom i: the last pointer before the first one past i + 1
+    # (the reference's scan breaks there), i.e. a search in the running maximum
+    if nres:
+        cummax = np.maximum.accumulate(res_ptr)
+        residue = np.maximum(np.searchsorted(cummax, np.arange(1, natom + 1), side="right") - 1, 0)
+    else:
+        residue = np.zeros(natom, np.int64)
+    atoms = AtomData(sigma, epsilon, mass, charge, element, residue.astype(np.uint32), [n.ljust(4) for n in names])
 
-    bonds_h = _ints(s, "BONDS_INC_HYDROGEN", 8, 3 * nbonh)
-    bonds_a = _ints(s, "BONDS_WITHOUT_HYDROGEN", 8, 3 * nbona)
-    angles_h = _ints(s, "ANGLES_INC_HYDROGEN", 8, 4 * ntheth)
-    angles_a = _ints(s, "ANGLES_WITHOUT_HYDROGEN", 8, 4 * ntheta)
-    dihed_h = _ints(s, "DIHEDRALS_INC_HYDROGEN", 8, 5 * nphih)
-    dihed_a = _ints(s, "DIHEDRALS_WITHOUT_HYDROGEN", 8, 5 * nphia)
-    bk = _floats(s, "BOND_FORCE_CONSTANT", 16, numbnd)
-    br0 = _floats(s, "BOND_EQUIL_VALUE", 16, numbnd)
-    ak = _floats(s, "ANGLE_FORCE_CONSTANT", 16, numang)
-    ath0 = _floats(s, "ANGLE_EQUIL_VALUE", 16, numang)
-    dk = _floats(s, "DIHEDRAL_FORCE_CONSTANT", 16, nptra)
-    dper = _floats(s, "DIHEDRAL_PERIODICITY", 16, nptra)
-    dphase = _floats(s, "DIHEDRAL_PHASE", 16, nptra)
-
-    raw_b = np.array(bonds_h + bonds_a, np.int64).reshape(-1, 3)
-    raw_a = np.array(angles_h + angles_a, np.int64).reshape(-1, 4)
-    raw_d = np.abs(np.array(dihed_h + dihed_a, np.int64).reshape(-1, 5))
+    raw_b = np.concatenate([_ints_np(s, "BONDS_INC_HYDROGEN", 8, 3 * nbonh),
+                            _ints_np(s, "BONDS_WITHOUT_HYDROGEN", 8, 3 * nbona)]).reshape(-1, 3)
+    raw_a = np.concatenate([_ints_np(s, "ANGLES_INC_HYDROGEN", 8, 4 * ntheth),
+                            _ints_np(s, "ANGLES_WITHOUT_HYDROGEN", 8, 4 * ntheta)]).reshape(-1, 4)
+    raw_d = np.concatenate([_ints_np(s, "DIHEDRALS_INC_HYDROGEN", 8, 5 * nphih),
+                            _ints_np(s, "DIHEDRALS_WITHOUT_HYDROGEN", 8, 5 * nphia)]).reshape(-1, 5)
+    bk = _floats_np(s, "BOND_FORCE_CONSTANT", 16, numbnd)
+    br0 = _floats_np(s, "BOND_EQUIL_VALUE", 16, numbnd)
+    ak = _floats_np(s, "ANGLE_FORCE_CONSTANT", 16, numang)
+    ath0 = _floats_np(s, "ANGLE_EQUIL_VALUE", 16, numang)
+    dk = _floats_np(s, "DIHEDRAL_FORCE_CONSTANT", 16, nptra)
+    dper = _floats_np(s, "DIHEDRAL_PERIODICITY", 16, nptra)
+    dphase = _floats_np(s, "DIHEDRAL_PHASE", 16, nptra)
     bt = raw_b[:, 2] - 1
     at = raw_a[:, 3] - 1
-    dt = np.array(dihed_h + dihed_a, np.int64).reshape(-1, 5)[:, 4] - 1
+    dt = raw_d[:, 4] - 1
+    abs_d = np.abs(raw_d)
 
-    excl_i, excl_j = [], []
-    cursor = 0
-    for i, cnt in enumerate(n_excluded):
-        for _ in range(cnt):
-            raw = excl_list[cursor]
-            cursor += 1
-            if raw == 0:
-                continue
-            excl_i.append(i)
-            excl_j.append(raw - 1)
+    # exclusions in list order, one run per atom, 0 entries skipped
+    # (prmtop.rs:303-317)
+    total = int(n_excluded.sum()) if natom else 0
+    if total > len(excl_list) or (natom and n_excluded.min() < 0):
+        raise PrmtopError(f"invalid value for key '%FLAG NUMBER_EXCLUDED_ATOMS': the counts ask for {total} "
+                          f"entries of EXCLUDED_ATOMS_LIST, which has {len(excl_list)}")
+    owner = np.repeat(np.arange(natom, dtype=np.int64), n_excluded) if natom else np.zeros(0, np.int64)
+    raw_e = excl_list[:total]
+    keep = raw_e != 0
 
-    f64 = lambda a: np.asarray(a, np.float64)  # noqa: E731
+    per = dper[dt]
     u32 = lambda a: np.asarray(a, np.uint32)  # noqa: E731
     topo = BondedTopology(
         bond_i=u32(raw_b[:, 0] // 3), bond_j=u32(raw_b[:, 1] // 3),
-        bond_k=f64([bk[t] for t in bt]), bond_r0=f64([br0[t] for t in bt]),
+        bond_k=bk[bt].astype(np.float64), bond_r0=br0[bt].astype(np.float64),
         angle_i=u32(raw_a[:, 0] // 3), angle_j=u32(raw_a[:, 1] // 3), angle_k=u32(raw_a[:, 2] // 3),
-        angle_kth=f64([ak[t] for t in at]), angle_th0=f64([ath0[t] for t in at]),
-        dihed_i=u32(raw_d[:, 0] // 3), dihed_j=u32(raw_d[:, 1] // 3), dihed_k=u32(raw_d[:, 2] // 3),
-        dihed_l=u32(raw_d[:, 3] // 3), dihed_kphi=f64([dk[t] for t in dt]),
-        dihed_n=u32([_round_half_away(dper[t]) for t in dt]), dihed_delta=f64([dphase[t] for t in dt]),
-        constr_i=u32([]), constr_j=u32([]), constr_dsq=f64([]),
-        excl_i=u32(excl_i), excl_j=u32(excl_j))
+        angle_kth=ak[at].astype(np.float64), angle_th0=ath0[at].astype(np.float64),
+        dihed_i=u32(abs_d[:, 0] // 3), dihed_j=u32(abs_d[:, 1] // 3), dihed_k=u32(abs_d[:, 2] // 3),
+        dihed_l=u32(abs_d[:, 3] // 3), dihed_kphi=dk[dt].astype(np.float64),
+        dihed_n=u32((np.floor(np.abs(per) + 0.5) * np.where(per >= 0, 1.0, -1.0)).astype(np.int64)),
+        dihed_delta=dphase[dt].astype(np.float64),
+        constr_i=u32([]), constr_j=u32([]), constr_dsq=np.zeros(0),
+        excl_i=u32(owner[keep]), excl_j=u32(raw_e[keep] - 1))
     return atoms, topo
 
 
@@ -270,6 +332,11 @@ def parse_inpcrd(text: str, expected_n_atoms: int, has_box: bool = False) -> Sta
         raise PrmtopError(f"expected {nlines} coordinate line(s) for {natom} atoms, found {len(data)}")
 
     def block(txt):
+        if txt.isascii():
+            try:
+                return np.frombuffer(txt[:nval * 12].encode("ascii").ljust(nval * 12), dtype="S12").astype(np.float64)
+            except ValueError:
+                pass
         return np.array([float(txt[i * 12:(i + 1) * 12].strip()) for i in range(nval)], np.float64)
 
     pos = block("".join(data[:nlines])).reshape(natom, 3).T.copy()
