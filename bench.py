@@ -48,12 +48,34 @@ def ns_per_day(steps, seconds):
     return DT_PS * 1e-3 * steps / seconds * 86400.0
 
 
+def replica_seed(rank):
+    """Each rank's replica is its own seeded system."""
+    return SEED + rank
+
+
+def max_over_ranks(sec, device):
+    """The timed span of the slowest rank, on every rank (one MAX all-reduce
+    in whatever process group is initialised; the value itself without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return sec
+    t = torch.tensor([sec], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_ns_per_day(world, steps, sec):
+    """Whole-job throughput: world replicas of `steps` steps each in `sec`."""
+    return world * ns_per_day(steps, sec)
+
+
 def workload(rank=0):
     from geodesic_cuda import synth
     # the lattice is over-compressed for its sigma range: FIRE-minimise it
     # (1000 iterations, two stages) so NVE starts near 300 K instead of
     # converting ~25 kcal/mol/atom of compression energy into heat
-    return synth.generate(N_ATOMS, seed=SEED + rank, temperature=300.0, relax_iters=1000)
+    return synth.generate(N_ATOMS, seed=replica_seed(rank), temperature=300.0, relax_iters=1000)
 
 
 def config_dict(extra=None):
@@ -162,18 +184,14 @@ def run_cuda(args, rank, world):
         t1 = time.perf_counter()
     torch.cuda.synchronize()
     c1 = be.counters()
-    sec = dev_ms / 1e3
-    if world > 1:
-        tt = torch.tensor([sec], device=f"cuda:{dev}", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        sec = float(tt.item())
+    sec = max_over_ranks(dev_ms / 1e3, f"cuda:{dev}")
     pairs = c1["pairs"]
     result = dict(sec=sec, wall=t1 - t0, pairs=pairs, rebuilds=c1["rebuilds"] - c0["rebuilds"],
                   launches=c1["launches"] - c0["launches"], clocks=clk.summary())
     if rank != 0:
         return None
     if args.quick:
-        return {"metric": METRIC, "value": round(world * ns_per_day(args.steps, sec), 3), "unit": "ns/day",
+        return {"metric": METRIC, "value": round(aggregate_ns_per_day(world, args.steps, sec), 3), "unit": "ns/day",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(1e3 * sec / args.steps, 5), "quick": True, "half_list_pairs": pairs,
                 "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"]),
@@ -254,7 +272,7 @@ def run_cuda(args, rank, world):
     cpu = cpu_baseline_sample(atoms, topo, state, result["rebuilds"] / max(args.steps, 1))
     steps_per_s = args.steps / sec
     line = {
-        "metric": METRIC, "value": round(world * ns_per_day(args.steps, sec), 3), "unit": "ns/day",
+        "metric": METRIC, "value": round(aggregate_ns_per_day(world, args.steps, sec), 3), "unit": "ns/day",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * sec / args.steps, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 pair math, int64 fixed-point forces, fp64 state/energy",
