@@ -5,8 +5,12 @@
 // and the force buffer, on the device.  Host entry points upload the caller's
 // arrays, run the kernels on the context's stream and copy results back;
 // the resident entry points keep everything on the device and run the BAB
-// loop as a CUDA graph (one captured step: half-kick, drift, SHAKE, rebuild
-// check, an IF node holding the list rebuild, forces, half-kick, RATTLE).
+// loop as a CUDA graph, one captured step per launch: without constraints the
+// fused kernel (the previous step's closing half-kick, this step's opening
+// one, drift, rebuild check, coordinate pack), an IF node holding the list
+// rebuild, and the forces (pair kernel beside the bonded/1-4 kernel); with
+// constraints half-kick, drift, SHAKE, check, the IF node, forces,
+// half-kick, RATTLE.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -59,13 +63,12 @@ struct gm_ctx {
         *d_cell_start = nullptr, *d_cell_cursor = nullptr, *d_tmp_atom = nullptr, *d_slot_of = nullptr;
     long long total_cells = 0;     // cell budget of all systems
     // systems of a batch (one for a plain context)
-    int n_sys = 1, n_slots = 0, scan_blocks = 0, max_sys_atoms = 0;
+    int n_sys = 1, n_slots = 0, max_sys_atoms = 0;
     std::vector<int> h_atom_off;
     int *d_sys_atom_off = nullptr, *d_sys_slot_off = nullptr, *d_sys_cell_off = nullptr, *d_atom_sys = nullptr,
         *d_group_sys = nullptr;
     unsigned int *d_sys_flag = nullptr;
     long long *d_e_sys = nullptr;  // per-system energies (batches)
-    int *d_scan = nullptr;
     GridInfo *d_grid = nullptr;
     double *d_bbox = nullptr;
     int bbox_blocks = 0;
@@ -230,8 +233,6 @@ ListArgs list_args(gm_ctx *c) {
     a.periodic = c->p.periodic;
     a.bbox_scratch = c->d_bbox;
     a.bbox_blocks = c->bbox_blocks;
-    a.scan_scratch = c->d_scan;
-    a.scan_blocks = c->scan_blocks;
     a.max_sys_atoms = c->max_sys_atoms;
     a.sys_atom_off = c->d_sys_atom_off;
     a.sys_slot_off = c->d_sys_slot_off;
@@ -1367,7 +1368,6 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
                 return bail(GM_ERR_UNSUPPORTED);
             }
             cell_off.push_back(cell_off.back() + (int)cells + 1);
-            c->scan_blocks = std::max(c->scan_blocks, (int)((cells + 1 + 1023) / 1024));
         }
         c->n_slots = slot_off.back();
         c->total_cells = cell_off.back();
@@ -1396,7 +1396,6 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dalloc(c, &c->d_cell_of, (size_t)n));
     TRY(dalloc(c, &c->d_cell_sorted, ns_));
     TRY(dalloc(c, &c->d_tmp_atom, ns_));
-    TRY(dalloc(c, &c->d_scan, (size_t)c->scan_blocks * n_sys));
     TRY(dalloc(c, &c->d_cell_count, (size_t)c->total_cells));
     TRY(dalloc(c, &c->d_cell_cursor, (size_t)c->total_cells));
     TRY(dalloc(c, &c->d_cell_start, (size_t)c->total_cells));

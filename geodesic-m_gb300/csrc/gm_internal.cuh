@@ -178,8 +178,7 @@ struct ListArgs {
     double r_list, box[3];
     int periodic;
     double *bbox_scratch;    // [n_sys][bbox_blocks][9] (min, max, sum per dimension)
-    int *scan_scratch;       // [n_sys][scan_blocks]: one total per 1024 cells
-    int bbox_blocks, scan_blocks, max_sys_atoms;
+    int bbox_blocks, max_sys_atoms;
     // systems: atoms [sys_atom_off[s], +1), slots [sys_slot_off[s], +1) (32-aligned),
     // cells [sys_cell_off[s], +1) (the system's cell budget + 1)
     const int *sys_atom_off, *sys_slot_off, *sys_cell_off;

@@ -211,18 +211,6 @@ __global__ void grid_kernel(ListArgs a, int blocks) {
     }
 }
 
-// Clears the cells the system's new grid uses (the only ones assign and the
-// scan touch), after the grid is laid out.
-__global__ void clear_cells_kernel(ListArgs a) {
-    const int s = blockIdx.y;
-    if (!a.sys_flag[s]) return;
-    const int c0 = a.sys_cell_off[s];
-    const int c1 = c0 + min(a.grid[s].ncell, a.sys_cell_off[s + 1] - c0 - 1);
-    for (int c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += gridDim.x * blockDim.x) {
-        a.cell_count[c] = 0;
-        a.cell_cursor[c] = 0;
-    }
-}
 
 __device__ __forceinline__ int cell_coord(float h, float lo, float inv_w, int nc) {
     float t = floorf((h - lo) * inv_w);
@@ -254,9 +242,8 @@ __global__ void assign_kernel(ListArgs a) {
     }
 }
 
-// Exclusive scan of each system's cell counts into its cell_start[0..ncell],
-// in three launches: per-block scans of 1024 cells with block totals, a scan
-// of the totals per system, then the block offsets added back.
+// Exclusive scan of one value per thread over a block (a multiple of 32
+// threads, at most 1024), with the block total.
 __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int x = v;
@@ -314,44 +301,8 @@ __global__ void __launch_bounds__(1024) scan_cells_kernel(ListArgs a) {
         carry += total;
     }
 }
-__global__ void scan_local_kernel(ListArgs a) {
-    __shared__ int warp_sums[32];
-    const int s = blockIdx.y;
-    if (!a.sys_flag[s]) return;
-    const int ncell = sys_ncell(a, s), coff = a.sys_cell_off[s];
-    if (blockIdx.x * blockDim.x >= ncell + 1) return;  // whole block idle (uniform)
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int v = i < ncell ? a.cell_count[coff + i] : 0;
-    int total;
-    const int excl = block_exclusive_scan(v, warp_sums, total);
-    if (i <= ncell) a.cell_start[coff + i] = excl;
-    if (threadIdx.x == 0) a.scan_scratch[(size_t)s * a.scan_blocks + blockIdx.x] = total;
-}
 
-__global__ void scan_blocks_kernel(ListArgs a) {
-    __shared__ int warp_sums[32];
-    const int s = blockIdx.x;
-    if (!a.sys_flag[s]) return;
-    int *sums = a.scan_scratch + (size_t)s * a.scan_blocks;
-    const int nblocks = (sys_ncell(a, s) + 1 + 1023) / 1024;
-    int carry = 0;
-    for (int base = 0; base < nblocks; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const int v = i < nblocks ? sums[i] : 0;
-        int total;
-        const int excl = block_exclusive_scan(v, warp_sums, total);
-        if (i < nblocks) sums[i] = excl + carry;
-        carry += total;
-    }
-}
 
-__global__ void scan_add_kernel(ListArgs a) {
-    const int s = blockIdx.y;
-    if (!a.sys_flag[s]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= sys_ncell(a, s))
-        a.cell_start[a.sys_cell_off[s] + i] += a.scan_scratch[(size_t)s * a.scan_blocks + blockIdx.x];
-}
 
 __global__ void scatter_kernel(ListArgs a) {
     int a0, a1;

@@ -27,7 +27,6 @@ namespace {
 constexpr int kMaxAtoms = GM_STATIC_MAX_ATOMS;
 constexpr int kMaxCells = 32768;
 constexpr int kBboxBlocks = (kMaxAtoms + 255) / 256;
-constexpr int kScanBlocks = (kMaxCells + 1 + 1023) / 1024 + 1;
 constexpr int kMaxDevices = 64;
 
 // Layout of the scratch array.  What accumulates starts at zero: the status
@@ -39,7 +38,6 @@ struct Scratch {
     GridInfo grid;
     DevStatus status;
     int cell_count[kMaxCells], cell_cursor[kMaxCells], cell_start[kMaxCells + 1];
-    int scan[kScanBlocks];
     int cell_of[kMaxAtoms], tmp_atom[kMaxAtoms], perm[kMaxAtoms], cell_sorted[kMaxAtoms];
     int row_count[kMaxAtoms], row_start[kMaxAtoms + 1];
     // the one system's tables (atoms, slots, cells) and rebuild flag
@@ -258,7 +256,6 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     a.sys_cell_off = S->sys_cell_off;
     a.sys_flag = S->sys_flag;
     a.max_sys_atoms = n;
-    a.scan_blocks = (kMaxCells + 1 + 1023) / 1024;
     a.pos = d_pos;
     a.ref = S->ref;
     a.perm = S->perm;
@@ -274,7 +271,6 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     for (int d = 0; d < 3; d++) a.box[d] = params->box[d];
     a.periodic = params->periodic ? 1 : 0;
     a.bbox_scratch = S->bbox;
-    a.scan_scratch = S->scan;
     a.bbox_blocks = (n + 255) / 256 < kBboxBlocks ? (n + 255) / 256 : kBboxBlocks;
 
     if (cudaMemsetAsync(&S->status, 0, sizeof(DevStatus), s) != cudaSuccess) return GM_ERR_DEVICE;
