@@ -243,6 +243,10 @@ ListArgs list_args(gm_ctx *c) {
     return a;
 }
 
+// periodic && bonded_min_image: bonded, 1-4 and constraint differences at the
+// nearest periodic image
+bool bonded_min_image(const gm_ctx *c) { return c->p.periodic && c->p.bonded_min_image; }
+
 ForceArgs force_args(gm_ctx *c) {
     ForceArgs a{};
     a.n = c->n;
@@ -282,6 +286,7 @@ ForceArgs force_args(gm_ctx *c) {
         a.box64[d] = c->p.box[d];
     }
     a.periodic = c->p.periodic;
+    a.bonded_mi = bonded_min_image(c);
     a.force = c->d_force;
     a.epart = c->d_epart;
     a.status = c->d_status;
@@ -327,6 +332,8 @@ ClusterArgs cluster_args(gm_ctx *c) {
     a.status = c->d_status;
     a.lam_sum = (c->ws_on || c->ws_rec_stride > 0) ? c->d_lam_sum : nullptr;
     a.lam0 = c->ws_on ? c->d_ws_lam0 : nullptr;
+    a.mi = bonded_min_image(c);
+    for (int d = 0; d < 3; d++) a.box64[d] = c->p.box[d];
     return a;
 }
 
@@ -1878,6 +1885,8 @@ int32_t gm_ws_record(gm_ctx *c, int64_t cap_steps, int32_t stride) {
     if (!c) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
     if (!c->n_constr) return fail(c, GM_ERR_UNSUPPORTED, "the system has no constraints");
+    if (bonded_min_image(c) && cap_steps > 0 && stride > 0)
+        return fail(c, GM_ERR_UNSUPPORTED, "the warm start's features take raw position differences: not with bonded_min_image");
     drop_graph(c);
     if (cap_steps <= 0 || stride <= 0) {  // stop; the samples stay for training
         c->ws_rec_stride = 0;
@@ -1951,6 +1960,8 @@ int32_t gm_ws_enable(gm_ctx *c, int32_t on) {
     if (!c) return GM_ERR_INVALID_ARGUMENT;
     if (on && !c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model (train or set one first)");
     if (on && !c->n_constr) return fail(c, GM_ERR_UNSUPPORTED, "the system has no constraints");
+    if (on && bonded_min_image(c))
+        return fail(c, GM_ERR_UNSUPPORTED, "the warm start's features take raw position differences: not with bonded_min_image");
     c->ws_on = on != 0;
     drop_graph(c);
     return GM_OK;

@@ -242,6 +242,34 @@ __device__ __forceinline__ V3<float> fdiff(const ForceArgs &a, int ia, int ib) {
     gm_ld_coord(a.coord + 2 * a.slot_of[ib], hb, lb);
     return {(ha.x - hb.x) + (la.x - lb.x), (ha.y - hb.y) + (la.y - lb.y), (ha.z - hb.z) + (la.z - lb.z)};
 }
+// pos[ia] - pos[ib] in FP64; with MI at the nearest periodic image (the
+// reference's min_image on each component)
+template <bool MI>
+__device__ __forceinline__ V3<double> pdiff(const ForceArgs &a, int ia, int ib) {
+    const int n = a.n;
+    V3<double> d = {a.pos[ia] - a.pos[ib], a.pos[n + ia] - a.pos[n + ib], a.pos[2 * n + ia] - a.pos[2 * n + ib]};
+    if constexpr (MI) {
+        d.x = gm_min_image(d.x, a.box64[0]);
+        d.y = gm_min_image(d.y, a.box64[1]);
+        d.z = gm_min_image(d.z, a.box64[2]);
+    }
+    return d;
+}
+// The T-typed difference a bonded term works in: fdiff (mixed) or the FP64
+// difference, or with MI the nearest-image FP64 difference narrowed to T (the
+// slot copies of two atoms on opposite faces of the box are not close, so
+// fdiff would lose the difference's low bits there)
+template <typename T, bool MI>
+__device__ __forceinline__ V3<T> term_diff(const ForceArgs &a, int ia, int ib) {
+    if constexpr (MI) {
+        const V3<double> d = pdiff<true>(a, ia, ib);
+        return {(T)d.x, (T)d.y, (T)d.z};
+    } else if constexpr (sizeof(T) == sizeof(float)) {
+        return fdiff(a, ia, ib);
+    } else {
+        return diff<T>(a.pos, a.n, ia, ib);
+    }
+}
 template <typename T>
 __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
@@ -261,7 +289,7 @@ __device__ __forceinline__ double gm_acos(double x) { return acos(x); }
 __device__ __forceinline__ float gm_atan2(float y, float x) { return atan2f(y, x); }
 __device__ __forceinline__ double gm_atan2(double y, double x) { return atan2(y, x); }
 
-template <typename T>
+template <typename T, bool MI>
 __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
     constexpr bool kMixed = sizeof(T) == sizeof(float);
     const int t = blk * blockDim.x + threadIdx.x;
@@ -276,7 +304,8 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         // reference's GPU backend also keeps bonded terms in FP64).
         const int i = a.bond_i[t], j = a.bond_j[t];
         first = i;
-        const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
+        const V3<double> bd = pdiff<MI>(a, j, i);
+        const double dx = bd.x, dy = bd.y, dz = bd.z;
         const double k = a.bond_k[t], r0 = a.bond_r0[t];
         const double r2 = dx * dx + dy * dy + dz * dz;
         bool done = false;
@@ -310,9 +339,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         const int q = t - a.n_bonds;
         const int i = a.angle_i[q], j = a.angle_j[q], kk = a.angle_k[q];
         first = i;
-        V3<T> b1, b2;
-        if constexpr (kMixed) { b1 = fdiff(a, i, j); b2 = fdiff(a, kk, j); }
-        else { b1 = diff<T>(a.pos, n, i, j); b2 = diff<T>(a.pos, n, kk, j); }
+        const V3<T> b1 = term_diff<T, MI>(a, i, j), b2 = term_diff<T, MI>(a, kk, j);
         const T r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
         if (kMixed && r1 != (T)0 && r2 != (T)0) {
             // mixed path: theta - theta0 = atan2(sin(theta - theta0),
@@ -321,7 +348,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
             //   |d1||d2| cos(theta - theta0) = (d1 . d2) cos theta0 + |d1 x d2| sin theta0
             // with |d1 x d2| from an FP32 square root and one Newton step in
             // FP64; no FP64 acos, square root or division
-            const V3<double> d1 = diff<double>(a.pos, n, i, j), d2 = diff<double>(a.pos, n, kk, j);
+            const V3<double> d1 = pdiff<MI>(a, i, j), d2 = pdiff<MI>(a, kk, j);
             const double dd = dot(d1, d2);
             const V3<double> cr = cross(d1, d2);
             const double q2 = dot(cr, cr);
@@ -349,7 +376,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
             // theta - theta0 in FP64 in both paths: an FP32 acos is off by
             // ~1e-7 rad, i.e. ~1e-5 kcal/mol/A at k = 50, which a structure
             // near equilibrium cannot absorb
-            const V3<double> d1 = diff<double>(a.pos, n, i, j), d2 = diff<double>(a.pos, n, kk, j);
+            const V3<double> d1 = pdiff<MI>(a, i, j), d2 = pdiff<MI>(a, kk, j);
             double c64 = dot(d1, d2) / sqrt(dot(d1, d1) * dot(d2, d2));
             c64 = c64 < -1.0 ? -1.0 : (c64 > 1.0 ? 1.0 : c64);
             const T c = (T)c64;
@@ -374,9 +401,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         const int q = t - a.n_bonds - a.n_angles;
         const int i = a.dihed_i[q], j = a.dihed_j[q], k = a.dihed_k[q], l = a.dihed_l[q];
         first = i;
-        V3<T> b1, b2, b3;
-        if constexpr (kMixed) { b1 = fdiff(a, j, i); b2 = fdiff(a, k, j); b3 = fdiff(a, l, k); }
-        else { b1 = diff<T>(a.pos, n, j, i); b2 = diff<T>(a.pos, n, k, j); b3 = diff<T>(a.pos, n, l, k); }
+        const V3<T> b1 = term_diff<T, MI>(a, j, i), b2 = term_diff<T, MI>(a, k, j), b3 = term_diff<T, MI>(a, l, k);
         const V3<T> m = cross(b1, b2), nv = cross(b2, b3);
         const T m2 = dot(m, m), n2 = dot(nv, nv), b2l = sqrt(dot(b2, b2));
         if (m2 != (T)0 && n2 != (T)0 && b2l != (T)0) {
@@ -415,7 +440,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
 
 // Scaled 1-4 pairs (beyond the reference): unswitched, no cutoff; LJ scaled by
 // scale14_lj, Coulomb by scale14_coul.  FP64 arithmetic, few pairs.
-template <bool MIXED>
+template <bool MIXED, bool MI>
 __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
     const int t = blk * blockDim.x + threadIdx.x;
     const int n = a.n;
@@ -426,7 +451,7 @@ __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
         // FP32 pair arithmetic as in the pair kernel, on the FP64 difference
         const int i = a.p14_i[t], j = a.p14_j[t];
         first = i;
-        const V3<float> d = fdiff(a, j, i);
+        const V3<float> d = term_diff<float, MI>(a, j, i);
         const float dx = d.x, dy = d.y, dz = d.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 > 0.f) {
@@ -452,7 +477,8 @@ __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
     } else if (!MIXED && t < a.n14) {
         const int i = a.p14_i[t], j = a.p14_j[t];
         first = i;
-        const double dx = a.pos[j] - a.pos[i], dy = a.pos[n + j] - a.pos[n + i], dz = a.pos[2 * n + j] - a.pos[2 * n + i];
+        const V3<double> d = pdiff<MI>(a, j, i);
+        const double dx = d.x, dy = d.y, dz = d.z;
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 > 0.0) {
             const double r = sqrt(r2), rinv = 1.0 / r;
@@ -487,16 +513,16 @@ __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
     if (bad && (threadIdx.x & 31) == 0) atomicOr(&a.status->error, bad);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) { bonded_block<T>(a, blockIdx.x); }
-template <bool MIXED>
-__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) { pair14_block<MIXED>(a, blockIdx.x); }
+template <typename T, bool MI>
+__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) { bonded_block<T, MI>(a, blockIdx.x); }
+template <bool MIXED, bool MI>
+__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) { pair14_block<MIXED, MI>(a, blockIdx.x); }
 // Both in one launch: the first bonded_blocks blocks take the bonded terms,
 // the rest the 1-4 pairs (independent work; integer force sums).
-template <typename T, bool MIXED>
+template <typename T, bool MIXED, bool MI>
 __global__ void __launch_bounds__(256) bonded_pair14_kernel(ForceArgs a) {
-    if ((int)blockIdx.x < a.bonded_blocks) bonded_block<T>(a, blockIdx.x);
-    else pair14_block<MIXED>(a, blockIdx.x - a.bonded_blocks);
+    if ((int)blockIdx.x < a.bonded_blocks) bonded_block<T, MI>(a, blockIdx.x);
+    else pair14_block<MIXED, MI>(a, blockIdx.x - a.bonded_blocks);
 }
 
 // Fixed-order sum of all energy partials (pair groups, bonded blocks, 1-4
@@ -553,21 +579,36 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
 
 void gm_launch_bonded(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.bonded_blocks == 0) return;
-    if (fp64) bonded_kernel<double><<<a.bonded_blocks, 256, 0, s>>>(a);
-    else bonded_kernel<float><<<a.bonded_blocks, 256, 0, s>>>(a);
+    if (a.bonded_mi) {
+        if (fp64) bonded_kernel<double, true><<<a.bonded_blocks, 256, 0, s>>>(a);
+        else bonded_kernel<float, true><<<a.bonded_blocks, 256, 0, s>>>(a);
+    } else {
+        if (fp64) bonded_kernel<double, false><<<a.bonded_blocks, 256, 0, s>>>(a);
+        else bonded_kernel<float, false><<<a.bonded_blocks, 256, 0, s>>>(a);
+    }
 }
 
 void gm_launch_bonded_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {
     const int blocks = a.bonded_blocks + a.blocks14;
     if (blocks == 0) return;
-    if (fp64) bonded_pair14_kernel<double, false><<<blocks, 256, 0, s>>>(a);
-    else bonded_pair14_kernel<float, true><<<blocks, 256, 0, s>>>(a);
+    if (a.bonded_mi) {
+        if (fp64) bonded_pair14_kernel<double, false, true><<<blocks, 256, 0, s>>>(a);
+        else bonded_pair14_kernel<float, true, true><<<blocks, 256, 0, s>>>(a);
+    } else {
+        if (fp64) bonded_pair14_kernel<double, false, false><<<blocks, 256, 0, s>>>(a);
+        else bonded_pair14_kernel<float, true, false><<<blocks, 256, 0, s>>>(a);
+    }
 }
 
 void gm_launch_pair14(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.blocks14 == 0) return;
-    if (fp64) pair14_kernel<false><<<a.blocks14, 256, 0, s>>>(a);
-    else pair14_kernel<true><<<a.blocks14, 256, 0, s>>>(a);
+    if (a.bonded_mi) {
+        if (fp64) pair14_kernel<false, true><<<a.blocks14, 256, 0, s>>>(a);
+        else pair14_kernel<true, true><<<a.blocks14, 256, 0, s>>>(a);
+    } else {
+        if (fp64) pair14_kernel<false, false><<<a.blocks14, 256, 0, s>>>(a);
+        else pair14_kernel<true, false><<<a.blocks14, 256, 0, s>>>(a);
+    }
 }
 
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s) {

@@ -98,6 +98,16 @@ __global__ void check_kernel(int n, const double *pos, const double *ref, double
     }
 }
 
+// The position difference a - b along axis d of a constraint: raw (the
+// reference), or at the nearest periodic image when c.mi (bonded_min_image).
+// Exact arithmetic (this file builds without FMA contraction), so the raw
+// difference is the same bits as before the option existed and the image
+// form those of the restated min_image.
+__device__ __forceinline__ double cdiff(const ClusterArgs &c, double a, double b, int d) {
+    const double v = a - b;
+    return c.mi ? gm_min_image(v, c.box64[d]) : v;
+}
+
 // One Jacobi iteration over a cluster.  Returns max|lambda| and its
 // constraint (first in ascending order, as the reference's strict '>').
 __device__ void shake_iteration(const ClusterArgs &c, int cl, const double *rvec, double *pos, int n_atoms,
@@ -109,9 +119,9 @@ __device__ void shake_iteration(const ClusterArgs &c, int cl, const double *rvec
     for (int q = c0; q < c1; q++) {
         const int k = c.cl_cons[q];
         const int i = c.constr_i[k], j = c.constr_j[k];
-        const double dx = pos[i] - pos[j];
-        const double dy = pos[n_atoms + i] - pos[n_atoms + j];
-        const double dz = pos[2 * n_atoms + i] - pos[2 * n_atoms + j];
+        const double dx = cdiff(c, pos[i], pos[j], 0);
+        const double dy = cdiff(c, pos[n_atoms + i], pos[n_atoms + j], 1);
+        const double dz = cdiff(c, pos[2 * n_atoms + i], pos[2 * n_atoms + j], 2);
         const double diff = dx * dx + dy * dy + dz * dz - c.constr_dsq[k];
         const double rx = rvec[k], ry = rvec[nc + k], rz = rvec[2 * nc + k];
         const double inv_mi = c.inv_mass[i], inv_mj = c.inv_mass[j];
@@ -153,9 +163,9 @@ __device__ void rattle_iteration(const ClusterArgs &c, int cl, const double *pos
     for (int q = c0; q < c1; q++) {
         const int k = c.cl_cons[q];
         const int i = c.constr_i[k], j = c.constr_j[k];
-        const double rx = pos[i] - pos[j];
-        const double ry = pos[n_atoms + i] - pos[n_atoms + j];
-        const double rz = pos[2 * n_atoms + i] - pos[2 * n_atoms + j];
+        const double rx = cdiff(c, pos[i], pos[j], 0);
+        const double ry = cdiff(c, pos[n_atoms + i], pos[n_atoms + j], 1);
+        const double rz = cdiff(c, pos[2 * n_atoms + i], pos[2 * n_atoms + j], 2);
         const double rsq = rx * rx + ry * ry + rz * rz;
         const double dvx = vel[i] - vel[j];
         const double dvy = vel[n_atoms + i] - vel[n_atoms + j];
@@ -197,9 +207,9 @@ __global__ void shake_prepare(ClusterArgs c, const double *dref, int n_atoms) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n_constr) return;
     const int i = c.constr_i[k], j = c.constr_j[k];
-    c.rvec[k] = dref[i] - dref[j];
-    c.rvec[c.n_constr + k] = dref[n_atoms + i] - dref[n_atoms + j];
-    c.rvec[2 * c.n_constr + k] = dref[2 * n_atoms + i] - dref[2 * n_atoms + j];
+    c.rvec[k] = cdiff(c, dref[i], dref[j], 0);
+    c.rvec[c.n_constr + k] = cdiff(c, dref[n_atoms + i], dref[n_atoms + j], 1);
+    c.rvec[2 * c.n_constr + k] = cdiff(c, dref[2 * n_atoms + i], dref[2 * n_atoms + j], 2);
     if (c.lam_sum) c.lam_sum[k] = 0.0;
 }
 
@@ -254,9 +264,9 @@ __device__ void cluster_star(const ClusterArgs &c, int cl, double *pos, double *
                 wq[q] = 2.0 * (inv_mi + inv_mj);
             } else {
                 const int i = cen_i[q] ? cen : h, j = cen_i[q] ? h : cen;
-                rx[q] = pos[i] - pos[j];
-                ry[q] = pos[n + i] - pos[n + j];
-                rz[q] = pos[2 * n + i] - pos[2 * n + j];
+                rx[q] = cdiff(c, pos[i], pos[j], 0);
+                ry[q] = cdiff(c, pos[n + i], pos[n + j], 1);
+                rz[q] = cdiff(c, pos[2 * n + i], pos[2 * n + j], 2);
                 const double rsq = rx[q] * rx[q] + ry[q] * ry[q] + rz[q] * rz[q];
                 wq[q] = (inv_mi + inv_mj) * rsq;
                 dsq[q] = 0.0;
@@ -306,9 +316,9 @@ __device__ void cluster_star(const ClusterArgs &c, int cl, double *pos, double *
                         const double rel_vel = dvx * rx[q] + dvy * ry[q] + dvz * rz[q];
                         l_ = wq[q] == 0.0 ? 0.0 : rel_vel / wq[q];
                     } else {
-                        const double dx = xi - xj;
-                        const double dy = yi - yj;
-                        const double dz = zi - zj;
+                        const double dx = cdiff(c, xi, xj, 0);
+                        const double dy = cdiff(c, yi, yj, 1);
+                        const double dz = cdiff(c, zi, zj, 2);
                         const double diff = dx * dx + dy * dy + dz * dz - dsq[q];
                         const double dot_new_old = dx * rx[q] + dy * ry[q] + dz * rz[q];
                         const double denom = wq[q] * dot_new_old;
@@ -472,9 +482,9 @@ __device__ void cluster_warp(const ClusterArgs &c, int cl, double *pos, double *
             wq = 2.0 * (inv_mi + inv_mj);
         } else {
             // constraint.rs:205-215: the bond vector of the fixed positions
-            rx = pos[i] - pos[j];
-            ry = pos[n + i] - pos[n + j];
-            rz = pos[2 * n + i] - pos[2 * n + j];
+            rx = cdiff(c, pos[i], pos[j], 0);
+            ry = cdiff(c, pos[n + i], pos[n + j], 1);
+            rz = cdiff(c, pos[2 * n + i], pos[2 * n + j], 2);
             const double rsq = rx * rx + ry * ry + rz * rz;
             wq = (inv_mi + inv_mj) * rsq;
         }
@@ -517,9 +527,9 @@ __device__ void cluster_warp(const ClusterArgs &c, int cl, double *pos, double *
                 const double rel_vel = dvx * rx + dvy * ry + dvz * rz;
                 l_ = wq == 0.0 ? 0.0 : rel_vel / wq;
             } else {
-                const double dx = xi - xj;
-                const double dy = yi - yj;
-                const double dz = zi - zj;
+                const double dx = cdiff(c, xi, xj, 0);
+                const double dy = cdiff(c, yi, yj, 1);
+                const double dz = cdiff(c, zi, zj, 2);
                 const double diff = dx * dx + dy * dy + dz * dz - dsq;
                 const double dot_new_old = dx * rx + dy * ry + dz * rz;
                 const double denom = wq * dot_new_old;
@@ -601,9 +611,9 @@ __device__ void cluster_single(const ClusterArgs &c, int cl, double *pos, double
         rx = c.rvec[k]; ry = c.rvec[ncst + k]; rz = c.rvec[2 * ncst + k];
         wq = 2.0 * (inv_mi + inv_mj);
     } else {
-        rx = pos[i] - pos[j];
-        ry = pos[n + i] - pos[n + j];
-        rz = pos[2 * n + i] - pos[2 * n + j];
+        rx = cdiff(c, pos[i], pos[j], 0);
+        ry = cdiff(c, pos[n + i], pos[n + j], 1);
+        rz = cdiff(c, pos[2 * n + i], pos[2 * n + j], 2);
         const double rsq = rx * rx + ry * ry + rz * rz;
         wq = (inv_mi + inv_mj) * rsq;
     }
@@ -637,9 +647,9 @@ __device__ void cluster_single(const ClusterArgs &c, int cl, double *pos, double
             const double rel_vel = dvx * rx + dvy * ry + dvz * rz;
             l_ = wq == 0.0 ? 0.0 : rel_vel / wq;
         } else {
-            const double dx = xi - xj;
-            const double dy = yi - yj;
-            const double dz = zi - zj;
+            const double dx = cdiff(c, xi, xj, 0);
+            const double dy = cdiff(c, yi, yj, 1);
+            const double dz = cdiff(c, zi, zj, 2);
             const double diff = dx * dx + dy * dy + dz * dz - dsq;
             const double dot_new_old = dx * rx + dy * ry + dz * rz;
             const double denom = wq * dot_new_old;

@@ -218,6 +218,7 @@ struct ForceArgs {
     float box[3], inv_box[3];
     double box64[3];
     int periodic;
+    int bonded_mi;  // periodic && bonded_min_image: bonded and 1-4 differences at the nearest image
     long long *force;
     double *epart;           // per pair-kernel warp (n_groups * split), then bonded, then 1-4
     DevStatus *status;
@@ -270,7 +271,13 @@ struct ClusterArgs {
     unsigned int max_iter;
     double tol;
     DevStatus *status;
+    int mi;                               // constraint differences at the nearest image of box64
+    double box64[3];
 };
+
+// d taken to the nearest periodic image of a box of length L: the reference's
+// min_image, d - L * round(d / L) with round half away from zero
+__device__ __forceinline__ double gm_min_image(double d, double L) { return d - L * round(d / L); }
 
 void gm_launch_half_kick(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          const DevStatus *st, cudaStream_t s);

@@ -75,7 +75,8 @@ class GmParams(C.Structure):
     _fields_ = [("box", C.c_double * 3), ("periodic", C.c_int32), ("precision", C.c_int32),
                 ("r_cutoff", C.c_double), ("r_skin", C.c_double), ("r_switch", C.c_double),
                 ("max_constr_iter", C.c_uint32), ("constr_tol", C.c_double), ("coulomb", C.c_int32),
-                ("scale14_lj", C.c_double), ("scale14_coul", C.c_double), ("device", C.c_int32)]
+                ("scale14_lj", C.c_double), ("scale14_coul", C.c_double), ("device", C.c_int32),
+                ("bonded_min_image", C.c_int32)]
 
 
 class GmConvergence(C.Structure):
@@ -100,11 +101,13 @@ class SimParams:
     scale14_lj: float = 0.0
     scale14_coul: float = 0.0
     device: int = 0
+    # with periodic: bonded, 1-4 and constraint differences at the nearest image
+    bonded_min_image: bool = False
 
     def to_c(self) -> GmParams:
         return GmParams((C.c_double * 3)(*self.box_size), int(self.periodic), int(self.precision), self.r_cutoff,
                         self.r_skin, self.r_switch, int(self.max_constr_iter), self.constr_tol, int(self.coulomb),
-                        self.scale14_lj, self.scale14_coul, int(self.device))
+                        self.scale14_lj, self.scale14_coul, int(self.device), int(self.bonded_min_image))
 
 
 _lib = None

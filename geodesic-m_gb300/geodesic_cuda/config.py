@@ -17,7 +17,10 @@ Additions (keys the reference does not know, so its parser rejects them):
   backend = "cuda"  the device-resident backend of this package;
   [cuda]         optional: precision ("mixed" | "fp64", default "mixed"),
                  frames_per_batch (u32 >= 1, default 64: trajectory frames the
-                 device buffers between host reads);
+                 device buffers between host reads), bonded_min_image (bool,
+                 default false: with `periodic`, bonded, 1-4 and constraint
+                 differences at the nearest image, which the reference leaves
+                 raw);
   [[system]]     an array of system tables runs its systems as one batch in
                  one device context (gm_create_ensemble).  Each entry has the
                  [system] keys plus an optional `name` (default: its index);
@@ -170,7 +173,8 @@ _CONSTRAINTS = _struct([("max_iter", (_uint(32, "u32"), _REQUIRED)), ("tolerance
 _OUTPUT = _struct([("trajectory", (_string, _REQUIRED)), ("energy_log", (_string, _REQUIRED))], "RawOutput")
 _MONITORING = _struct([("energy_drift_threshold_kcal", (_f64, _REQUIRED)),
                        ("energy_drift_action", (_string, _REQUIRED))], "RawMonitoring")
-_CUDA = _struct([("precision", (_string, "mixed")), ("frames_per_batch", (_uint(32, "u32"), 64))], "RawCuda")
+_CUDA = _struct([("precision", (_string, "mixed")), ("frames_per_batch", (_uint(32, "u32"), 64)),
+                 ("bonded_min_image", (_bool, False))], "RawCuda")
 
 
 def _system_or_batch(v, key):
@@ -243,6 +247,7 @@ class Config:
     monitoring: MonitoringConfig | None
     precision: str = "mixed"
     frames_per_batch: int = 64
+    bonded_min_image: bool = False
 
     # the reference's single-system fields
     @property
@@ -287,7 +292,7 @@ class Config:
         entries, batch = raw["system"]
         systems = [SystemConfig(e.get("name") if e.get("name") is not None else str(k), e["prmtop"], e["inpcrd"],
                                 e["box_size"], e["periodic"]) for k, e in enumerate(entries)]
-        cuda = raw["cuda"] or {"precision": "mixed", "frames_per_batch": 64}
+        cuda = raw["cuda"] or {"precision": "mixed", "frames_per_batch": 64, "bonded_min_image": False}
         integ, nb, con, out = raw["integrator"], raw["nonbonded"], raw["constraints"], raw["output"]
         c = cls(n_steps=run["n_steps"], frame_interval=run["frame_interval"], backend=backend,
                 n_threads=run["n_threads"], systems=systems, batch=batch, dt=integ["dt"],
@@ -295,7 +300,7 @@ class Config:
                 r_switch=nb["r_switch"], max_constr_iter=con["max_iter"], constr_tol=con["tolerance"],
                 constrain_hydrogens=con["constrain_hydrogens"], trajectory=out["trajectory"],
                 energy_log=out["energy_log"], monitoring=monitoring, precision=cuda["precision"],
-                frames_per_batch=cuda["frames_per_batch"])
+                frames_per_batch=cuda["frames_per_batch"], bonded_min_image=cuda["bonded_min_image"])
         _validate(c)
         return c
 
@@ -314,7 +319,8 @@ class Config:
         return _be.SimParams(box_size=tuple(self.box_size), periodic=self.periodic, r_cutoff=self.r_cutoff,
                              r_skin=self.r_skin, r_switch=self.r_switch, max_constr_iter=self.max_constr_iter,
                              constr_tol=self.constr_tol,
-                             precision=_be.PRECISION_FP64 if self.precision == "fp64" else _be.PRECISION_MIXED)
+                             precision=_be.PRECISION_FP64 if self.precision == "fp64" else _be.PRECISION_MIXED,
+                             bonded_min_image=self.bonded_min_image)
 
 
 def _validate(c: Config) -> None:

@@ -76,6 +76,13 @@ typedef struct {
     int32_t coulomb;          /* q_i q_j 332.0522173 / r with the LJ switch */
     double scale14_lj, scale14_coul;
     int32_t device;           /* CUDA device ordinal */
+    /* beyond the reference: with periodic, the displacement between the two
+     * atoms of a bond, angle arm, dihedral bond vector, 1-4 pair or
+     * constraint goes to the nearest periodic image, d - L round(d / L), the
+     * reference's min_image (neighbor.rs:74-76) that its bonded and
+     * constraint terms leave out (memory.md:140-144).  0 = off = reference.
+     * The SHAKE warm start (gm_ws_record, gm_ws_enable) is unsupported with it. */
+    int32_t bonded_min_image;
 } gm_params;
 
 /* ConvergenceError::ConstraintSolver (geodesic-core/src/error.rs:50-63). */

@@ -21,6 +21,15 @@
 /* neighbor.rs:74-76 — Rust f64::round is half-away-from-zero, i.e. C round(). */
 double or_min_image(double d, double box_len) { return d - box_len * round(d / box_len); }
 
+/* Beyond reference: with a box (periodic + bonded_min_image), the
+ * displacement between the two atoms of a bond, an angle arm, a dihedral
+ * bond vector, a 1-4 pair or a constraint goes to the nearest image with the
+ * reference's min_image expression (neighbor.rs:74-76); the reference keeps
+ * them raw (memory.md:140-144).  NULL box: the raw difference, unchanged. */
+static double bdiff(double d, const double *mi_box, int c) { return mi_box ? or_min_image(d, mi_box[c]) : d; }
+
+static const double *mi_box_of(const or_params *p) { return (p->periodic && p->bonded_min_image) ? p->box : NULL; }
+
 /* neighbor.rs:86-88 */
 double or_wrap_coord(double x, double box_len) { return x - box_len * floor(x / box_len); }
 
@@ -330,14 +339,15 @@ int64_t or_pairs14(const or_topology *t, int64_t n_atoms, int64_t cap, uint32_t 
     return count;
 }
 
-double or_pair14_forces(const double *px, const double *py, const double *pz, const or_atoms *a,
-                        const uint32_t *p14_i, const uint32_t *p14_j, int64_t n14,
-                        double scale_lj, double scale_coul, int32_t coulomb,
-                        double *fx, double *fy, double *fz) {
+double or_pair14_forces_box(const double *px, const double *py, const double *pz, const or_atoms *a,
+                            const uint32_t *p14_i, const uint32_t *p14_j, int64_t n14,
+                            double scale_lj, double scale_coul, int32_t coulomb, const double *mi_box,
+                            double *fx, double *fy, double *fz) {
     double potential = 0.0;
     for (int64_t k = 0; k < n14; k++) {
         uint32_t i = p14_i[k], j = p14_j[k];
-        double dx = px[j] - px[i], dy = py[j] - py[i], dz = pz[j] - pz[i];
+        double dx = bdiff(px[j] - px[i], mi_box, 0), dy = bdiff(py[j] - py[i], mi_box, 1);
+        double dz = bdiff(pz[j] - pz[i], mi_box, 2);
         double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 == 0.0) continue;
         double r = sqrt(r2);
@@ -362,18 +372,25 @@ double or_pair14_forces(const double *px, const double *py, const double *pz, co
     return potential;
 }
 
+double or_pair14_forces(const double *px, const double *py, const double *pz, const or_atoms *a,
+                        const uint32_t *p14_i, const uint32_t *p14_j, int64_t n14,
+                        double scale_lj, double scale_coul, int32_t coulomb,
+                        double *fx, double *fy, double *fz) {
+    return or_pair14_forces_box(px, py, pz, a, p14_i, p14_j, n14, scale_lj, scale_coul, coulomb, NULL, fx, fy, fz);
+}
+
 /* -------------------------------------------------------------- bonded */
 
-double or_bond_forces(const double *px, const double *py, const double *pz, const or_topology *t,
-                      double *fx, double *fy, double *fz) {
+double or_bond_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                          const double *mi_box, double *fx, double *fy, double *fz) {
     /* force/bonded.rs:5-40 */
     double potential = 0.0;
     for (int64_t n = 0; n < t->n_bonds; n++) {
         uint32_t i = t->bond_i[n], j = t->bond_j[n];
         double k = t->bond_k[n], r0 = t->bond_r0[n];
-        double dx = px[j] - px[i];
-        double dy = py[j] - py[i];
-        double dz = pz[j] - pz[i];
+        double dx = bdiff(px[j] - px[i], mi_box, 0);
+        double dy = bdiff(py[j] - py[i], mi_box, 1);
+        double dz = bdiff(pz[j] - pz[i], mi_box, 2);
         double r = sqrt(dx * dx + dy * dy + dz * dz);
         if (r == 0.0) continue;
         double dv_dr = 2.0 * k * (r - r0);
@@ -385,6 +402,11 @@ double or_bond_forces(const double *px, const double *py, const double *pz, cons
     return potential;
 }
 
+double or_bond_forces(const double *px, const double *py, const double *pz, const or_topology *t,
+                      double *fx, double *fy, double *fz) {
+    return or_bond_forces_box(px, py, pz, t, NULL, fx, fy, fz);
+}
+
 static double clamp_rs(double x, double lo, double hi) {
     /* Rust f64::clamp: NaN passes through */
     if (x < lo) x = lo;
@@ -392,15 +414,17 @@ static double clamp_rs(double x, double lo, double hi) {
     return x;
 }
 
-double or_angle_forces(const double *px, const double *py, const double *pz, const or_topology *t,
-                       double *fx, double *fy, double *fz) {
+double or_angle_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                           const double *mi_box, double *fx, double *fy, double *fz) {
     /* force/bonded.rs:44-102 */
     double potential = 0.0;
     for (int64_t n = 0; n < t->n_angles; n++) {
         uint32_t i = t->angle_i[n], j = t->angle_j[n], kk = t->angle_k[n];
         double k_const = t->angle_kth[n], theta0 = t->angle_th0[n];
-        double b1[3] = {px[i] - px[j], py[i] - py[j], pz[i] - pz[j]};
-        double b2[3] = {px[kk] - px[j], py[kk] - py[j], pz[kk] - pz[j]};
+        double b1[3] = {bdiff(px[i] - px[j], mi_box, 0), bdiff(py[i] - py[j], mi_box, 1),
+                        bdiff(pz[i] - pz[j], mi_box, 2)};
+        double b2[3] = {bdiff(px[kk] - px[j], mi_box, 0), bdiff(py[kk] - py[j], mi_box, 1),
+                        bdiff(pz[kk] - pz[j], mi_box, 2)};
         double r1 = sqrt(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
         double r2 = sqrt(b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2]);
         if (r1 == 0.0 || r2 == 0.0) continue;
@@ -423,6 +447,11 @@ double or_angle_forces(const double *px, const double *py, const double *pz, con
     return potential;
 }
 
+double or_angle_forces(const double *px, const double *py, const double *pz, const or_topology *t,
+                       double *fx, double *fy, double *fz) {
+    return or_angle_forces_box(px, py, pz, t, NULL, fx, fy, fz);
+}
+
 static void v_sub(const double *a, const double *b, double *o) { o[0] = a[0] - b[0]; o[1] = a[1] - b[1]; o[2] = a[2] - b[2]; }
 static void v_add(const double *a, const double *b, double *o) { o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2]; }
 static void v_cross(const double *a, const double *b, double *o) {
@@ -433,8 +462,8 @@ static void v_cross(const double *a, const double *b, double *o) {
 static double v_dot(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 static void v_scale(const double *a, double s, double *o) { o[0] = a[0] * s; o[1] = a[1] * s; o[2] = a[2] * s; }
 
-double or_dihedral_forces(const double *px, const double *py, const double *pz, const or_topology *t,
-                          double *fx, double *fy, double *fz) {
+double or_dihedral_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                              const double *mi_box, double *fx, double *fy, double *fz) {
     /* force/bonded.rs:112-164 */
     double potential = 0.0;
     for (int64_t n = 0; n < t->n_diheds; n++) {
@@ -448,6 +477,11 @@ double or_dihedral_forces(const double *px, const double *py, const double *pz, 
         v_sub(pj, pi_, b1);
         v_sub(pk, pj, b2);
         v_sub(pl, pk, b3);
+        for (int c = 0; c < 3; c++) {
+            b1[c] = bdiff(b1[c], mi_box, c);
+            b2[c] = bdiff(b2[c], mi_box, c);
+            b3[c] = bdiff(b3[c], mi_box, c);
+        }
         v_cross(b1, b2, m);
         v_cross(b2, b3, nv);
         double m_len2 = v_dot(m, m);
@@ -480,13 +514,19 @@ double or_dihedral_forces(const double *px, const double *py, const double *pz, 
     return potential;
 }
 
+double or_dihedral_forces(const double *px, const double *py, const double *pz, const or_topology *t,
+                          double *fx, double *fy, double *fz) {
+    return or_dihedral_forces_box(px, py, pz, t, NULL, fx, fy, fz);
+}
+
 /* ---------------------------------------------------------- constraints */
 
-int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
-                               const double *rx, const double *ry, const double *rz,
-                               double *px, double *py, double *pz,
-                               uint32_t max_iter, double tol, uint64_t step,
-                               const double *lam0, double *lam_out, or_convergence_error *err) {
+int64_t or_constraint_solve_box(const or_topology *t, const or_atoms *a,
+                                const double *rx, const double *ry, const double *rz,
+                                double *px, double *py, double *pz,
+                                uint32_t max_iter, double tol, uint64_t step,
+                                const double *lam0, double *lam_out, const double *mi_box,
+                                or_convergence_error *err) {
     /* constraint.rs:62-152 */
     int64_t n_constr = t->n_constr;
     if (n_constr == 0) return 0;
@@ -499,7 +539,8 @@ int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
          * update formula as a Jacobi sweep (constraint.rs:116-121, 130-134) */
         for (int64_t c = 0; c < n_constr; c++) {
             uint32_t i = t->constr_i[c], j = t->constr_j[c];
-            double rxx = rx[i] - rx[j], ryy = ry[i] - ry[j], rzz = rz[i] - rz[j];
+            double rxx = bdiff(rx[i] - rx[j], mi_box, 0), ryy = bdiff(ry[i] - ry[j], mi_box, 1);
+            double rzz = bdiff(rz[i] - rz[j], mi_box, 2);
             double inv_mi = 1.0 / a->mass[i], inv_mj = 1.0 / a->mass[j];
             double lambda = lam0[c];
             dx_[i] -= lambda * inv_mi * rxx; dy_[i] -= lambda * inv_mi * ryy; dz_[i] -= lambda * inv_mi * rzz;
@@ -516,13 +557,13 @@ int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
         for (int64_t c = 0; c < n_constr; c++) {
             uint32_t i = t->constr_i[c], j = t->constr_j[c];
             double dsq_target = t->constr_dsq[c];
-            double dx = px[i] - px[j];
-            double dy = py[i] - py[j];
-            double dz = pz[i] - pz[j];
+            double dx = bdiff(px[i] - px[j], mi_box, 0);
+            double dy = bdiff(py[i] - py[j], mi_box, 1);
+            double dz = bdiff(pz[i] - pz[j], mi_box, 2);
             double diff = dx * dx + dy * dy + dz * dz - dsq_target;
-            double rxx = rx[i] - rx[j];
-            double ryy = ry[i] - ry[j];
-            double rzz = rz[i] - rz[j];
+            double rxx = bdiff(rx[i] - rx[j], mi_box, 0);
+            double ryy = bdiff(ry[i] - ry[j], mi_box, 1);
+            double rzz = bdiff(rz[i] - rz[j], mi_box, 2);
             double inv_mi = 1.0 / a->mass[i];
             double inv_mj = 1.0 / a->mass[j];
             double dot_new_old = dx * rxx + dy * ryy + dz * rzz;
@@ -546,17 +587,26 @@ int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
     return -1;
 }
 
+int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
+                               const double *rx, const double *ry, const double *rz,
+                               double *px, double *py, double *pz,
+                               uint32_t max_iter, double tol, uint64_t step,
+                               const double *lam0, double *lam_out, or_convergence_error *err) {
+    return or_constraint_solve_box(t, a, rx, ry, rz, px, py, pz, max_iter, tol, step, lam0, lam_out, NULL, err);
+}
+
 int64_t or_constraint_solve(const or_topology *t, const or_atoms *a,
                             const double *rx, const double *ry, const double *rz,
                             double *px, double *py, double *pz,
                             uint32_t max_iter, double tol, uint64_t step, or_convergence_error *err) {
-    return or_constraint_solve_ws(t, a, rx, ry, rz, px, py, pz, max_iter, tol, step, NULL, NULL, err);
+    return or_constraint_solve_box(t, a, rx, ry, rz, px, py, pz, max_iter, tol, step, NULL, NULL, NULL, err);
 }
 
-int64_t or_constrain_velocities(const or_topology *t, const or_atoms *a,
-                                const double *px, const double *py, const double *pz,
-                                double *vx, double *vy, double *vz,
-                                uint32_t max_iter, double tol, uint64_t step, or_convergence_error *err) {
+int64_t or_constrain_velocities_box(const or_topology *t, const or_atoms *a,
+                                    const double *px, const double *py, const double *pz,
+                                    double *vx, double *vy, double *vz,
+                                    uint32_t max_iter, double tol, uint64_t step, const double *mi_box,
+                                    or_convergence_error *err) {
     /* constraint.rs:170-259 */
     int64_t n_constr = t->n_constr;
     if (n_constr == 0) return 0;
@@ -571,9 +621,9 @@ int64_t or_constrain_velocities(const or_topology *t, const or_atoms *a,
         int64_t w0 = 0, w1 = 0, w2 = 0;
         for (int64_t c = 0; c < n_constr; c++) {
             uint32_t i = t->constr_i[c], j = t->constr_j[c];
-            double rxx = px[i] - px[j];
-            double ryy = py[i] - py[j];
-            double rzz = pz[i] - pz[j];
+            double rxx = bdiff(px[i] - px[j], mi_box, 0);
+            double ryy = bdiff(py[i] - py[j], mi_box, 1);
+            double rzz = bdiff(pz[i] - pz[j], mi_box, 2);
             double rsq = rxx * rxx + ryy * ryy + rzz * rzz;
             double dvx = vx[i] - vx[j];
             double dvy = vy[i] - vy[j];
@@ -600,6 +650,13 @@ int64_t or_constrain_velocities(const or_topology *t, const or_atoms *a,
     return -1;
 }
 
+int64_t or_constrain_velocities(const or_topology *t, const or_atoms *a,
+                                const double *px, const double *py, const double *pz,
+                                double *vx, double *vy, double *vz,
+                                uint32_t max_iter, double tol, uint64_t step, or_convergence_error *err) {
+    return or_constrain_velocities_box(t, a, px, py, pz, vx, vy, vz, max_iter, tol, step, NULL, err);
+}
+
 /* ---------------------------------------------------------- integrator */
 
 #define FORCE_TO_ACCEL_ANG_PER_PS2 (20.455 * 20.455) /* integrator.rs:9 */
@@ -615,10 +672,10 @@ void or_half_kick(int64_t n, double *vx, double *vy, double *vz,
     }
 }
 
-int64_t or_drift_and_constrain(int64_t n, double *px, double *py, double *pz,
-                               double *vx, double *vy, double *vz, const or_topology *t, const or_atoms *a,
-                               double dt, uint32_t max_iter, double tol, uint64_t step,
-                               or_convergence_error *err) {
+int64_t or_drift_and_constrain_box(int64_t n, double *px, double *py, double *pz,
+                                   double *vx, double *vy, double *vz, const or_topology *t, const or_atoms *a,
+                                   double dt, uint32_t max_iter, double tol, uint64_t step, const double *mi_box,
+                                   or_convergence_error *err) {
     /* integrator.rs:32-71 */
     double *ref = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * 3);
     double *rx = ref, *ry = ref + n, *rz = ref + 2 * n;
@@ -630,7 +687,8 @@ int64_t or_drift_and_constrain(int64_t n, double *px, double *py, double *pz,
         py[i] += dt * vy[i];
         pz[i] += dt * vz[i];
     }
-    int64_t iters = or_constraint_solve(t, a, rx, ry, rz, px, py, pz, max_iter, tol, step, err);
+    int64_t iters = or_constraint_solve_box(t, a, rx, ry, rz, px, py, pz, max_iter, tol, step, NULL, NULL, mi_box,
+                                            err);
     if (iters < 0) { free(ref); return iters; }
     for (int64_t i = 0; i < n; i++) {
         vx[i] = (px[i] - rx[i]) / dt;
@@ -639,6 +697,13 @@ int64_t or_drift_and_constrain(int64_t n, double *px, double *py, double *pz,
     }
     free(ref);
     return iters;
+}
+
+int64_t or_drift_and_constrain(int64_t n, double *px, double *py, double *pz,
+                               double *vx, double *vy, double *vz, const or_topology *t, const or_atoms *a,
+                               double dt, uint32_t max_iter, double tol, uint64_t step,
+                               or_convergence_error *err) {
+    return or_drift_and_constrain_box(n, px, py, pz, vx, vy, vz, t, a, dt, max_iter, tol, step, NULL, err);
 }
 
 double or_kinetic_energy(int64_t n, const double *vx, const double *vy, const double *vz, const double *mass) {
@@ -782,12 +847,13 @@ double or_backend_compute_forces(or_backend *b, const double *px, const double *
     double *bf = b->bonded_buf;
     memset(bf, 0, sizeof(double) * (size_t)n * 3);
     double potential = 0.0;
-    potential += or_bond_forces(px, py, pz, &b->topo, bf, bf + n, bf + 2 * n);
-    potential += or_angle_forces(px, py, pz, &b->topo, bf, bf + n, bf + 2 * n);
-    potential += or_dihedral_forces(px, py, pz, &b->topo, bf, bf + n, bf + 2 * n);
+    const double *mb = mi_box_of(&b->params);
+    potential += or_bond_forces_box(px, py, pz, &b->topo, mb, bf, bf + n, bf + 2 * n);
+    potential += or_angle_forces_box(px, py, pz, &b->topo, mb, bf, bf + n, bf + 2 * n);
+    potential += or_dihedral_forces_box(px, py, pz, &b->topo, mb, bf, bf + n, bf + 2 * n);
     if (b->n14)
-        potential += or_pair14_forces(px, py, pz, &b->atoms, b->p14_i, b->p14_j, b->n14, b->params.scale14_lj,
-                                      b->params.scale14_coul, b->params.coulomb, bf, bf + n, bf + 2 * n);
+        potential += or_pair14_forces_box(px, py, pz, &b->atoms, b->p14_i, b->p14_j, b->n14, b->params.scale14_lj,
+                                          b->params.scale14_coul, b->params.coulomb, mb, bf, bf + n, bf + 2 * n);
     int nt = b->n_threads;
     int64_t chunk = (b->n_pairs + nt - 1) / nt;
     if (chunk < 1) chunk = 1;
@@ -826,8 +892,9 @@ int64_t or_backend_geodesic_drift(or_backend *b, double *px, double *py, double 
                                   double *vx, double *vy, double *vz, double dt, uint64_t step,
                                   or_convergence_error *err) {
     /* cpu_backend.rs:184-194 */
-    return or_drift_and_constrain(b->atoms.n, px, py, pz, vx, vy, vz, &b->topo, &b->atoms, dt,
-                                  b->params.max_constr_iter, b->params.constr_tol, step, err);
+    return or_drift_and_constrain_box(b->atoms.n, px, py, pz, vx, vy, vz, &b->topo, &b->atoms, dt,
+                                      b->params.max_constr_iter, b->params.constr_tol, step, mi_box_of(&b->params),
+                                      err);
 }
 
 /* ------------------------------------------------------------- run loop */
@@ -852,7 +919,8 @@ int64_t or_run(const or_atoms *a, const or_topology *t, const or_params *p,
     or_backend_build_neighbor_list(b, px, py, pz);
     double pe = or_backend_compute_forces(b, px, py, pz, fx, fy, fz);
     if (!all_finite(n, fx, fy, fz)) { rc = -2; goto done; }
-    if (or_constrain_velocities(&b->topo, a, px, py, pz, vx, vy, vz, p->max_constr_iter, p->constr_tol, 0, err) < 0) {
+    if (or_constrain_velocities_box(&b->topo, a, px, py, pz, vx, vy, vz, p->max_constr_iter, p->constr_tol, 0,
+                                    mi_box_of(p), err) < 0) {
         rc = -1; goto done;
     }
 #define EMIT_FRAME()                                                                  \
@@ -876,7 +944,8 @@ int64_t or_run(const or_atoms *a, const or_topology *t, const or_params *p,
         pe = or_backend_compute_forces(b, px, py, pz, fx, fy, fz);
         if (!all_finite(n, fx, fy, fz)) { rc = -2; goto done; }
         or_half_kick(n, vx, vy, vz, fx, fy, fz, a->mass, dt / 2.0);
-        if (or_constrain_velocities(&b->topo, a, px, py, pz, vx, vy, vz, p->max_constr_iter, p->constr_tol, step, err) < 0) {
+        if (or_constrain_velocities_box(&b->topo, a, px, py, pz, vx, vy, vz, p->max_constr_iter, p->constr_tol,
+                                        step, mi_box_of(p), err) < 0) {
             rc = -1; goto done;
         }
         step += 1;

@@ -50,6 +50,9 @@ typedef struct {
     /* beyond reference: Coulomb and scaled 1-4 pairs (0 = off = reference) */
     int32_t coulomb;
     double scale14_lj, scale14_coul;
+    /* beyond reference: with periodic, bonded, 1-4 and constraint
+     * displacements go to the nearest image (0 = off = reference) */
+    int32_t bonded_min_image;
 } or_params;
 
 /* ConvergenceError::ConstraintSolver (geodesic-core/src/error.rs:50-63). */
@@ -131,6 +134,38 @@ int64_t or_constraint_solve_ws(const or_topology *t, const or_atoms *a,
                                double *px, double *py, double *pz,
                                uint32_t max_iter, double tol, uint64_t step,
                                const double *lam0, double *lam_out, or_convergence_error *err);
+
+/* Beyond reference: the same functions with the displacement between the two
+ * atoms of a bond, angle arm, dihedral bond vector, 1-4 pair or constraint
+ * taken to the nearest image of box mi_box (or_min_image per component);
+ * mi_box == NULL is the function above, bit for bit.  The reference keeps
+ * these differences raw (memory.md:140-144); CpuBackend and or_run pass the
+ * box when params.periodic && params.bonded_min_image. */
+double or_pair14_forces_box(const double *px, const double *py, const double *pz, const or_atoms *a,
+                            const uint32_t *p14_i, const uint32_t *p14_j, int64_t n14,
+                            double scale_lj, double scale_coul, int32_t coulomb, const double *mi_box,
+                            double *fx, double *fy, double *fz);
+double or_bond_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                          const double *mi_box, double *fx, double *fy, double *fz);
+double or_angle_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                           const double *mi_box, double *fx, double *fy, double *fz);
+double or_dihedral_forces_box(const double *px, const double *py, const double *pz, const or_topology *t,
+                              const double *mi_box, double *fx, double *fy, double *fz);
+int64_t or_constraint_solve_box(const or_topology *t, const or_atoms *a,
+                                const double *rx, const double *ry, const double *rz,
+                                double *px, double *py, double *pz,
+                                uint32_t max_iter, double tol, uint64_t step,
+                                const double *lam0, double *lam_out, const double *mi_box,
+                                or_convergence_error *err);
+int64_t or_constrain_velocities_box(const or_topology *t, const or_atoms *a,
+                                    const double *px, const double *py, const double *pz,
+                                    double *vx, double *vy, double *vz,
+                                    uint32_t max_iter, double tol, uint64_t step, const double *mi_box,
+                                    or_convergence_error *err);
+int64_t or_drift_and_constrain_box(int64_t n, double *px, double *py, double *pz,
+                                   double *vx, double *vy, double *vz, const or_topology *t, const or_atoms *a,
+                                   double dt, uint32_t max_iter, double tol, uint64_t step, const double *mi_box,
+                                   or_convergence_error *err);
 
 /* integrator.rs:14-21 and :32-71 */
 void or_half_kick(int64_t n, double *vx, double *vy, double *vz,

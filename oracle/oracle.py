@@ -41,7 +41,8 @@ class OrParams(C.Structure):
     _fields_ = [("box", C.c_double * 3), ("periodic", C.c_int32), ("n_threads", C.c_int32),
                 ("r_cutoff", C.c_double), ("r_skin", C.c_double), ("r_switch", C.c_double),
                 ("max_constr_iter", C.c_uint32), ("constr_tol", C.c_double),
-                ("coulomb", C.c_int32), ("scale14_lj", C.c_double), ("scale14_coul", C.c_double)]
+                ("coulomb", C.c_int32), ("scale14_lj", C.c_double), ("scale14_coul", C.c_double),
+                ("bonded_min_image", C.c_int32)]
 
 
 class OrConvergenceError(C.Structure):
@@ -90,6 +91,21 @@ def lib():
             f = getattr(L, name)
             f.restype = C.c_double
             f.argtypes = [_f64p, _f64p, _f64p, P(OrTopology), _f64p, _f64p, _f64p]
+            f = getattr(L, name + "_box")
+            f.restype = C.c_double
+            f.argtypes = [_f64p, _f64p, _f64p, P(OrTopology), _f64p, _f64p, _f64p, _f64p]
+        L.or_pair14_forces_box.restype = C.c_double
+        L.or_pair14_forces_box.argtypes = [_f64p, _f64p, _f64p, P(OrAtoms), _u32p, _u32p, C.c_int64, C.c_double,
+                                           C.c_double, C.c_int32, _f64p, _f64p, _f64p, _f64p]
+        L.or_constraint_solve_box.restype = C.c_int64
+        L.or_constraint_solve_box.argtypes = [P(OrTopology), P(OrAtoms)] + [_f64p] * 6 + [
+            C.c_uint32, C.c_double, C.c_uint64, _f64p, _f64p, _f64p, P(OrConvergenceError)]
+        L.or_constrain_velocities_box.restype = C.c_int64
+        L.or_constrain_velocities_box.argtypes = [P(OrTopology), P(OrAtoms)] + [_f64p] * 6 + [
+            C.c_uint32, C.c_double, C.c_uint64, _f64p, P(OrConvergenceError)]
+        L.or_drift_and_constrain_box.restype = C.c_int64
+        L.or_drift_and_constrain_box.argtypes = [C.c_int64] + [_f64p] * 6 + [
+            P(OrTopology), P(OrAtoms), C.c_double, C.c_uint32, C.c_double, C.c_uint64, _f64p, P(OrConvergenceError)]
         L.or_constraint_solve_ws.restype = C.c_int64
         L.or_constraint_solve_ws.argtypes = [P(OrTopology), P(OrAtoms), _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
                                              C.c_uint32, C.c_double, C.c_uint64, _f64p, _f64p, P(OrConvergenceError)]
@@ -176,9 +192,17 @@ class Arrays:
 
 def make_params(box=(1000.0, 1000.0, 1000.0), periodic=False, r_cutoff=12.0, r_skin=14.0, r_switch=10.0,
                 max_constr_iter=100, constr_tol=1e-10, n_threads=1, coulomb=False, scale14_lj=0.0,
-                scale14_coul=0.0):
+                scale14_coul=0.0, bonded_min_image=False):
     return OrParams((C.c_double * 3)(*box), int(periodic), int(n_threads), r_cutoff, r_skin, r_switch,
-                    int(max_constr_iter), constr_tol, int(coulomb), scale14_lj, scale14_coul)
+                    int(max_constr_iter), constr_tol, int(coulomb), scale14_lj, scale14_coul, int(bonded_min_image))
+
+
+def _box(box):
+    """The nearest-image box of the *_box functions (None: raw differences)."""
+    if box is None:
+        return None, None
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    return b, _p(b, C.c_double)
 
 
 def host_threads() -> int:
@@ -238,26 +262,34 @@ def pairs14(topo, n_atoms):
     return pi[:cnt].copy(), pj[:cnt].copy()
 
 
-def pair14_forces(pos, atoms, p14_i, p14_j, scale_lj, scale_coul, coulomb, force=None):
+def pair14_forces(pos, atoms, p14_i, p14_j, scale_lj, scale_coul, coulomb, force=None, box=None):
     L = lib()
     arr = Arrays(atoms, _empty_topo())
     n = pos.shape[1]
     force = np.zeros((3, n)) if force is None else force
     pi, pj = _u32(p14_i), _u32(p14_j)
-    e = L.or_pair14_forces(*(_p(_f64(pos[d]), C.c_double) for d in range(3)), C.byref(arr.atoms),
-                           _p(pi, C.c_uint32), _p(pj, C.c_uint32), len(pi), scale_lj, scale_coul, int(coulomb),
-                           *(_p(force[d], C.c_double) for d in range(3)))
+    keep, bp = _box(box)
+    e = L.or_pair14_forces_box(*(_p(_f64(pos[d]), C.c_double) for d in range(3)), C.byref(arr.atoms),
+                               _p(pi, C.c_uint32), _p(pj, C.c_uint32), len(pi), scale_lj, scale_coul, int(coulomb),
+                               bp, *(_p(force[d], C.c_double) for d in range(3)))
     return e, force
 
 
-def bonded_forces(kind, pos, topo, force=None):
-    """kind in {'bond', 'angle', 'dihedral'} -> (energy, force)."""
+def bonded_forces(kind, pos, topo, force=None, box=None):
+    """kind in {'bond', 'angle', 'dihedral'} -> (energy, force); `box`: the
+    nearest-image box of the *_box variants."""
     L = lib()
     n = pos.shape[1]
     arr = Arrays(_dummy_atoms(n), topo)
     force = np.zeros((3, n)) if force is None else force
-    fn = {"bond": L.or_bond_forces, "angle": L.or_angle_forces, "dihedral": L.or_dihedral_forces}[kind]
-    e = fn(*(_p(_f64(pos[d]), C.c_double) for d in range(3)), C.byref(arr.topo),
+    if box is None:
+        fn = {"bond": L.or_bond_forces, "angle": L.or_angle_forces, "dihedral": L.or_dihedral_forces}[kind]
+        e = fn(*(_p(_f64(pos[d]), C.c_double) for d in range(3)), C.byref(arr.topo),
+               *(_p(force[d], C.c_double) for d in range(3)))
+        return e, force
+    fn = {"bond": L.or_bond_forces_box, "angle": L.or_angle_forces_box, "dihedral": L.or_dihedral_forces_box}[kind]
+    keep, bp = _box(box)
+    e = fn(*(_p(_f64(pos[d]), C.c_double) for d in range(3)), C.byref(arr.topo), bp,
            *(_p(force[d], C.c_double) for d in range(3)))
     return e, force
 
@@ -280,13 +312,16 @@ def constraint_solve(topo, atoms, ref, pos, max_iter, tol, step=0, lam0=None, wa
     return (int(it), lam_out) if want_lambda else int(it)
 
 
-def constrain_velocities(topo, atoms, pos, vel, max_iter, tol, step=0):
+def constrain_velocities(topo, atoms, pos, vel, max_iter, tol, step=0, box=None):
     L = lib()
     arr = Arrays(atoms, topo)
     err = OrConvergenceError()
     posc = _f64(pos)
-    it = L.or_constrain_velocities(C.byref(arr.topo), C.byref(arr.atoms), *(_p(posc[d], C.c_double) for d in range(3)),
-                                   *(_p(vel[d], C.c_double) for d in range(3)), max_iter, tol, step, C.byref(err))
+    keep, bp = _box(box)
+    it = L.or_constrain_velocities_box(C.byref(arr.topo), C.byref(arr.atoms),
+                                       *(_p(posc[d], C.c_double) for d in range(3)),
+                                       *(_p(vel[d], C.c_double) for d in range(3)), max_iter, tol, step, bp,
+                                       C.byref(err))
     if it < 0:
         raise ConvergenceError(err)
     return int(it)
@@ -299,13 +334,14 @@ def half_kick(vel, force, mass, dt_half):
                    _p(m, C.c_double), dt_half)
 
 
-def drift_and_constrain(pos, vel, topo, atoms, dt, max_iter, tol, step=0):
+def drift_and_constrain(pos, vel, topo, atoms, dt, max_iter, tol, step=0, box=None):
     L = lib()
     arr = Arrays(atoms, topo)
     err = OrConvergenceError()
-    it = L.or_drift_and_constrain(pos.shape[1], *(_p(pos[d], C.c_double) for d in range(3)),
-                                  *(_p(vel[d], C.c_double) for d in range(3)), C.byref(arr.topo), C.byref(arr.atoms),
-                                  dt, max_iter, tol, step, C.byref(err))
+    keep, bp = _box(box)
+    it = L.or_drift_and_constrain_box(pos.shape[1], *(_p(pos[d], C.c_double) for d in range(3)),
+                                      *(_p(vel[d], C.c_double) for d in range(3)), C.byref(arr.topo),
+                                      C.byref(arr.atoms), dt, max_iter, tol, step, bp, C.byref(err))
     if it < 0:
         raise ConvergenceError(err)
     return int(it)

@@ -51,3 +51,28 @@ def test_invalid_parameters_rejected_before_any_device_call(library):
         backend.CudaBackend(atoms, amber.BondedTopology.empty(),
                             backend.SimParams(r_cutoff=10.0, r_skin=9.0, r_switch=8.0))
     assert e.value.status == 1
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of gm_atoms, gm_topology, gm_params and
+    gm_convergence have the header's size and field offsets (gcc on the header)."""
+    import subprocess
+
+    structs = {"gm_atoms": backend.GmAtoms, "gm_topology": backend.GmTopology, "gm_params": backend.GmParams,
+               "gm_convergence": backend.GmConvergence}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "geodesic_cuda.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                             check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[f"{cname} size"]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname} {fname}"]) == getattr(py, fname).offset, (cname, fname)

@@ -98,8 +98,11 @@ def test_integers_are_accepted_for_reals_and_optional_tables_read():
     c = config.Config.from_toml_str(text)
     assert c.dt == 1.0 and isinstance(c.dt, float)
     assert c.monitoring == config.MonitoringConfig(2.0, config.DriftAction.STOP)
-    c = config.Config.from_toml_str(GOLDEN_CONFIG + '\n[cuda]\nprecision = "fp64"\nframes_per_batch = 8\n')
-    assert (c.precision, c.frames_per_batch) == ("fp64", 8)
+    c = config.Config.from_toml_str(GOLDEN_CONFIG + '\n[cuda]\nprecision = "fp64"\nframes_per_batch = 8\n'
+                                    'bonded_min_image = true\n')
+    assert (c.precision, c.frames_per_batch, c.bonded_min_image) == ("fp64", 8, True)
+    assert c.sim_params().bonded_min_image is True
+    assert config.Config.from_toml_str(GOLDEN_CONFIG).sim_params().bonded_min_image is False
 
 
 @pytest.mark.parametrize("old,new,key", [
