@@ -164,9 +164,21 @@ def run(config: Config, base: str = "", make_backend=None):
         be.close()
 
 
-def _initial_state(be, pos, vel):
-    """lib.rs:261-282: the velocity projection, then the resident state's
-    forces and energies."""
+def _wrap_into_box(pos, box) -> None:
+    """neighbor.rs:78-88: x - L * floor(x / L) per coordinate, in place."""
+    for d in range(3):
+        pos[d] -= box[d] * np.floor(pos[d] / box[d])
+
+
+def _initial_state(config: Config, be, pos, vel):
+    """lib.rs:261-282: the first list build (which wraps a periodic system
+    into the box), the velocity projection on those positions, then the
+    resident state's forces and energies.  The wrap is done here, on the
+    host, so that frame 0 and the projection see the wrapped positions as in
+    the reference; the device's own wrap at its first build then changes
+    nothing (a coordinate in [0, L) wraps to itself)."""
+    if config.periodic:
+        _wrap_into_box(pos, config.box_size)
     be.constrain_velocities(pos, vel, 0)
     be.upload_state(pos, vel)
     be.forces_resident()
@@ -177,7 +189,7 @@ def _run_single(config: Config, be, pos, vel, paths) -> RunSummary:
     traj, log = paths
     be.frames_enable(fi, config.frames_per_batch)
     with DcdWriter(traj, n, fi, dt) as dcd, EnergyLogWriter(log, n) as csv:
-        _initial_state(be, pos, vel)
+        _initial_state(config, be, pos, vel)
         e_pot, e_kin = be.resident_energies()
         dcd.write_frame(pos[0].astype(np.float32), pos[1].astype(np.float32), pos[2].astype(np.float32))
         csv.write_row(0, 0.0, e_pot, e_kin)
@@ -226,7 +238,7 @@ def _run_batch(config: Config, be, pos, vel, paths, sizes) -> list:
         for k in range(ns):
             dcds.append(DcdWriter(paths[k][0], sizes[k], fi, dt))
             csvs.append(EnergyLogWriter(paths[k][1], sizes[k]))
-        _initial_state(be, pos, vel)
+        _initial_state(config, be, pos, vel)
         ep, ek = be.ensemble_energies()
         monitors = [_DriftMonitor(config, ep[k] + ek[k], config.systems[k].name) for k in range(ns)]
         last_kin = np.array(ek, dtype=np.float64)

@@ -16,7 +16,9 @@ class OracleResident:
     def __init__(self, atoms_list, topo_list, params):
         self.p = oracle.make_params(box=tuple(params.box_size), periodic=params.periodic, r_cutoff=params.r_cutoff,
                                     r_skin=params.r_skin, r_switch=params.r_switch,
-                                    max_constr_iter=params.max_constr_iter, constr_tol=params.constr_tol, n_threads=1)
+                                    max_constr_iter=params.max_constr_iter, constr_tol=params.constr_tol, n_threads=1,
+                                    bonded_min_image=params.bonded_min_image)
+        self.box = tuple(params.box_size) if params.periodic and params.bonded_min_image else None
         self.max_iter, self.tol = params.max_constr_iter, params.constr_tol
         self.systems = [(a, t, oracle.CpuBackend(a, t, self.p)) for a, t in zip(atoms_list, topo_list)]
         sizes = [a.n for a in atoms_list]
@@ -37,7 +39,7 @@ class OracleResident:
         for k, (a, t, _) in enumerate(self.systems):
             sl = self._sl(k)
             p, v = np.ascontiguousarray(pos[:, sl]), np.ascontiguousarray(vel[:, sl])
-            oracle.constrain_velocities(t, a, p, v, self.max_iter, self.tol, step)
+            oracle.constrain_velocities(t, a, p, v, self.max_iter, self.tol, step, box=self.box)
             vel[:, sl] = v
 
     def upload_state(self, pos, vel):
@@ -85,7 +87,7 @@ class OracleResident:
                 self.force[k] = b.compute_forces(p)
                 self.e_pot[k] = b.potential_energy
                 oracle.half_kick(v, self.force[k], a.mass, dt / 2.0)
-                oracle.constrain_velocities(t, a, p, v, self.max_iter, self.tol, step)
+                oracle.constrain_velocities(t, a, p, v, self.max_iter, self.tol, step, box=self.box)
             if self.fi and (step + 1) % self.fi == 0:
                 if len(self.ring) == self.cap:
                     self.lost += 1

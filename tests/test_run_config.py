@@ -253,23 +253,27 @@ def test_cuda_table_errors():
 # ------------------------------------------------------------ run loop
 
 def write_case(tmp_path, systems, n_steps, frame_interval, constrain=True, frames_per_batch=3, extra="", tol=1e-8,
-               files=None):
+               files=None, box=1000.0, periodic=False, centre=None, min_image=False):
     """Writes each (name, n_atoms, seed, h_fraction) system's AMBER files and
     a config running them; returns the config path.  `files`: (name, prmtop,
-    inpcrd) entries already in tmp_path, used instead."""
+    inpcrd) entries already in tmp_path, used instead.  `centre`: where the
+    system's centroid is put (default: where the generator put it)."""
     entries = list(files or [])
     for name, n, seed, hf in ([] if files else systems):
         atoms, topo, state, _ = synth.generate(n, seed=seed, h_fraction=hf, temperature=300.0, relax_iters=200)
+        if centre is not None:
+            state.pos = state.pos - state.pos.mean(axis=1, keepdims=True) + np.asarray(centre, float)[:, None]
         prm, crd = amber_files.write_system(tmp_path, name, atoms, topo, state)
         entries.append((name, prm, crd))
     batch = len(entries) > 1
+    box_text = f"box_size = [{box!r}, {box!r}, {box!r}]\nperiodic = {'true' if periodic else 'false'}\n"
     if batch:
-        sys_text = "".join(f'[[system]]\nname = "{nm}"\nprmtop = "{p}"\ninpcrd = "{c}"\n'
-                           f"box_size = [1000.0, 1000.0, 1000.0]\n\n" for nm, p, c in entries)
+        sys_text = "".join(f'[[system]]\nname = "{nm}"\nprmtop = "{p}"\ninpcrd = "{c}"\n{box_text}\n'
+                           for nm, p, c in entries)
         traj, log = "traj_{system}.dcd", "energy_{system}.csv"
     else:
         nm, p, c = entries[0]
-        sys_text = f'[system]\nprmtop = "{p}"\ninpcrd = "{c}"\nbox_size = [1000.0, 1000.0, 1000.0]\n\n'
+        sys_text = f'[system]\nprmtop = "{p}"\ninpcrd = "{c}"\n{box_text}\n'
         traj, log = "traj.dcd", "energy.csv"
     text = f"""[run]
 n_steps = {n_steps}
@@ -297,18 +301,20 @@ energy_log = "{log}"
 
 [cuda]
 frames_per_batch = {frames_per_batch}
+bonded_min_image = {"true" if min_image else "false"}
 {extra}"""
     path = tmp_path / "config.toml"
     path.write_text(text)
     return path
 
 
-def oracle_expected(tmp_path, stem, n_steps, frame_interval, constrain=True, tol=1e-8):
+def oracle_expected(tmp_path, stem, n_steps, frame_interval, constrain=True, tol=1e-8, box=1000.0, periodic=False,
+                    min_image=False):
     atoms, topo, state = amber.load(str(tmp_path / f"{stem}.prmtop"), str(tmp_path / f"{stem}.inpcrd"))
     if constrain:
         topo = amber.promote_hydrogen_bonds(topo, atoms)
-    p = oracle.make_params(box=(1000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=11.0, r_switch=8.0,
-                           max_constr_iter=100, constr_tol=tol, n_threads=1)
+    p = oracle.make_params(box=(box,) * 3, periodic=periodic, r_cutoff=10.0, r_skin=11.0, r_switch=8.0,
+                           max_constr_iter=100, constr_tol=tol, n_threads=1, bonded_min_image=min_image)
     frames, pot, kin = oracle.run(atoms, topo, p, np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel),
                                   0.002, n_steps, frame_interval)
     return atoms.n, frames, pot, kin
@@ -421,3 +427,20 @@ def test_run_errors(tmp_path):
     assert str(e.value).startswith(f"I/O error at '{tmp_path / 'missing.prmtop'}': ")
     with pytest.raises(run.SimIoError):
         run.run_from_config_file(tmp_path / "no_such.toml", make_backend=oracle_resident.make)
+
+
+@pytest.mark.parametrize("centre,min_image", [((95.0, -25.0, 155.0), False), ((0.0, 0.0, 0.0), True)])
+def test_periodic_run_wraps_before_frame_zero(tmp_path, centre, min_image):
+    """A periodic system placed outside the box (moved inside whole by the
+    first wrap) or around a corner (split by it; with bonded_min_image): the
+    wrap comes before frame 0 and the velocity projection, as in the
+    reference's first list build (lib.rs:261-282), so the files are those of
+    oracle.run, bit for bit."""
+    cfg = write_case(tmp_path, [("sys", 250, 52, 0.3)], 20, 5, box=60.0, periodic=True, centre=centre,
+                     min_image=min_image)
+    run.run_from_config_file(cfg, make_backend=oracle_resident.make)
+    n, frames, pot, kin = oracle_expected(tmp_path, "sys", 20, 5, box=60.0, periodic=True, min_image=min_image)
+    header, dcd = read_dcd(tmp_path / "traj.dcd")
+    assert np.array_equal(dcd.view(np.uint32), frames.view(np.uint32))
+    assert np.all((dcd[0] >= 0.0) & (dcd[0] < 60.0))  # frame 0 is already in the box
+    assert (tmp_path / "energy.csv").read_text() == expected_csv(tmp_path, n, 5, pot, kin)
