@@ -444,3 +444,16 @@ def test_periodic_run_wraps_before_frame_zero(tmp_path, centre, min_image):
     assert np.array_equal(dcd.view(np.uint32), frames.view(np.uint32))
     assert np.all((dcd[0] >= 0.0) & (dcd[0] < 60.0))  # frame 0 is already in the box
     assert (tmp_path / "energy.csv").read_text() == expected_csv(tmp_path, n, 5, pot, kin)
+
+
+def test_periodic_batch_wraps_every_system(tmp_path):
+    """A periodic [[system]] batch (one shared box, bonded_min_image): each
+    system placed around a corner of the box writes oracle.run's files."""
+    systems = [("a", 200, 53, 0.3), ("b", 260, 54, 0.2)]
+    cfg = write_case(tmp_path, systems, 20, 10, box=60.0, periodic=True, centre=(0.0, 60.0, -3.0), min_image=True)
+    out = run.run_from_config_file(cfg, make_backend=oracle_resident.make)
+    for (name, _, _, _), s in zip(systems, out):
+        n, frames, pot, kin = oracle_expected(tmp_path, name, 20, 10, box=60.0, periodic=True, min_image=True)
+        header, dcd = read_dcd(tmp_path / f"traj_{name}.dcd")
+        assert np.array_equal(dcd.view(np.uint32), frames.view(np.uint32)), name
+        assert (tmp_path / f"energy_{name}.csv").read_text() == expected_csv(tmp_path, n, 10, pot, kin), name
