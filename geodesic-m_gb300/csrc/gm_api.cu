@@ -48,8 +48,8 @@ struct gm_ctx {
     int ntypes = 0;
     double *d_mass = nullptr, *d_inv_mass = nullptr, *d_sigma = nullptr, *d_eps = nullptr, *d_charge64 = nullptr;
     int *d_type = nullptr;
-    float *d_charge = nullptr;
-    float2 *d_tab32 = nullptr;
+    float2 *d_qw = nullptr;  // per atom (Q_hi, Q_lo | type) of the mixed pair kernel's slot records
+    float4 *d_tab32 = nullptr;
     double2 *d_tab64 = nullptr;
     // state
     double *d_pos = nullptr, *d_vel = nullptr, *d_ref = nullptr, *d_dref = nullptr, *d_fout = nullptr,
@@ -86,11 +86,10 @@ struct gm_ctx {
         *d_dj = nullptr, *d_dk = nullptr, *d_dl = nullptr, *d_dn = nullptr;
     double *d_bk = nullptr, *d_br0 = nullptr, *d_akth = nullptr, *d_ath0 = nullptr, *d_dkphi = nullptr,
            *d_ddelta = nullptr;
+    double2 *d_dcs = nullptr;  // (cos delta, sin delta) per dihedral
     // 1-4
     int n14 = 0, blocks14 = 0;
     int *d_p14i = nullptr, *d_p14j = nullptr;
-    float4 *d_p14par = nullptr;
-    double2 *d_acs = nullptr;
     // constraints
     int n_constr = 0, n_clusters = 0, n_single = 0, n_star_end = 0, n_warp_end = 0;
     int *d_ci = nullptr, *d_cj = nullptr, *d_cl_cstart = nullptr, *d_cl_cons = nullptr, *d_cl_astart = nullptr,
@@ -217,7 +216,7 @@ ListArgs list_args(gm_ctx *c) {
     a.cell_cursor = c->d_cell_cursor;
     a.tmp_atom = c->d_tmp_atom;
     a.type = c->d_type;
-    a.charge = c->d_charge;
+    a.qw = c->d_qw;
     a.charge64 = c->d_charge64;
     a.excl_start = c->d_excl_start;
     a.excl = c->d_excl;
@@ -229,6 +228,8 @@ ListArgs list_args(gm_ctx *c) {
     a.grid = c->d_grid;
     a.status = c->d_status;
     a.r_list = c->p.r_skin;
+    a.r_cut = c->p.r_cutoff;
+    a.r_switch = c->p.r_switch;
     for (int d = 0; d < 3; d++) a.box[d] = c->p.box[d];
     a.periodic = c->p.periodic;
     a.bbox_scratch = c->d_bbox;
@@ -260,7 +261,6 @@ ForceArgs force_args(gm_ctx *c) {
     a.pair_warps = c->pair_warps;
     a.pair_grid = c->pair_grid;
     a.coord = c->d_coord;
-    a.slot_of = c->d_slot_of;
     a.pos64s = c->d_pos64s;
     a.type_sorted = c->d_type_sorted;
     a.perm = c->d_perm;
@@ -271,14 +271,24 @@ ForceArgs force_args(gm_ctx *c) {
     a.tab32 = c->d_tab32;
     a.tab64 = c->d_tab64;
     const double rc = c->p.r_cutoff, rsw = c->p.r_switch;
-    a.rc2 = (float)(rc * rc);
-    a.rsw = (float)rsw;
-    a.rc = (float)rc;
-    a.inv_wsw = (float)(1.0 / (rc - rsw));
     a.rc2_64 = rc * rc;
     a.rsw_64 = rsw;
     a.rc_64 = rc;
     a.inv_wsw_64 = 1.0 / (rc - rsw);
+    {
+        // double-float constants of the mixed pair kernel
+        auto split = [](double x, float &h, float &l) { h = (float)x; l = (float)(x - (double)h); };
+        PairConst &k = a.pc;
+        k.rc2 = (float)(rc * rc);
+        k.rsw2 = (float)(rsw * rsw);
+        split(rsw, k.rsw, k.rsw_lo);
+        split(1.0 / (rc - rsw), k.inv_w, k.inv_w_lo);
+        split(-30.0 / (rc - rsw), k.mds, k.mds_lo);
+        for (int d = 0; d < 3; d++) {
+            split(c->p.box[d], k.box[d], k.box_lo[d]);
+            k.inv_box[d] = (float)(1.0 / c->p.box[d]);
+        }
+    }
     a.coulomb = c->p.coulomb;
     for (int d = 0; d < 3; d++) {
         a.box[d] = (float)c->p.box[d];
@@ -296,16 +306,14 @@ ForceArgs force_args(gm_ctx *c) {
     a.n_diheds = c->n_diheds;
     a.bond_i = c->d_bi; a.bond_j = c->d_bj; a.bond_k = c->d_bk; a.bond_r0 = c->d_br0;
     a.angle_i = c->d_ai; a.angle_j = c->d_aj; a.angle_k = c->d_ak; a.angle_kth = c->d_akth; a.angle_th0 = c->d_ath0;
-    a.angle_cs = c->d_acs;
     a.dihed_i = c->d_di; a.dihed_j = c->d_dj; a.dihed_k = c->d_dk; a.dihed_l = c->d_dl; a.dihed_kphi = c->d_dkphi;
-    a.dihed_n = c->d_dn; a.dihed_delta = c->d_ddelta;
+    a.dihed_n = c->d_dn; a.dihed_delta = c->d_ddelta; a.dihed_cs = c->d_dcs;
     a.bonded_blocks = c->bonded_blocks;
     const int pair_parts = c->n_groups * a.split;
     a.epart_bonded = c->d_epart + pair_parts;
     a.n14 = c->n14; a.p14_i = c->d_p14i; a.p14_j = c->d_p14j;
     a.scale14_lj = c->p.scale14_lj; a.scale14_coul = c->p.scale14_coul;
     a.sigma = c->d_sigma; a.epsilon = c->d_eps; a.charge64 = c->d_charge64;
-    a.p14par = c->d_p14par;
     a.blocks14 = c->blocks14;
     a.epart14 = c->d_epart + pair_parts + c->bonded_blocks;
     a.energy = c->d_energy;
@@ -421,7 +429,7 @@ PackArgs pack_args(gm_ctx *c) {
     p.slot_of = c->d_slot_of;
     p.grid = c->d_grid;
     p.type = c->d_type;
-    p.charge = c->d_charge;
+    p.qw = c->d_qw;
     p.charge64 = c->d_charge64;
     p.fp64 = c->fp64 ? 1 : 0;
     return p;
@@ -1167,7 +1175,7 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         return bail(GM_ERR_UNSUPPORTED);
     }
     const size_t T2 = (size_t)c->ntypes * c->ntypes;
-    std::vector<float2> tab32(T2 * (size_t)n_sys, make_float2(0.f, 0.f));
+    std::vector<float4> tab32(T2 * (size_t)n_sys, make_float4(0.f, 0.f, 0.f, 0.f));
     std::vector<double2> tab64(T2 * (size_t)n_sys, make_double2(0.0, 0.0));
     for (int sy = 0; sy < n_sys; sy++) {
         const auto &sg_ = tsig[(size_t)sy];
@@ -1178,22 +1186,36 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
                 const double sg = 0.5 * (sg_[a] + sg_[b]);
                 const double ep = std::sqrt(ep_[a] * ep_[b]);
                 tab64[T2 * (size_t)sy + a * (size_t)c->ntypes + b] = make_double2(sg, ep);
-                tab32[T2 * (size_t)sy + a * (size_t)c->ntypes + b] = make_float2((float)(sg * sg), (float)ep);
+                // the mixed pair kernel's double-float (sigma^2, 24 epsilon)
+                const double s2 = sg * sg, e24 = 24.0 * ep;
+                const float s2h = (float)s2, e24h = (float)e24;
+                tab32[T2 * (size_t)sy + a * (size_t)c->ntypes + b] =
+                    make_float4(s2h, (float)(s2 - (double)s2h), e24h, (float)(e24 - (double)e24h));
             }
     }
     std::vector<double> inv_mass((size_t)n), charge64((size_t)n);
-    std::vector<float> charge((size_t)n);
+    std::vector<float2> qw((size_t)n);
     for (int i = 0; i < n; i++) {
         inv_mass[(size_t)i] = 1.0 / atoms->mass[i];  // integrator.rs:16, constraint.rs:110
         charge64[(size_t)i] = atoms->charge ? atoms->charge[i] : 0.0;
-        charge[(size_t)i] = (float)charge64[(size_t)i];
+        // Q = sqrt(k_C) q as a double-float, so that Q_i Q_j = k_C q_i q_j
+        // (k_C = 332.0522173, the reference's kcal/mol conversion,
+        // prmtop.rs:5-9); the low 8 bits of Q_lo carry the atom's type
+        const double Q = std::sqrt(332.0522173) * charge64[(size_t)i];
+        const float qh = (float)Q, ql = (float)(Q - (double)qh);
+        uint32_t bits;
+        std::memcpy(&bits, &ql, sizeof bits);
+        bits = (bits & ~0xffu) | (uint32_t)type[(size_t)i];
+        float qlt;
+        std::memcpy(&qlt, &bits, sizeof qlt);
+        qw[(size_t)i] = make_float2(qh, qlt);
     }
     TRY(dupload(c, &c->d_mass, atoms->mass, (size_t)n));
     TRY(dupload(c, &c->d_inv_mass, inv_mass.data(), (size_t)n));
     TRY(dupload(c, &c->d_sigma, atoms->sigma, (size_t)n));
     TRY(dupload(c, &c->d_eps, atoms->epsilon, (size_t)n));
     TRY(dupload(c, &c->d_charge64, charge64.data(), (size_t)n));
-    TRY(dupload(c, &c->d_charge, charge.data(), (size_t)n));
+    TRY(dupload(c, &c->d_qw, qw.data(), (size_t)n));
     TRY(dupload(c, &c->d_type, type.data(), (size_t)n));
     TRY(dupload(c, &c->d_tab32, tab32.data(), tab32.size()));
     TRY(dupload(c, &c->d_tab64, tab64.data(), tab64.size()));
@@ -1242,11 +1264,6 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dupload(c, &c->d_ak, v(t->angle_k, t->n_angles).data(), (size_t)t->n_angles));
     TRY(dupload(c, &c->d_akth, t->angle_kth, (size_t)t->n_angles));
     TRY(dupload(c, &c->d_ath0, t->angle_th0, (size_t)t->n_angles));
-    {
-        std::vector<double2> cs((size_t)t->n_angles);
-        for (int64_t q = 0; q < t->n_angles; q++) cs[(size_t)q] = make_double2(std::cos(t->angle_th0[q]), std::sin(t->angle_th0[q]));
-        TRY(dupload(c, &c->d_acs, cs.data(), cs.size()));
-    }
     TRY(dupload(c, &c->d_di, v(t->dihed_i, t->n_diheds).data(), (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_dj, v(t->dihed_j, t->n_diheds).data(), (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_dk, v(t->dihed_k, t->n_diheds).data(), (size_t)t->n_diheds));
@@ -1254,6 +1271,12 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dupload(c, &c->d_dkphi, t->dihed_kphi, (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_dn, v(t->dihed_n, t->n_diheds).data(), (size_t)t->n_diheds));
     TRY(dupload(c, &c->d_ddelta, t->dihed_delta, (size_t)t->n_diheds));
+    {
+        std::vector<double2> cs((size_t)t->n_diheds);
+        for (int64_t q = 0; q < t->n_diheds; q++)
+            cs[(size_t)q] = make_double2(std::cos(t->dihed_delta[q]), std::sin(t->dihed_delta[q]));
+        TRY(dupload(c, &c->d_dcs, cs.data(), cs.size()));
+    }
     // ---- scaled 1-4 pairs (beyond the reference; off by default)
     if (p.scale14_lj != 0.0 || (p.coulomb && p.scale14_coul != 0.0)) {
         std::vector<std::pair<int, int>> close;
@@ -1278,16 +1301,6 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         c->blocks14 = (c->n14 + 255) / 256;
         TRY(dupload(c, &c->d_p14i, a.data(), a.size()));
         TRY(dupload(c, &c->d_p14j, b.data(), b.size()));
-        // FP32 parameters of the mixed path (force/nonbonded.rs:20-82 mixing)
-        std::vector<float4> par(p14.size());
-        for (size_t k = 0; k < p14.size(); k++) {
-            const int i = a[k], j = b[k];
-            const double sg = 0.5 * (atoms->sigma[i] + atoms->sigma[j]);
-            const double ep = std::sqrt(atoms->epsilon[i] * atoms->epsilon[j]);
-            const double qq = p.coulomb ? 332.0522173 * charge64[(size_t)i] * charge64[(size_t)j] : 0.0;
-            par[k] = make_float4((float)(sg * sg), (float)(p.scale14_lj * 4.0 * ep), (float)(p.scale14_coul * qq), 0.f);
-        }
-        TRY(dupload(c, &c->d_p14par, par.data(), par.size()));
     }
     // ---- constraints as independent clusters
     c->n_constr = (int)t->n_constr;
@@ -1378,6 +1391,10 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         }
         c->n_slots = slot_off.back();
         c->total_cells = cell_off.back();
+        if (c->n_slots > GM_SLOT_MASK) {
+            fail(c, GM_ERR_UNSUPPORTED, "%d padded atom slots; at most %d are supported", c->n_slots, GM_SLOT_MASK);
+            return bail(GM_ERR_UNSUPPORTED);
+        }
         TRY(dupload(c, &c->d_sys_atom_off, mg.atom_off.data(), mg.atom_off.size()));
         TRY(dupload(c, &c->d_sys_slot_off, slot_off.data(), slot_off.size()));
         TRY(dupload(c, &c->d_sys_cell_off, cell_off.data(), cell_off.size()));

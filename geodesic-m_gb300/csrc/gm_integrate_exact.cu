@@ -977,11 +977,7 @@ __global__ void kick_drift_check_kernel(int n, double *pos, double *vel, double 
         // pack_kernel's work for this atom, from the same FP64 position
         const int sl = pk.slot_of[i];
         const GridInfo *g = pk.grid + atom_sys[i];
-        const double ox = np[0] - g->origin[0], oy = np[1] - g->origin[1], oz = np[2] - g->origin[2];
-        const float hx = (float)ox, hy = (float)oy, hz = (float)oz;
-        pk.coord[2 * sl] = make_float4(hx, hy, hz, __int_as_float(pk.type[i]));
-        pk.coord[2 * sl + 1] = make_float4((float)(ox - (double)hx), (float)(oy - (double)hy), (float)(oz - (double)hz),
-                                           pk.charge[i]);
+        gm_pack_record(pk.coord + 2 * sl, np[0] - g->origin[0], np[1] - g->origin[1], np[2] - g->origin[2], pk.qw[i]);
         if (pk.fp64) {
             pk.pos64s[sl] = make_double4(np[0], np[1], np[2], pk.charge64[i]);
             pk.type_sorted[sl] = pk.type[i];

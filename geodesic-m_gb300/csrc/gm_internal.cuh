@@ -8,9 +8,10 @@
 //     value = F * 2^-40 kcal/mol/A.  Integer sums are associative, so
 //     atomics from any thread order give bit-identical totals.
 //   * Cell-sorted copies for the pair kernel: perm[s] = caller index of
-//     sorted slot s; hi[s] = (float(x-o), float(y-o), float(z-o), type bits),
-//     lo[s] = (float residues of the same, charge) so hi+lo carries each
-//     coordinate to ~2^-48 relative; FP64 mode keeps a sorted double4 copy.
+//     sorted slot s; hi[s] = (x-o, y-o, z-o rounded to multiples of 2^-8 A,
+//     Q_hi), lo[s] = (FP32 remainders of the same, Q_lo with the type in its
+//     low 8 bits), Q = sqrt(k_C) q as a double-float; hi+lo carries each
+//     coordinate to ~2^-33 A; FP64 mode keeps a sorted double4 copy.
 //   * Full (symmetric) neighbour list in warp-interleaved columns: the 32
 //     atoms of group g own a slab of 32*cap ints; entry e of lane l sits at
 //     g*32*cap + e*32 + l, so one list row is a 128-byte coalesced load.
@@ -19,6 +20,7 @@
 #include <stdint.h>
 
 #include "geodesic_cuda.h"
+#include "gm_df.h"
 #include "gm_exact_math.h"
 
 #define GM_FIX_SCALE 1099511627776.0        // 2^40
@@ -26,8 +28,9 @@
 #define GM_FIX_SCALE_F 1099511627776.0f
 #define GM_FIX_LIMIT 4194304.0              // 2^22: |contribution| must stay below
 
-// Ceiling on distinct (sigma, epsilon) parameter pairs: the pair table lives
-// in shared memory (64 x 64 x 8 B = 32 KB).
+// Ceiling on distinct (sigma, epsilon) parameter pairs (the type sits in 8
+// bits of a slot record; a single system's pair table of 16 B entries lives
+// in shared memory while it fits in 48 KB, in L1 otherwise).
 #define GM_MAX_TYPES 64
 #define GM_WARP 32
 #define GM_MAX_SPLIT 16      // largest number of warps per 32-atom group
@@ -37,6 +40,11 @@
 // the block then concatenates the segments, layer by layer, into each lane's
 // list column.
 #define GM_NSEG 5
+// List columns are ordered by build-time distance in GM_NBUCKET buckets; the
+// build stages a slot index with its bucket in the top bits.
+#define GM_NBUCKET 4
+#define GM_BUCKET_SHIFT 27
+#define GM_SLOT_MASK ((1 << GM_BUCKET_SHIFT) - 1)  // slots per context stay below 2^27
 
 // Device status bits (DevStatus::error).
 enum : unsigned int {
@@ -147,6 +155,23 @@ __device__ __forceinline__ void gm_ld_coord(const float4 *p, float4 &h, float4 &
         : "l"(p));
 }
 
+// A slot's atom type, kept in the low 8 bits of its Q_lo (the low part of a
+// double-float charge; those bits are below 2^-39 of Q).
+__device__ __forceinline__ int gm_slot_type(float qlo) { return __float_as_int(qlo) & 0xff; }
+
+// Per atom: (Q_hi, Q_lo | type), Q = sqrt(k_C) q, built on the host.
+// The slot record of an atom at FP64 offset (ox, oy, oz) from its system's
+// grid origin: coordinates rounded to the 2^-8 A grid (differences of two
+// such values, and their squares below 16 A, are exact in FP32) and the FP32
+// remainders.
+__device__ __forceinline__ void gm_pack_record(float4 *rec, double ox, double oy, double oz, float2 qw) {
+    const float hx = rintf((float)ox * 256.f) * (1.f / 256.f);
+    const float hy = rintf((float)oy * 256.f) * (1.f / 256.f);
+    const float hz = rintf((float)oz * 256.f) * (1.f / 256.f);
+    rec[0] = make_float4(hx, hy, hz, qw.x);
+    rec[1] = make_float4((float)(ox - (double)hx), (float)(oy - (double)hy), (float)(oz - (double)hz), qw.y);
+}
+
 // ------------------------------------------------------- launcher exports
 
 struct ListArgs {
@@ -156,7 +181,7 @@ struct ListArgs {
     int cap;                 // list entries per atom
     int cap_seg;             // staging entries per atom and z layer
     const double *pos;       // FP64 x|y|z rows of n atoms, caller order
-    float4 *coord;           // per slot two float4: (hi x, y, z, type bits), (lo x, y, z, charge)
+    float4 *coord;           // per slot two float4 written by gm_pack_record
     double4 *pos64s;         // per slot FP64 copy (FP64 mode) or nullptr
     int *type_sorted;        // per slot types (FP64 mode)
     int *perm;               // slot -> atom (global index), -1 on padding slots
@@ -166,7 +191,7 @@ struct ListArgs {
     int *cell_count, *cell_start, *cell_cursor;  // system s at sys_cell_off[s] (cell_start: ncell + 1 entries)
     int *tmp_atom;           // slot -> atom of the system, before the in-cell rank
     const int *type;         // caller order
-    const float *charge;     // caller order
+    const float2 *qw;        // caller order: (Q_hi, Q_lo | type), see gm_pack_record
     const double *charge64;  // caller order (FP64 mode)
     const int *excl_start, *excl;   // caller-order CSR (both directions, sorted)
     int *list, *count, *gmax;
@@ -175,7 +200,7 @@ struct ListArgs {
     long long *force;        // zeroed with the pack
     GridInfo *grid;          // one per system
     DevStatus *status;
-    double r_list, box[3];
+    double r_list, r_cut, r_switch, box[3];
     int periodic;
     double *bbox_scratch;    // [n_sys][bbox_blocks][9] (min, max, sum per dimension)
     int bbox_blocks, max_sys_atoms;
@@ -195,6 +220,15 @@ void gm_launch_bin(const ListArgs &a, cudaStream_t s);
 void gm_launch_build(const ListArgs &a, cudaStream_t s);
 void gm_launch_pack(const ListArgs &a, bool fp64, cudaStream_t s);
 
+// Constants of the mixed pair kernel; the low parts complete double-floats.
+struct PairConst {
+    float rc2, rsw2;          // cutoff^2, switch radius^2 (FP32 tests)
+    float rsw, rsw_lo;        // switch radius
+    float inv_w, inv_w_lo;    // 1 / (cutoff - switch radius)
+    float mds, mds_lo;        // -30 / (cutoff - switch radius): dS/dr = mds u^2 (1 - u)^2
+    float box[3], box_lo[3], inv_box[3];
+};
+
 struct ForceArgs {
     int n, n_groups, cap;
     int n_slots;             // n_groups * 32 (each system padded to whole groups)
@@ -204,15 +238,14 @@ struct ForceArgs {
     int pair_warps;          // warps per block of the FP32 pair kernel (2, 4, 8)
     int pair_grid;           // blocks of the FP32 pair kernel (0: one work item per warp; fewer: persistent)
     const float4 *coord;     // per slot (hi, lo) pairs: one 32-byte sector per gathered atom
-    const int *slot_of;      // atom -> slot
     const double4 *pos64s;
     const int *type_sorted;  // FP64 mode
     const int *perm;
     const int *list, *count, *gmax;
     int ntypes;
-    const float2 *tab32;     // (sigma_ij^2, epsilon_ij) per type pair
+    const float4 *tab32;     // (sigma_ij^2, 24 epsilon_ij) per type pair, each a double-float (hi, lo)
     const double2 *tab64;    // (sigma_ij, epsilon_ij)
-    float rc2, rsw, rc, inv_wsw;
+    PairConst pc;            // the mixed pair kernel's constants
     double rc2_64, rsw_64, rc_64, inv_wsw_64;
     int coulomb;
     float box[3], inv_box[3];
@@ -227,15 +260,14 @@ struct ForceArgs {
     int n_bonds, n_angles, n_diheds;
     const int *bond_i, *bond_j; const double *bond_k, *bond_r0;
     const int *angle_i, *angle_j, *angle_k; const double *angle_kth, *angle_th0;
-    const double2 *angle_cs;  // (cos theta0, sin theta0) per angle
     const int *dihed_i, *dihed_j, *dihed_k, *dihed_l; const double *dihed_kphi; const int *dihed_n;
     const double *dihed_delta;
+    const double2 *dihed_cs;  // (cos delta, sin delta) per dihedral
     double *epart_bonded;    // per block
     int bonded_blocks;
     // scaled 1-4 pairs
     int n14; const int *p14_i, *p14_j; double scale14_lj, scale14_coul;
     const double *sigma, *epsilon, *charge64;
-    const float4 *p14par;     // per 1-4 pair: (sigma_ij^2, 4 eps_ij * scale_lj, k_C q_i q_j * scale_coul, 0)
     double *epart14; int blocks14;
     double *energy;          // total
     int n_epart_total;       // n_groups * split + bonded_blocks + blocks14 entries
@@ -312,7 +344,7 @@ struct PackArgs {
     const int *slot_of;
     const GridInfo *grid;
     const int *type;
-    const float *charge;
+    const float2 *qw;
     const double *charge64;
     int fp64;
 };

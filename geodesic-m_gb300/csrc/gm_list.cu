@@ -344,7 +344,7 @@ __global__ void rank_kernel(ListArgs a) {
     }
 }
 
-// Every slot of every system, every force evaluation: the FP32 hi/lo copies
+// Every slot of every system, every force evaluation: the slot records
 // relative to the system's grid origin, and the force accumulators cleared.
 __global__ void pack_kernel(ListArgs a, bool fp64) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -354,10 +354,7 @@ __global__ void pack_kernel(ListArgs a, bool fp64) {
     const int n = a.n;
     const GridInfo *g = a.grid + a.atom_sys[at];
     const double x = a.pos[at], y = a.pos[n + at], z = a.pos[2 * n + at];
-    const double dx = x - g->origin[0], dy = y - g->origin[1], dz = z - g->origin[2];
-    const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
-    a.coord[2 * s] = make_float4(hx, hy, hz, __int_as_float(a.type[at]));
-    a.coord[2 * s + 1] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), a.charge[at]);
+    gm_pack_record(a.coord + 2 * s, x - g->origin[0], y - g->origin[1], z - g->origin[2], a.qw[at]);
     if (fp64) {
         a.pos64s[s] = make_double4(x, y, z, a.charge64[at]);
         a.type_sorted[s] = a.type[at];
@@ -391,16 +388,21 @@ __device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c
 // One block per group, one warp per z layer: warp `seg` tests the candidates
 // of z layer `seg` of each row box its lanes need and stages them; the block
 // then concatenates the layers into each lane's list column.
+// Each lane's column is written in distance-bucket order (GM_NBUCKET buckets
+// of the build-time distance, bounds in bucket_r2): inside the switch radius,
+// the switch band, the shell beyond the cutoff.  Within a bucket the entries
+// keep the single-warp sweep order.  The pair kernel's lanes then meet the
+// same kind of pair at the same entry and branch together.
 template <bool PERIODIC>
 __global__ void __launch_bounds__(GM_NSEG * 32)
-build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
+build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64, float3 bucket_r2) {
     // candidates of the current batch: coordinates relative to the group's
     // first atom (FP32; the rounding, under 1e-5 A for candidates within a
     // few list radii, stays far inside the FP64 re-decision margin) and
     // caller indices
     __shared__ float4 s_rel[GM_NSEG][32];
     __shared__ int s_orig[GM_NSEG][32];
-    __shared__ int s_cnt[GM_NSEG][32];
+    __shared__ int s_cnt[GM_NSEG][GM_NBUCKET][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int group = blockIdx.x, seg = wib;
     const int gseg = group * GM_NSEG + seg;
@@ -455,6 +457,7 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     const int cap_seg = a.cap_seg;
     int *my_stage = a.stage + (size_t)gseg * 32 * cap_seg + lane;
     int cnt = 0;
+    int nb[GM_NBUCKET] = {0, 0, 0, 0};  // staged entries per bucket
     const double bx[3] = {a.box[0], a.box[1], a.box[2]};
     unsigned remaining = __ballot_sync(0xffffffffu, valid);
     while (remaining) {
@@ -499,7 +502,7 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                     // distance tests of all 32 staged candidates: bit k of
                     // `near` within the list radius plus the margin, of `sure`
                     // within it minus the margin
-                    unsigned near = 0, sure = 0;
+                    unsigned near = 0, sure = 0, bkt_lo = 0, bkt_hi = 0;
 #pragma unroll
                     for (int k = 0; k < 32; k++) {
                         const float4 c = s_rel[wib][k];
@@ -512,6 +515,11 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                         const float r2 = dx * dx + dy * dy + dz * dz;
                         near |= (r2 <= rl2_hi ? 1u : 0u) << k;
                         sure |= (r2 <= rl2_lo ? 1u : 0u) << k;
+                        // the bucket, two bits per candidate
+                        const unsigned bk = (r2 > bucket_r2.x ? 1u : 0u) + (r2 > bucket_r2.y ? 1u : 0u) +
+                                            (r2 > bucket_r2.z ? 1u : 0u);
+                        if (k < 16) bkt_lo |= bk << (2 * k);
+                        else bkt_hi |= bk << (2 * (k - 16));
                     }
                     near &= m < 32 ? (1u << m) - 1u : 0xffffffffu;
                     const int self = s - base;
@@ -539,7 +547,12 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
                                 for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
                             if (excluded) continue;
                         }
-                        if (cnt < cap_seg) my_stage[(size_t)cnt * 32] = base + k;
+                        const int bk = (int)(((k < 16 ? bkt_lo >> (2 * k) : bkt_hi >> (2 * (k - 16)))) & 3u);
+                        if (cnt < cap_seg) {
+                            my_stage[(size_t)cnt * 32] = (base + k) | (bk << GM_BUCKET_SHIFT);
+#pragma unroll
+                            for (int q = 0; q < GM_NBUCKET; q++) nb[q] += bk == q;
+                        }
                         cnt++;
                     }
                 }
@@ -551,20 +564,39 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64) {
     for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
     if (lane == 0) atomicMax(&a.status->max_layer, (unsigned)lmax);
     const int staged = cnt < cap_seg ? cnt : cap_seg;
-    s_cnt[seg][lane] = staged;
-    __syncthreads();
-    int off = 0, total = 0;
 #pragma unroll
-    for (int k = 0; k < GM_NSEG; k++) {
-        const int ck = s_cnt[k][lane];
-        off += k < seg ? ck : 0;
-        total += ck;
+    for (int q = 0; q < GM_NBUCKET; q++) s_cnt[seg][q][lane] = nb[q];
+    __syncthreads();
+    // this layer's first position in each bucket: the earlier buckets of all
+    // layers, then this bucket of the earlier layers
+    int off[GM_NBUCKET];
+    int total = 0;
+#pragma unroll
+    for (int q = 0; q < GM_NBUCKET; q++) {
+        int before = 0, all = 0;
+#pragma unroll
+        for (int k = 0; k < GM_NSEG; k++) {
+            const int ck = s_cnt[k][q][lane];
+            before += k < seg ? ck : 0;
+            all += ck;
+        }
+        off[q] = total + before;
+        total += all;
     }
     int smax = staged;
     for (int o = 16; o > 0; o >>= 1) smax = max(smax, __shfl_xor_sync(0xffffffffu, smax, o));
     int *my_list = a.list + (size_t)group * 32 * cap + lane;
     for (int e = 0; e < smax; e++) {
-        if (e < staged && off + e < cap) my_list[(size_t)(off + e) * 32] = my_stage[(size_t)e * 32];
+        if (e < staged) {
+            const int v = my_stage[(size_t)e * 32];
+            const int bk = v >> GM_BUCKET_SHIFT;
+            int pos = 0;
+#pragma unroll
+            for (int q = 0; q < GM_NBUCKET; q++) {
+                if (bk == q) { pos = off[q]; off[q]++; }
+            }
+            if (pos < cap) my_list[(size_t)pos * 32] = v & GM_SLOT_MASK;
+        }
     }
     if (seg == 0) {
         if (valid) a.count[s] = total < cap ? total : cap;
@@ -628,8 +660,11 @@ void gm_launch_build(const ListArgs &a, cudaStream_t s) {
     const int groups = a.n_slots / 32;
     const double rl2 = a.r_list * a.r_list;  // neighbor.rs:25
     const double margin = 1e-3 * (rl2 > 144.0 ? rl2 / 144.0 : 1.0);
+    // bucket bounds: the switch radius, the cutoff, halfway to the list radius
+    const double rsh = 0.5 * (a.r_cut + a.r_list);
+    const float3 bk = make_float3((float)(a.r_switch * a.r_switch), (float)(a.r_cut * a.r_cut), (float)(rsh * rsh));
     if (a.periodic)
-        build_kernel<true><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
+        build_kernel<true><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2, bk);
     else
-        build_kernel<false><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2);
+        build_kernel<false><<<groups, GM_NSEG * 32, 0, s>>>(a, (float)(rl2 - margin), (float)(rl2 + margin), rl2, bk);
 }
