@@ -78,14 +78,14 @@ def workload(rank=0):
     return synth.generate(N_ATOMS, seed=replica_seed(rank), temperature=300.0, relax_iters=1000)
 
 
-def config_dict(extra=None):
-    d = {"workload": "synthetic lattice chain, 50,000 atoms (cube 79.6 A), mixed precision, 2 fs BAB + RATTLE",
-         "n_atoms": N_ATOMS, "seed": SEED, "cutoff_A": 10.0, "switch_A": 8.0, "list_radius_A": 12.0,
-         "coulomb": True, "scale14": [0.5, 1 / 1.2], "periodic": False, "dt_fs": 2.0,
-         "l2": "flushed between timed steps (256 MB memset outside the timed span)"}
-    if extra:
-        d.update(extra)
-    return d
+def config_dict():
+    """The workload, identical in both arms' lines."""
+    return {"workload": "synthetic lattice chain, 50,000 atoms (2.15 A lattice, cube 79.6 A), FIRE-minimised "
+                        "(1000 iterations) then MB 300 K, mixed precision, 2 fs BAB + RATTLE",
+            "n_atoms": N_ATOMS, "seed": SEED, "cutoff_A": 10.0, "switch_A": 8.0, "list_radius_A": 12.0,
+            "coulomb": True, "scale14": [0.5, 1 / 1.2], "periodic": False, "dt_fs": 2.0,
+            "relaxation": "FIRE, 1000 iterations", "parallelism": "replicas, one system per GPU",
+            "l2": "flushed between timed steps (256 MB memset outside the timed span)"}
 
 
 class ClockSampler:
@@ -135,7 +135,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(k)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "span": "the whole CUDA arm (warm-up, timed steps, profiling loops)"}
 
 
 def measured_peaks():
@@ -157,14 +157,25 @@ def pinned_like(a):
 
 
 def run_cuda(args, rank, world):
+    """The CUDA arm; nvidia-smi samples the clocks over all of it."""
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    atoms, topo, state, info = workload(rank)
+    with ClockSampler(dev) as clk:
+        line = _cuda_arm(args, rank, world, dev, atoms, topo, state)
+    if line is not None:
+        line["clocks"] = clk.summary()
+    return line
+
+
+def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     import torch
 
     from geodesic_cuda import backend
     import oracle
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    atoms, topo, state, info = workload(rank)
     p = backend.SimParams(precision=backend.PRECISION_MIXED, device=dev, **PHYS)
     be = backend.CudaBackend(atoms, topo, p)
     be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
@@ -177,17 +188,16 @@ def run_cuda(args, rank, world):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        t0 = time.perf_counter()
-        dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
-                               flush_bytes=L2_FLUSH_BYTES)
-        t1 = time.perf_counter()
+    t0 = time.perf_counter()
+    dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                           flush_bytes=L2_FLUSH_BYTES)
+    t1 = time.perf_counter()
     torch.cuda.synchronize()
     c1 = be.counters()
     sec = max_over_ranks(dev_ms / 1e3, f"cuda:{dev}")
     pairs = c1["pairs"]
     result = dict(sec=sec, wall=t1 - t0, pairs=pairs, rebuilds=c1["rebuilds"] - c0["rebuilds"],
-                  launches=c1["launches"] - c0["launches"], clocks=clk.summary())
+                  launches=c1["launches"] - c0["launches"])
     if rank != 0:
         return None
     if args.quick:
@@ -197,9 +207,15 @@ def run_cuda(args, rank, world):
                 "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"]),
                 "kernel_ms": {"pair": round(be.profile("pair", 3), 5), "rebuild": round(be.profile("rebuild", 2), 5)},
                 "autotuner": tuned}
-    # steady state: back-to-back steps, no flush (L2 keeps part of the list)
-    t_bb = be.time_steps(DT_PS, min(args.steps, 2000), first_step=args.warmup + args.steps) / 1e3
-    # roofline of the pair kernel: SURVEY algorithmic bytes 4 P + 52 N per launch
+    # steady state: 1,000 back-to-back steps, no flush (L2 keeps part of the
+    # list), with the list rebuilds they meet (amortised per step)
+    cb0 = be.counters()
+    n_bb = 1000
+    t_bb = be.time_steps(DT_PS, n_bb, first_step=args.warmup + args.steps) / 1e3
+    reb_bb = be.counters()["rebuilds"] - cb0["rebuilds"]
+    # roofline of the pair kernel: algorithmic bytes 4 P + 52 N per launch (one
+    # int32 index per half-list pair of neighbor.rs:25-43, plus per atom the
+    # coordinates, charge, type, force and energy of force/nonbonded.rs:20-82)
     t_pair = be.profile("pair", 30) / 1e3
     t_bonded = be.profile("bonded", 30) / 1e3
     t_rebuild = be.profile("rebuild", 5) / 1e3
@@ -220,11 +236,11 @@ def run_cuda(args, rank, world):
     pos_end = np.ascontiguousarray(np.zeros((3, N_ATOMS)))
     vel_end = np.ascontiguousarray(np.zeros((3, N_ATOMS)))
     be.download_state(pos_end, vel_end)
-    step_end = args.warmup + args.steps + min(args.steps, 2000)
+    step_end = args.warmup + args.steps + n_bb
     op = oracle.make_params(box=PHYS["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0,
                             n_threads=0, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2)
     errs = {}
-    fp64_nsday = None
+    fp64_nsday = fp64_tuned = fp64_pair_ms = lattice = None
     from geodesic_cuda import synth
     raw = synth.generate(N_ATOMS, seed=SEED, temperature=300.0, relax_iters=0)[2].pos
     for label, pos_k in (("generator_lattice", np.ascontiguousarray(raw)), ("step0", np.ascontiguousarray(state.pos)),
@@ -240,6 +256,14 @@ def run_cuda(args, rank, world):
             pp = pos_k.copy()
             b2.build_neighbor_list(pp)
             f = b2.compute_forces(pp).copy()
+            if label == "generator_lattice" and prec == backend.PRECISION_MIXED:
+                # the literal lattice (no relaxation): its pair count and the
+                # mixed pair kernel's time on it, beside the timed state's
+                b2.upload_state(np.ascontiguousarray(raw), np.ascontiguousarray(state.vel))
+                b2.forces_resident()
+                b2.autotune(reps=3)
+                lattice = {"half_list_pairs": int(b2.counters()["pairs"]),
+                           "pair_kernel_ms": round(b2.profile("pair", 20), 5)}
             errs[label][name] = dict(
                 force_rel_l2=float(np.linalg.norm(f - f_ref) / np.linalg.norm(f_ref)),
                 force_max_rel=float(np.max(np.abs(f - f_ref) / np.maximum(np.abs(f_ref), 1.0))),
@@ -247,6 +271,8 @@ def run_cuda(args, rank, world):
             if prec == backend.PRECISION_FP64 and fp64_nsday is None:
                 b2.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
                 b2.forces_resident()
+                fp64_tuned = b2.autotune(reps=3)  # the FP64 pair kernel gets the same tuning
+                fp64_pair_ms = b2.profile("pair", 10)
                 b2.run_resident(DT_PS, 3)
                 b2.synchronize()
                 n64 = max(50, min(args.steps, 300))
@@ -277,12 +303,15 @@ def run_cuda(args, rank, world):
         "ms_per_step": round(1e3 * sec / args.steps, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 pair math, int64 fixed-point forces, fp64 state/energy",
         "data": "synthetic (seeded generator, no dataset)",
-        "config": config_dict({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                               "list_rebuilds_in_timed_region": result["rebuilds"]}),
+        "config": config_dict(), "replicas": world, "list_rebuilds_in_timed_region": result["rebuilds"],
         "pairs_per_s": round(world * pairs * steps_per_s, 1), "half_list_pairs": pairs,
+        "literal_lattice": lattice,
         "fp64_path_ns_per_day": round(fp64_nsday, 3) if fp64_nsday else None,
+        "fp64_pair_kernel": {"ms": round(fp64_pair_ms, 5) if fp64_pair_ms else None, "autotuner": fp64_tuned},
         "mixed_over_fp64": round(ns_per_day(args.steps, sec) / fp64_nsday, 2) if fp64_nsday else None,
-        "steady_state_ns_per_day": round(ns_per_day(min(args.steps, 2000), t_bb), 3),
+        "steady_state": {"ns_per_day": round(ns_per_day(n_bb, t_bb), 3), "steps": n_bb,
+                         "ms_per_step": round(1e3 * t_bb / n_bb, 5), "list_rebuilds": int(reb_bb),
+                         "note": "back to back, no L2 flush, list rebuilds included (amortised)"},
         "errors_vs_fp64_oracle": errs,
         "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
                       "pair14": round(t_pair14 * 1e3, 5), "forces": round(t_forces * 1e3, 5),
@@ -295,7 +324,6 @@ def run_cuda(args, rank, world):
                 "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
         "gpu_launches": int(result["launches"]),
         "autotuner": tuned,
-        "clocks": result["clocks"],
         "cpu_baseline": cpu,
     }
     return line
@@ -362,8 +390,8 @@ def run_reference(args):
     pi, pj = oracle.neighbor_build(pos.copy(), atoms, topo, op, cells=True)
     b.set_pairs(pi, pj, pos)  # the reference's pair set, without timing its O(N^2) build here
     f = b.compute_forces(pos)
-    n_w = min(args.warmup, 3)
-    n_t = max(1, min(args.steps, 20))
+    n_w = args.warmup
+    n_t = max(1, min(args.steps, 200))  # ~30 ms per step: a bounded sample
     t_total, n_reb = 0.0, 0
     for k in range(n_w + n_t):
         t0 = time.perf_counter()
@@ -381,7 +409,7 @@ def run_reference(args):
     return {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "ns/day", "n_gpus": 1,
             "steps": n_t, "warmup": n_w, "ms_per_step": round(1e3 * t_total / n_t, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded generator)",
-            "config": config_dict({"steps_requested": args.steps}),
+            "config": config_dict(), "replicas": 1, "steps_requested": args.steps,
             "cpu_baseline": {"value": round(val, 4), "unit": "ns/day", "cores": nthreads, "kind": "port",
                              "sample": f"{n_t} BAB steps of the oracle loop after {n_w} warm-up steps "
                                        f"({n_reb} O(N^2) list rebuilds in the timed steps)"},
@@ -599,8 +627,10 @@ def run_scaled(args, n_atoms, precision, relax, steps_default):
     t_reb = be.profile("rebuild", 3) / 1e3
     peak, peak_kind = measured_peaks()
     alg_pair = 4 * pairs + 52 * n_atoms
-    # list build algorithmic bytes (SURVEY 8d B_list): N (16 + 8 + 16) + 4 P + 4 N
-    alg_list = n_atoms * 44 + 4 * 2 * pairs
+    # list build algorithmic bytes: per atom 16 B read, 8 B cell key and index,
+    # 16 B sorted coordinates and 4 B offset written, plus one int32 index per
+    # half-list pair (neighbor.rs:8-55's output)
+    alg_list = n_atoms * 44 + 4 * pairs
     return {"metric": f"ns/day at {n_atoms} atoms", "value": round(ns_per_day(steps, sec), 3), "unit": "ns/day",
             "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sec / steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

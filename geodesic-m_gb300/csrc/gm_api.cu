@@ -74,7 +74,7 @@ struct gm_ctx {
     int bbox_blocks = 0;
     // list
     int cap = 0, cap_seg = 0, n_groups = 0;  // list entries per atom; staging entries per atom and z layer
-    int split = 1;                   // warps per group in the FP32 pair kernel
+    int split = 1;                   // warps per group in the pair kernel
     int pair_warps = 4, pair_grid = 0;  // FP32 pair kernel block size and grid (0: one item per warp)
     int *d_list = nullptr, *d_count = nullptr, *d_gmax = nullptr, *d_stage = nullptr;
     bool built = false;
@@ -87,6 +87,7 @@ struct gm_ctx {
     double *d_bk = nullptr, *d_br0 = nullptr, *d_akth = nullptr, *d_ath0 = nullptr, *d_dkphi = nullptr,
            *d_ddelta = nullptr;
     double2 *d_dcs = nullptr;  // (cos delta, sin delta) per dihedral
+    double4 *d_p14par = nullptr;  // per 1-4 pair (sigma, 4 eps s_lj, 24 eps s_lj, k_C q_i q_j s_coul)
     // 1-4
     int n14 = 0, blocks14 = 0;
     int *d_p14i = nullptr, *d_p14j = nullptr;
@@ -257,7 +258,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.atom_sys = c->d_atom_sys;
     a.e_sys = c->n_sys > 1 ? c->d_e_sys : nullptr;
     a.cap = c->cap;
-    a.split = c->fp64 ? 1 : c->split;
+    a.split = c->split;
     a.pair_warps = c->pair_warps;
     a.pair_grid = c->pair_grid;
     a.coord = c->d_coord;
@@ -314,6 +315,7 @@ ForceArgs force_args(gm_ctx *c) {
     a.n14 = c->n14; a.p14_i = c->d_p14i; a.p14_j = c->d_p14j;
     a.scale14_lj = c->p.scale14_lj; a.scale14_coul = c->p.scale14_coul;
     a.sigma = c->d_sigma; a.epsilon = c->d_eps; a.charge64 = c->d_charge64;
+    a.p14par = c->d_p14par;
     a.blocks14 = c->blocks14;
     a.epart14 = c->d_epart + pair_parts + c->bonded_blocks;
     a.energy = c->d_energy;
@@ -1298,9 +1300,20 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         std::vector<int> a((size_t)p14.size()), b((size_t)p14.size());
         for (size_t k = 0; k < p14.size(); k++) { a[k] = p14[k].first; b[k] = p14[k].second; }
         c->n14 = (int)p14.size();
-        c->blocks14 = (c->n14 + 255) / 256;
+        c->blocks14 = (c->n14 + GM_BONDED_THREADS - 1) / GM_BONDED_THREADS;
         TRY(dupload(c, &c->d_p14i, a.data(), a.size()));
         TRY(dupload(c, &c->d_p14j, b.data(), b.size()));
+        // per-pair parameters (force/nonbonded.rs:46-47 mixing; the scales
+        // and Coulomb factor applied once)
+        std::vector<double4> par(p14.size());
+        for (size_t k = 0; k < p14.size(); k++) {
+            const int i = a[k], j = b[k];
+            const double sg = 0.5 * (atoms->sigma[i] + atoms->sigma[j]);
+            const double ep = std::sqrt(atoms->epsilon[i] * atoms->epsilon[j]);
+            const double qq = p.coulomb ? 332.0522173 * charge64[(size_t)i] * charge64[(size_t)j] : 0.0;
+            par[k] = make_double4(sg, p.scale14_lj * 4.0 * ep, p.scale14_lj * 24.0 * ep, p.scale14_coul * qq);
+        }
+        TRY(dupload(c, &c->d_p14par, par.data(), par.size()));
     }
     // ---- constraints as independent clusters
     c->n_constr = (int)t->n_constr;
@@ -2183,7 +2196,6 @@ int32_t gm_ensemble_energies(gm_ctx *c, double *e_pot, double *e_kin) {
 int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
     if (!c || reps < 1) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
-    if (c->fp64) return fail(c, GM_ERR_UNSUPPORTED, "the autotuner tunes the FP32 pair kernel");
     int rc = ensure_forces(c);
     if (rc) return rc;
     int sms = 0;
@@ -2203,9 +2215,9 @@ int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
                 c->pair_warps = w;
                 c->pair_grid = gk ? gk * std::max(sms, 1) : 0;
                 ForceArgs fa = force_args(c);
-                gm_launch_pair(fa, false, c->stream);  // warm-up
+                gm_launch_pair(fa, c->fp64, c->stream);  // warm-up
                 cudaEventRecord(e0, c->stream);
-                for (int r = 0; r < reps; r++) gm_launch_pair(fa, false, c->stream);
+                for (int r = 0; r < reps; r++) gm_launch_pair(fa, c->fp64, c->stream);
                 cudaEventRecord(e1, c->stream);
                 cudaEventSynchronize(e1);
                 float ms = 0.f;

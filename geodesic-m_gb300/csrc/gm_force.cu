@@ -17,7 +17,6 @@
 
 namespace {
 
-constexpr int kPairWarps = 4;
 constexpr int kChunk = 32;
 constexpr int kBatch = 4;  // list entries gathered together in the mixed pair kernel
 constexpr double kCoulomb64 = 332.0522173;
@@ -227,21 +226,30 @@ pair_kernel_mixed(int n, int n_slots, int cap, int split, const float4 *__restri
     }
 }
 
-template <bool PERIODIC, bool COULOMB, bool BATCH>
-__global__ void __launch_bounds__(kPairWarps * 32)
-pair_kernel_f64(int n, int n_slots, int cap, const double4 *__restrict__ p64, const int *__restrict__ type_s,
-                const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
-                const int *__restrict__ gmax, int ntypes, const double2 *__restrict__ tab, double rc2, double rsw,
-                double rc, double bx, double by, double bz, long long *__restrict__ force,
-                double *__restrict__ epart, DevStatus *st, const int *__restrict__ group_sys, long long *e_sys) {
+// FP64 nonbonded kernel (the FP64 path): the reference's arithmetic
+// (force/nonbonded.rs:20-82) in FP64 on the sorted FP64 copies.  The same
+// work split as the mixed kernel (a 32-atom group's columns over `split`
+// warps, 2/4/8 warps per block, optional persistent grid), and the same
+// summation: FP64 sums over chunks of 32 entries folded into int64, so every
+// launch shape gives the same bits.
+template <bool PERIODIC, bool COULOMB, bool BATCH, int W>
+__global__ void __launch_bounds__(W * 32)
+pair_kernel_f64(int n, int n_slots, int cap, int split, const double4 *__restrict__ p64,
+                const int *__restrict__ type_s, const int *__restrict__ perm, const int *__restrict__ list,
+                const int *__restrict__ count, const int *__restrict__ gmax, int ntypes,
+                const double2 *__restrict__ tab, double rc2, double rsw, double rc, double bx, double by, double bz,
+                long long *__restrict__ force, double *__restrict__ epart, DevStatus *st,
+                const int *__restrict__ group_sys, long long *e_sys) {
     extern __shared__ double2 s_tab64[];
     if (!BATCH) {
         for (int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x) s_tab64[t] = tab[t];
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
-    const int group = blockIdx.x * kPairWarps + (threadIdx.x >> 5);
-    if (group * 32 >= n_slots) return;
+    const double wsw = rc - rsw;
+    const int n_work = (n_slots / 32) * split;
+    for (int wid = blockIdx.x * W + (threadIdx.x >> 5); wid < n_work; wid += gridDim.x * W) {
+    const int group = wid / split, part = wid - group * split;
     const int s = group * 32 + lane;
     const int atom = perm[s];  // -1 on a padding slot
     const bool valid = atom >= 0;
@@ -251,61 +259,70 @@ pair_kernel_f64(int n, int n_slots, int cap, const double4 *__restrict__ p64, co
     const double2 *trow = (BATCH ? tab + (size_t)group_sys[group] * ntypes * ntypes : s_tab64) + ti * ntypes;
     const double qi = mi.w * kCoulomb64;
     const int gm = gmax[group];
+    const int per = ((gm + split - 1) / split + kChunk - 1) / kChunk * kChunk;
+    const int e_begin = part * per, e_end = min(gm, e_begin + per);
     const int *L = list + (size_t)group * 32 * cap + lane;
-    double fx = 0, fy = 0, fz = 0, eacc = 0;
-    const double wsw = rc - rsw;
-    for (int e = 0; e < gm; e++) {
-        if (e >= cnt) continue;
-        const int j = __ldg(L + (size_t)e * 32);
-        const double4 pj = p64[j];
-        double dx = pj.x - mi.x, dy = pj.y - mi.y, dz = pj.z - mi.z;
-        if (PERIODIC) {
-            dx -= bx * round(dx / bx);
-            dy -= by * round(dy / by);
-            dz -= bz * round(dz / bz);
-        }
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 > rc2 || r2 == 0.0) continue;
-        const double r = sqrt(r2);
-        const double rinv = 1.0 / r;
-        const double2 p = trow[type_s[j]];
-        double v = 0.0, fr = 0.0;  // fr = F_r (radial magnitude)
-        if (p.y != 0.0) {
-            const double sr = p.x * rinv;
-            const double s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
-            v = 4.0 * p.y * (s12 - s6);
-            fr = 24.0 * p.y * rinv * (2.0 * s12 - s6);
-        }
-        if (COULOMB) {
-            const double vc = qi * pj.w * rinv;
-            v += vc;
-            fr += vc * rinv;
-        }
-        if (r > rsw) {
-            const double u = (r - rsw) / wsw;
-            const double u2 = u * u;
-            const double sw = 1.0 - 10.0 * u2 * u + 15.0 * u2 * u2 - 6.0 * u2 * u2 * u;
-            const double dsw = -30.0 * u2 * (1.0 - u) * (1.0 - u) / wsw;
-            fr = fr * sw - v * dsw;
-            v *= sw;
-        }
-        const double g = fr * rinv;
-        fx -= g * dx;
-        fy -= g * dy;
-        fz -= g * dz;
-        eacc += v;
-    }
+    long long ax = 0, ay = 0, az = 0;
+    double eacc = 0.0;
     unsigned int bad = 0;
-    if (valid) {
-        gm_atomic_fix_add(force + atom, gm_to_fix_checked(fx, bad));
-        gm_atomic_fix_add(force + n + atom, gm_to_fix_checked(fy, bad));
-        gm_atomic_fix_add(force + 2 * n + atom, gm_to_fix_checked(fz, bad));
+    for (int e0 = e_begin; e0 < e_end; e0 += kChunk) {
+        double fx = 0, fy = 0, fz = 0;
+        const int e1 = min(e0 + kChunk, min(e_end, cnt));
+        for (int e = e0; e < e1; e++) {
+            const int j = __ldg(L + (size_t)e * 32);
+            const double4 pj = p64[j];
+            double dx = pj.x - mi.x, dy = pj.y - mi.y, dz = pj.z - mi.z;
+            if (PERIODIC) {
+                dx = gm_min_image(dx, bx);
+                dy = gm_min_image(dy, by);
+                dz = gm_min_image(dz, bz);
+            }
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 > rc2 || r2 == 0.0) continue;
+            const double r = sqrt(r2);
+            const double rinv = 1.0 / r;
+            const double2 p = trow[type_s[j]];
+            double v = 0.0, fr = 0.0;  // fr = F_r (radial magnitude)
+            if (p.y != 0.0) {
+                const double sr = p.x * rinv;
+                const double s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
+                v = 4.0 * p.y * (s12 - s6);
+                fr = 24.0 * p.y * rinv * (2.0 * s12 - s6);
+            }
+            if (COULOMB) {
+                const double vc = qi * pj.w * rinv;
+                v += vc;
+                fr += vc * rinv;
+            }
+            if (r > rsw) {
+                const double u = (r - rsw) / wsw;
+                const double u2 = u * u;
+                const double sw = 1.0 - 10.0 * u2 * u + 15.0 * u2 * u2 - 6.0 * u2 * u2 * u;
+                const double dsw = -30.0 * u2 * (1.0 - u) * (1.0 - u) / wsw;
+                fr = fr * sw - v * dsw;
+                v *= sw;
+            }
+            const double g = fr * rinv;
+            fx -= g * dx;
+            fy -= g * dy;
+            fz -= g * dz;
+            eacc += v;
+        }
+        ax += gm_to_fix_checked(fx, bad);
+        ay += gm_to_fix_checked(fy, bad);
+        az += gm_to_fix_checked(fz, bad);
+    }
+    if (valid && e_begin < e_end) {
+        gm_atomic_fix_add(force + atom, ax);
+        gm_atomic_fix_add(force + n + atom, ay);
+        gm_atomic_fix_add(force + 2 * n + atom, az);
     }
     for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
-    if (lane == 0) epart[group] = 0.5 * eacc;
+    if (lane == 0) epart[wid] = 0.5 * eacc;
     if (e_sys && lane == 0) gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
     bad = __reduce_or_sync(0xffffffffu, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
+    }
 }
 
 // ----------------------------------------------------------------- bonded
@@ -357,10 +374,10 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         const double k = a.bond_k[t], r0 = a.bond_r0[t];
         const double r2 = dot(d, d);
         if (r2 > 0.0) {
-            const double r = sqrt(r2);
-            const double dr = r - r0;
+            const double ir = rsqrt(r2);
+            const double dr = r2 * ir - r0;
             e = k * dr * dr;
-            const double g = 2.0 * k * dr / r;
+            const double g = 2.0 * k * dr * ir;
             add_force(a.force, n, i, g * d.x, g * d.y, g * d.z, bad);
             add_force(a.force, n, j, -g * d.x, -g * d.y, -g * d.z, bad);
         }
@@ -370,9 +387,10 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         const int i = a.angle_i[q], j = a.angle_j[q], kk = a.angle_k[q];
         first = i;
         const V3 b1 = pdiff<MI>(a, i, j), b2 = pdiff<MI>(a, kk, j);
-        const double r1 = sqrt(dot(b1, b1)), r2 = sqrt(dot(b2, b2));
-        if (r1 != 0.0 && r2 != 0.0) {
-            double c = dot(b1, b2) / sqrt(dot(b1, b1) * dot(b2, b2));
+        const double q1 = dot(b1, b1), q2 = dot(b2, b2);
+        if (q1 != 0.0 && q2 != 0.0) {
+            const double i1 = rsqrt(q1), i2 = rsqrt(q2);
+            double c = dot(b1, b2) * i1 * i2;
             c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
             double sn = sqrt(1.0 - c * c);
             sn = sn > 1e-8 ? sn : 1e-8;
@@ -380,7 +398,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
             const double k = a.angle_kth[q];
             e = k * dth * dth;
             const double aa = 2.0 * k * dth / sn;
-            const double ir12 = 1.0 / (r1 * r2), ir11 = 1.0 / (r1 * r1), ir22 = 1.0 / (r2 * r2);
+            const double ir12 = i1 * i2, ir11 = i1 * i1, ir22 = i2 * i2;
             const V3 fi = {aa * (b2.x * ir12 - c * b1.x * ir11), aa * (b2.y * ir12 - c * b1.y * ir11),
                            aa * (b2.z * ir12 - c * b1.z * ir11)};
             const V3 fk = {aa * (b1.x * ir12 - c * b2.x * ir22), aa * (b1.y * ir12 - c * b2.y * ir22),
@@ -396,16 +414,17 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         first = i;
         const V3 b1 = pdiff<MI>(a, j, i), b2 = pdiff<MI>(a, k, j), b3 = pdiff<MI>(a, l, k);
         const V3 m = cross(b1, b2), nv = cross(b2, b3);
-        const double m2 = dot(m, m), n2 = dot(nv, nv), b2l = sqrt(dot(b2, b2));
-        if (m2 != 0.0 && n2 != 0.0 && b2l != 0.0) {
+        const double m2 = dot(m, m), n2 = dot(nv, nv), b22 = dot(b2, b2);
+        if (m2 != 0.0 && n2 != 0.0 && b22 != 0.0) {
+            const double ib2 = rsqrt(b22), b2l = b22 * ib2;
             // phi = atan2(y, x) as in the reference; cos(n phi - delta) and
             // sin(n phi - delta) are taken without the transcendentals:
             // (cos phi, sin phi) = (x, y) / |(x, y)|, raised to the n-th
             // power as a complex number, then rotated by delta (the FP64
             // pipe of this part is 1/64 of its FP32 one)
             const double x = dot(m, nv);
-            const double y = dot(cross(m, nv), b2) / b2l;
-            const double ir = 1.0 / sqrt(x * x + y * y);
+            const double y = dot(cross(m, nv), b2) * ib2;
+            const double ir = rsqrt(x * x + y * y);
             const double c1 = x * ir, s1 = y * ir;
             const unsigned mult = a.dihed_n[q];
             double cn = 1.0, sn = 0.0;
@@ -418,9 +437,10 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
             const double kphi = a.dihed_kphi[q];
             e = kphi * (1.0 + (cn * cs.x + sn * cs.y));
             const double dv = kphi * (double)mult * (sn * cs.x - cn * cs.y);  // -dV/dphi
-            const double si = -dv * b2l / m2, sl = dv * b2l / n2;
+            const double imn = dv * b2l / (m2 * n2);
+            const double si = -imn * n2, sl = imn * m2;
             const V3 fi = {m.x * si, m.y * si, m.z * si}, fl = {nv.x * sl, nv.y * sl, nv.z * sl};
-            const double ib = 1.0 / (b2l * b2l);
+            const double ib = ib2 * ib2;
             const double p = dot(b1, b2) * ib, qq = dot(b3, b2) * ib;
             const V3 fj = {-(p + 1.0) * fi.x + qq * fl.x, -(p + 1.0) * fi.y + qq * fl.y, -(p + 1.0) * fi.z + qq * fl.z};
             const V3 fk = {p * fi.x - (qq + 1.0) * fl.x, p * fi.y - (qq + 1.0) * fl.y, p * fi.z - (qq + 1.0) * fl.z};
@@ -431,10 +451,10 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, int blk) {
         }
     }
     // fixed-order block reduction of the energy
-    __shared__ double se[256];
+    __shared__ double se[GM_BONDED_THREADS];
     se[threadIdx.x] = e;
     __syncthreads();
-    for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    for (int s2 = GM_BONDED_THREADS / 2; s2 > 0; s2 >>= 1) {
         if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
         __syncthreads();
     }
@@ -459,29 +479,21 @@ __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
         const V3 d = pdiff<MI>(a, j, i);
         const double r2 = dot(d, d);
         if (r2 > 0.0) {
-            const double r = sqrt(r2), rinv = 1.0 / r;
-            double v = 0.0, fr = 0.0;
-            const double sg = 0.5 * (a.sigma[i] + a.sigma[j]), ep = sqrt(a.epsilon[i] * a.epsilon[j]);
-            if (a.scale14_lj != 0.0 && ep != 0.0) {
-                const double sr = sg * rinv, s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
-                v += a.scale14_lj * (4.0 * ep * (s12 - s6));
-                fr += a.scale14_lj * (24.0 * ep * rinv * (2.0 * s12 - s6));
-            }
-            if (a.coulomb && a.scale14_coul != 0.0) {
-                const double qq = kCoulomb64 * a.charge64[i] * a.charge64[j];
-                v += a.scale14_coul * qq * rinv;
-                fr += a.scale14_coul * qq * rinv * rinv;
-            }
-            e = v;
-            const double g = fr * rinv;
+            // (sigma_ij, 4 eps_ij s_lj, 24 eps_ij s_lj, k_C q_i q_j s_coul)
+            const double4 p = a.p14par[t];
+            const double rinv = rsqrt(r2);
+            const double sr = p.x * rinv, s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
+            const double vc = p.w * rinv;
+            e = p.y * (s12 - s6) + vc;
+            const double g = (p.z * (2.0 * s12 - s6) + vc) * rinv * rinv;
             add_force(a.force, n, i, -g * d.x, -g * d.y, -g * d.z, bad);
             add_force(a.force, n, j, g * d.x, g * d.y, g * d.z, bad);
         }
     }
-    __shared__ double se[256];
+    __shared__ double se[GM_BONDED_THREADS];
     se[threadIdx.x] = e;
     __syncthreads();
-    for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    for (int s2 = GM_BONDED_THREADS / 2; s2 > 0; s2 >>= 1) {
         if (threadIdx.x < s2) se[threadIdx.x] += se[threadIdx.x + s2];
         __syncthreads();
     }
@@ -492,13 +504,13 @@ __device__ __forceinline__ void pair14_block(const ForceArgs &a, int blk) {
 }
 
 template <bool MI>
-__global__ void __launch_bounds__(256) bonded_kernel(ForceArgs a) { bonded_block<MI>(a, blockIdx.x); }
+__global__ void __launch_bounds__(GM_BONDED_THREADS) bonded_kernel(ForceArgs a) { bonded_block<MI>(a, blockIdx.x); }
 template <bool MI>
-__global__ void __launch_bounds__(256) pair14_kernel(ForceArgs a) { pair14_block<MI>(a, blockIdx.x); }
+__global__ void __launch_bounds__(GM_BONDED_THREADS) pair14_kernel(ForceArgs a) { pair14_block<MI>(a, blockIdx.x); }
 // Both in one launch: the first bonded_blocks blocks take the bonded terms,
 // the rest the 1-4 pairs (independent work; integer force sums).
 template <bool MI>
-__global__ void __launch_bounds__(256) bonded_pair14_kernel(ForceArgs a) {
+__global__ void __launch_bounds__(GM_BONDED_THREADS) bonded_pair14_kernel(ForceArgs a) {
     if ((int)blockIdx.x < a.bonded_blocks) bonded_block<MI>(a, blockIdx.x);
     else pair14_block<MI>(a, blockIdx.x - a.bonded_blocks);
 }
@@ -515,12 +527,11 @@ __global__ void __launch_bounds__(256) energy_kernel(const double *epart, int n,
 
 int gm_bonded_blocks(int nb, int na, int nd) {
     const long long t = (long long)nb + na + nd;
-    return (int)((t + 255) / 256);
+    return (int)((t + GM_BONDED_THREADS - 1) / GM_BONDED_THREADS);
 }
 
 void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
     if (a.n == 0) return;
-    const int blocks = (a.n_groups + kPairWarps - 1) / kPairWarps;
     const bool batch = a.e_sys != nullptr;
     if (!fp64) {
         const int W = a.pair_warps == 2 || a.pair_warps == 8 ? a.pair_warps : 4;
@@ -544,17 +555,25 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
 #undef GM_PAIRM
 #undef GM_PAIRMW
     } else {
-        const size_t smem = batch ? 0 : sizeof(double2) * (size_t)a.ntypes * a.ntypes;
-#define GM_PAIR64(P, Q, B)                                                                                        \
-    pair_kernel_f64<P, Q, B><<<blocks, kPairWarps * 32, smem, s>>>(                                               \
-        a.n, a.n_slots, a.cap, a.pos64s, a.type_sorted, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab64,     \
+        const int W = a.pair_warps == 2 || a.pair_warps == 8 ? a.pair_warps : 4;
+        int blocks64 = (a.n_groups * a.split + W - 1) / W;
+        if (a.pair_grid > 0 && a.pair_grid < blocks64) blocks64 = a.pair_grid;
+        const size_t tab_bytes = sizeof(double2) * (size_t)a.ntypes * a.ntypes;
+        const bool gtab = batch || tab_bytes > 48 * 1024;
+        const size_t smem = gtab ? 0 : tab_bytes;
+#define GM_PAIR64W(P, Q, B, WW)                                                                                   \
+    pair_kernel_f64<P, Q, B, WW><<<blocks64, WW * 32, smem, s>>>(                                                  \
+        a.n, a.n_slots, a.cap, a.split, a.pos64s, a.type_sorted, a.perm, a.list, a.count, a.gmax, a.ntypes, a.tab64, \
         a.rc2_64, a.rsw_64, a.rc_64, a.box64[0], a.box64[1], a.box64[2], a.force, a.epart, a.status, a.group_sys, \
         a.e_sys)
-#define GM_PAIR64B(P, Q) { if (batch) GM_PAIR64(P, Q, true); else GM_PAIR64(P, Q, false); }
+#define GM_PAIR64(P, Q, B) { if (W == 2) GM_PAIR64W(P, Q, B, 2); else if (W == 8) GM_PAIR64W(P, Q, B, 8); \
+                             else GM_PAIR64W(P, Q, B, 4); }
+#define GM_PAIR64B(P, Q) { if (gtab) GM_PAIR64(P, Q, true) else GM_PAIR64(P, Q, false) }
         if (a.periodic) { if (a.coulomb) GM_PAIR64B(true, true) else GM_PAIR64B(true, false) }
         else { if (a.coulomb) GM_PAIR64B(false, true) else GM_PAIR64B(false, false) }
 #undef GM_PAIR64B
 #undef GM_PAIR64
+#undef GM_PAIR64W
     }
 }
 
@@ -562,21 +581,40 @@ void gm_launch_pair(const ForceArgs &a, bool fp64, cudaStream_t s) {
 // pair kernel only).
 void gm_launch_bonded(const ForceArgs &a, bool, cudaStream_t s) {
     if (a.bonded_blocks == 0) return;
-    if (a.bonded_mi) bonded_kernel<true><<<a.bonded_blocks, 256, 0, s>>>(a);
-    else bonded_kernel<false><<<a.bonded_blocks, 256, 0, s>>>(a);
+    if (a.bonded_mi) bonded_kernel<true><<<a.bonded_blocks, GM_BONDED_THREADS, 0, s>>>(a);
+    else bonded_kernel<false><<<a.bonded_blocks, GM_BONDED_THREADS, 0, s>>>(a);
 }
 
+// The bonded / 1-4 kernel runs beside the pair kernel on a second stream; it
+// is launched at the device's highest priority, in blocks small enough to fit
+// in the registers the pair kernel's blocks leave free on an SM, so that its
+// blocks are placed among the pair kernel's instead of after them (the two
+// load different pipes: FP64 here, FP32 there).
 void gm_launch_bonded_pair14(const ForceArgs &a, bool, cudaStream_t s) {
     const int blocks = a.bonded_blocks + a.blocks14;
     if (blocks == 0) return;
-    if (a.bonded_mi) bonded_pair14_kernel<true><<<blocks, 256, 0, s>>>(a);
-    else bonded_pair14_kernel<false><<<blocks, 256, 0, s>>>(a);
+    static int prio = [] {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        return greatest;
+    }();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(GM_BONDED_THREADS);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = prio;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (a.bonded_mi) cudaLaunchKernelEx(&cfg, bonded_pair14_kernel<true>, a);
+    else cudaLaunchKernelEx(&cfg, bonded_pair14_kernel<false>, a);
 }
 
 void gm_launch_pair14(const ForceArgs &a, bool, cudaStream_t s) {
     if (a.blocks14 == 0) return;
-    if (a.bonded_mi) pair14_kernel<true><<<a.blocks14, 256, 0, s>>>(a);
-    else pair14_kernel<false><<<a.blocks14, 256, 0, s>>>(a);
+    if (a.bonded_mi) pair14_kernel<true><<<a.blocks14, GM_BONDED_THREADS, 0, s>>>(a);
+    else pair14_kernel<false><<<a.blocks14, GM_BONDED_THREADS, 0, s>>>(a);
 }
 
 void gm_launch_energy(const ForceArgs &a, cudaStream_t s) {

@@ -40,6 +40,8 @@
 // the block then concatenates the segments, layer by layer, into each lane's
 // list column.
 #define GM_NSEG 5
+// Threads per block of the bonded and 1-4 kernels.
+#define GM_BONDED_THREADS 64
 // List columns are ordered by build-time distance in GM_NBUCKET buckets; the
 // build stages a slot index with its bucket in the top bits.
 #define GM_NBUCKET 4
@@ -268,6 +270,7 @@ struct ForceArgs {
     // scaled 1-4 pairs
     int n14; const int *p14_i, *p14_j; double scale14_lj, scale14_coul;
     const double *sigma, *epsilon, *charge64;
+    const double4 *p14par;   // per 1-4 pair: (sigma_ij, 4 eps_ij s_lj, 24 eps_ij s_lj, k_C q_i q_j s_coul)
     double *epart14; int blocks14;
     double *energy;          // total
     int n_epart_total;       // n_groups * split + bonded_blocks + blocks14 entries
@@ -308,8 +311,12 @@ struct ClusterArgs {
 };
 
 // d taken to the nearest periodic image of a box of length L: the reference's
-// min_image, d - L * round(d / L) with round half away from zero
-__device__ __forceinline__ double gm_min_image(double d, double L) { return d - L * round(d / L); }
+// min_image, d - L * round(d / L) with round half away from zero; each
+// operation rounded on its own (never contracted into an FMA, whatever the
+// translation unit's -fmad setting), so the bits are the reference's
+__device__ __forceinline__ double gm_min_image(double d, double L) {
+    return __dsub_rn(d, __dmul_rn(L, round(__ddiv_rn(d, L))));
+}
 
 void gm_launch_half_kick(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                          const DevStatus *st, cudaStream_t s);

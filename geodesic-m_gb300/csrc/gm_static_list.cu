@@ -194,10 +194,13 @@ __global__ void scan_rows_kernel(int n, Scratch *S) {
 }
 
 // Writes row i at row_start[i], kept ascending in j by insertion as it is
-// filled.  Nothing is written when the total exceeds the caller's capacity.
+// filled.  Nothing is written when the total exceeds the caller's capacity,
+// nor after an earlier launch of the build raised an error (non-finite
+// positions, an extent or cell overflow), so an error return leaves the
+// caller's pair buffers untouched.
 __global__ void emit_rows_kernel(PairTest t, uint32_t *pair_i, uint32_t *pair_j, long long max_pairs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= t.n || (long long)t.S->row_start[t.n] > max_pairs) return;
+    if (i >= t.n || t.S->status.error || (long long)t.S->row_start[t.n] > max_pairs) return;
     const int base = t.S->row_start[i];
     int k = 0;
     for_each_partner(t, i, [&](int j) {
@@ -213,6 +216,24 @@ __global__ void emit_rows_kernel(PairTest t, uint32_t *pair_i, uint32_t *pair_j,
 }
 
 bool positive_finite(double v) { return std::isfinite(v) && v > 0.0; }
+
+// Makes `device` current for the call and gives the caller back the device
+// it had current, on every return path.
+struct CurrentDevice {
+    int prev = -1;
+    bool changed = false;
+    cudaError_t enter(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev == device) return cudaSuccess;
+        e = cudaSetDevice(device);
+        changed = e == cudaSuccess;
+        return e;
+    }
+    ~CurrentDevice() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -235,7 +256,8 @@ extern "C" int32_t gm_build_pairs_static(double *d_pos, int32_t n_atoms, const i
     if (params->device < 0 || params->device >= kMaxDevices) return GM_ERR_INVALID_ARGUMENT;
     if (n_atoms == 0) return GM_OK;
     if (!d_pos) return GM_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(params->device) != cudaSuccess) return GM_ERR_NO_DEVICE;
+    CurrentDevice current;
+    if (current.enter(params->device) != cudaSuccess) return GM_ERR_NO_DEVICE;
     Scratch *S = nullptr;
     int rc = scratch_for(params->device, &S);
     if (rc) return rc;

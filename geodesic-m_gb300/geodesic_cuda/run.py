@@ -164,21 +164,16 @@ def run(config: Config, base: str = "", make_backend=None):
         be.close()
 
 
-def _wrap_into_box(pos, box) -> None:
-    """neighbor.rs:78-88: x - L * floor(x / L) per coordinate, in place."""
-    for d in range(3):
-        pos[d] -= box[d] * np.floor(pos[d] / box[d])
-
-
 def _initial_state(config: Config, be, pos, vel):
     """lib.rs:261-282: the first list build (which wraps a periodic system
-    into the box), the velocity projection on those positions, then the
-    resident state's forces and energies.  The wrap is done here, on the
-    host, so that frame 0 and the projection see the wrapped positions as in
-    the reference; the device's own wrap at its first build then changes
-    nothing (a coordinate in [0, L) wraps to itself)."""
-    if config.periodic:
-        _wrap_into_box(pos, config.box_size)
+    into the box, neighbor.rs:10-16), the velocity projection on those
+    positions, then the resident state's forces and energies.  The first
+    build is the backend's own list build on the host arrays, so the wrap
+    runs once, on the device, as the reference runs it once; frame 0 and the
+    projection see the wrapped positions, and the resident forces use the
+    list that build made (the uploaded positions are its own, so nothing is
+    wrapped twice)."""
+    be.build_neighbor_list(pos)
     be.constrain_velocities(pos, vel, 0)
     be.upload_state(pos, vel)
     be.forces_resident()

@@ -238,13 +238,13 @@ int32_t gm_frames_take(gm_ctx *ctx, int64_t max_frames, float *xyz, uint64_t *st
 
 /* ---- autotuner (no reference counterpart) ------------------------------
  *
- * Times the FP32 pair kernel on the current list (reps launches per
- * candidate, CUDA events on the context's stream) over warps per 32-atom
- * group (1-16: list columns per warp), warps per block (2, 4, 8) and grid
- * (one work item per warp, or a persistent grid of 2-16 blocks per SM), and
- * keeps the fastest.  Every candidate computes the same bits (fixed 32-entry
- * FP32 chunks folded into int64 sums).  choice (nullable): split, warps per
- * block, grid (0 = one item per warp). */
+ * Times the context's pair kernel (mixed or FP64) on the current list
+ * (reps launches per candidate, CUDA events on the context's stream) over
+ * warps per 32-atom group (1-16: list columns per warp), warps per block (2,
+ * 4, 8) and grid (one work item per warp, or a persistent grid of 2-16
+ * blocks per SM), and keeps the fastest.  Every candidate computes the same
+ * bits (fixed 32-entry chunks folded into int64 sums).  choice (nullable):
+ * split, warps per block, grid (0 = one item per warp). */
 int32_t gm_autotune(gm_ctx *ctx, int32_t reps, int64_t *choice);
 
 /* ---- constraint warm start (no reference counterpart) ------------------
@@ -307,8 +307,9 @@ int32_t gm_ws_last(gm_ctx *ctx, float *feat, double *lam0, double *lam_sum);
  * device memory is held by its own pool, or a step running beside other
  * streams, where cudaFree waits for the whole device.
  *
- * All pointers but params and n_pairs are DEVICE pointers on params->device
- * (made current).  d_pos: x|y|z rows of n_atoms doubles, wrapped into the
+ * All pointers but params and n_pairs are DEVICE pointers on params->device,
+ * which is current during the call; the caller's current device is restored
+ * before it returns.  d_pos: x|y|z rows of n_atoms doubles, wrapped into the
  * box in place when periodic (as gm_build_list does).  d_excl_start
  * (n_atoms + 1) / d_excl: exclusions as CSR, both directions, each row
  * ascending (both NULL for none).  The pairs (i < j, |r_ij| <= r_skin by the
@@ -316,7 +317,8 @@ int32_t gm_ws_last(gm_ctx *ctx, float *feat, double *lam0, double *lam_sum);
  * sorted by (i, then j): the same list gm_get_pairs returns.  *n_pairs
  * (host) receives the count; with d_pair_i == NULL only the count is
  * computed.  If the count exceeds max_pairs nothing is written and
- * GM_ERR_LIST_OVERFLOW is returned.  n_atoms > GM_STATIC_MAX_ATOMS returns
+ * GM_ERR_LIST_OVERFLOW is returned; after any other error return the pair
+ * buffers are untouched as well.  n_atoms > GM_STATIC_MAX_ATOMS returns
  * GM_ERR_UNSUPPORTED before any device call.  Runs on `stream` (a
  * cudaStream_t; NULL = the default stream) and returns after it finished.
  *

@@ -73,10 +73,10 @@ static void wrap_into_box(int64_t n, double *px, double *py, double *pz, const d
 
 /* ------------------------------------------------------- neighbour list */
 
-int64_t or_neighbor_build(int64_t n, double *px, double *py, double *pz, const or_params *p,
-                          const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
-    /* neighbor.rs:13-15 */
-    if (p->periodic) wrap_into_box(n, px, py, pz, p->box);
+/* The pairs of neighbor.rs:25-43 over the (already wrapped) positions, all
+ * i < j; at most cap are stored, the count is returned. */
+static int64_t pairs_all(int64_t n, const double *px, const double *py, const double *pz, const or_params *p,
+                         const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
     int64_t nk;
     uint64_t *keys = exclusion_keys(t, &nk);
     /* neighbor.rs:25 */
@@ -106,9 +106,9 @@ static int cmp_u32(const void *a, const void *b) {
     return (x > y) - (x < y);
 }
 
-int64_t or_neighbor_build_cells(int64_t n, double *px, double *py, double *pz, const or_params *p,
-                                const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
-    if (p->periodic) wrap_into_box(n, px, py, pz, p->box);
+/* The same pairs found through a cell grid (same set, same order). */
+static int64_t pairs_cells(int64_t n, const double *px, const double *py, const double *pz, const or_params *p,
+                           const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
     int64_t nk;
     uint64_t *keys = exclusion_keys(t, &nk);
     const double r_skin_sq = p->r_skin * p->r_skin;
@@ -197,6 +197,29 @@ int64_t or_neighbor_build_cells(int64_t n, double *px, double *py, double *pz, c
     }
     free(buf); free(members); free(cursor); free(cellof); free(cstart); free(keys);
     return count;
+}
+
+/* neighbor::build (neighbor.rs:8-55): wraps a periodic system into the box
+ * once (neighbor.rs:13-15), then lists the pairs.  A caller that only learns
+ * the count from this call fetches the pairs with or_neighbor_pairs, which
+ * does not wrap again (a coordinate that the wrap put exactly on L would turn
+ * into 0 on a second one, which the reference never does). */
+int64_t or_neighbor_build(int64_t n, double *px, double *py, double *pz, const or_params *p,
+                          const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
+    if (p->periodic) wrap_into_box(n, px, py, pz, p->box);
+    return pairs_all(n, px, py, pz, p, t, cap, pair_i, pair_j);
+}
+
+int64_t or_neighbor_build_cells(int64_t n, double *px, double *py, double *pz, const or_params *p,
+                                const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j) {
+    if (p->periodic) wrap_into_box(n, px, py, pz, p->box);
+    return pairs_cells(n, px, py, pz, p, t, cap, pair_i, pair_j);
+}
+
+int64_t or_neighbor_pairs(int64_t n, const double *px, const double *py, const double *pz, const or_params *p,
+                          const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j, int32_t cells) {
+    return cells ? pairs_cells(n, px, py, pz, p, t, cap, pair_i, pair_j)
+                 : pairs_all(n, px, py, pz, p, t, cap, pair_i, pair_j);
 }
 
 int32_t or_needs_rebuild(int64_t n, const double *px, const double *py, const double *pz,
@@ -771,13 +794,15 @@ int32_t or_backend_n_threads(const or_backend *b) { return b->n_threads; }
 int64_t or_backend_build_neighbor_list(or_backend *b, double *px, double *py, double *pz) {
     /* cpu_backend.rs:88-90 -> neighbor::build */
     int64_t n = b->atoms.n;
+    int64_t cnt = or_neighbor_build(n, px, py, pz, &b->params, &b->topo, b->cap, b->pair_i, b->pair_j);
     for (;;) {
-        int64_t cnt = or_neighbor_build(n, px, py, pz, &b->params, &b->topo, b->cap, b->pair_i, b->pair_j);
         if (cnt <= b->cap) { b->n_pairs = cnt; break; }
         free(b->pair_i); free(b->pair_j);
         b->cap = cnt + cnt / 8 + 16;
         b->pair_i = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)b->cap);
         b->pair_j = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)b->cap);
+        /* the positions are wrapped already: fetch the pairs only */
+        cnt = or_neighbor_pairs(n, px, py, pz, &b->params, &b->topo, b->cap, b->pair_i, b->pair_j, 0);
     }
     memcpy(b->ref, px, sizeof(double) * (size_t)n);
     memcpy(b->ref + n, py, sizeof(double) * (size_t)n);

@@ -78,6 +78,10 @@ int64_t or_neighbor_build(int64_t n, double *px, double *py, double *pz, const o
  * large N; it is validated against or_neighbor_build in the tests. */
 int64_t or_neighbor_build_cells(int64_t n, double *px, double *py, double *pz, const or_params *p,
                                 const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j);
+/* The pairs of already wrapped positions (no wrap): the fill call after a
+ * counting or_neighbor_build / or_neighbor_build_cells (cells != 0). */
+int64_t or_neighbor_pairs(int64_t n, const double *px, const double *py, const double *pz, const or_params *p,
+                          const or_topology *t, int64_t cap, uint32_t *pair_i, uint32_t *pair_j, int32_t cells);
 
 /* neighbor.rs:60-72 */
 int32_t or_needs_rebuild(int64_t n, const double *px, const double *py, const double *pz,

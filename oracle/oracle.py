@@ -75,6 +75,8 @@ def lib():
         L.or_neighbor_build.argtypes = [C.c_int64, _f64p, _f64p, _f64p, P(OrParams), P(OrTopology), C.c_int64, _u32p, _u32p]
         L.or_neighbor_build_cells.restype = C.c_int64
         L.or_neighbor_build_cells.argtypes = L.or_neighbor_build.argtypes
+        L.or_neighbor_pairs.restype = C.c_int64
+        L.or_neighbor_pairs.argtypes = L.or_neighbor_build.argtypes + [C.c_int32]
         L.or_needs_rebuild.restype = C.c_int32
         L.or_needs_rebuild.argtypes = [C.c_int64] + [_f64p] * 6 + [C.c_double, C.c_double]
         for name in ("or_pair_forces", "or_coulomb_forces"):
@@ -220,7 +222,9 @@ def neighbor_build(pos, atoms, topo, params, cells=False):
     cnt = fn(n, px, py, pz, C.byref(params), C.byref(arr.topo), 0, None, None)
     pi = np.zeros(max(cnt, 1), np.uint32)
     pj = np.zeros(max(cnt, 1), np.uint32)
-    cnt2 = fn(n, px, py, pz, C.byref(params), C.byref(arr.topo), cnt, _p(pi, C.c_uint32), _p(pj, C.c_uint32))
+    # the positions are wrapped now: the fill call does not wrap again
+    cnt2 = L.or_neighbor_pairs(n, px, py, pz, C.byref(params), C.byref(arr.topo), cnt, _p(pi, C.c_uint32),
+                               _p(pj, C.c_uint32), int(cells))
     assert cnt2 == cnt
     return pi[:cnt].copy(), pj[:cnt].copy()
 

@@ -25,6 +25,7 @@ class OracleResident:
         self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
         self.n, self.n_sys = int(self.offsets[-1]), len(sizes)
         self.pos = self.vel = self.force = None
+        self.built = False  # a list build on the host arrays that the resident forces reuse
         self.e_pot = np.zeros(self.n_sys)
         self.fi, self.cap, self.ring, self.lost = 0, 0, [], 0
         self.calls = []
@@ -34,6 +35,17 @@ class OracleResident:
         return slice(int(self.offsets[k]), int(self.offsets[k + 1]))
 
     # ------------------------------------------------------------ state
+    def build_neighbor_list(self, pos):
+        """The trait's list build on host arrays (wraps a periodic system in
+        place); the next forces_resident reuses these lists."""
+        self.calls.append("build_neighbor_list")
+        for k, (_, _, b) in enumerate(self.systems):
+            sl = self._sl(k)
+            p = np.ascontiguousarray(pos[:, sl])
+            b.build_neighbor_list(p)
+            pos[:, sl] = p
+        self.built = True
+
     def constrain_velocities(self, pos, vel, step=0):
         self.calls.append("constrain_velocities")
         for k, (a, t, _) in enumerate(self.systems):
@@ -58,9 +70,11 @@ class OracleResident:
         self.calls.append("forces_resident")
         self.force = []
         for k, (_, _, b) in enumerate(self.systems):
-            b.build_neighbor_list(self.pos[k])
+            if not self.built:
+                b.build_neighbor_list(self.pos[k])
             self.force.append(b.compute_forces(self.pos[k]))
             self.e_pot[k] = b.potential_energy
+        self.built = False
 
     def _kinetic(self):
         return np.array([oracle.kinetic_energy(self.vel[k], a.mass) for k, (a, _, _) in enumerate(self.systems)])

@@ -1,0 +1,83 @@
+"""Device error paths, provoked from the host with valid inputs (needs a GPU).
+
+Neither test faults, traps or hangs the device: the kernels record the
+condition in the status word, finish their launches, and the host turns the
+word into an error code.
+
+* A neighbour list that outgrows its capacity inside a resident run: a
+  resident run cannot grow the list, so the in-graph rebuild stores at most
+  `cap` entries per atom (writes stay inside the buffer), sets the overflow
+  bit, and the call returns GM_ERR_LIST_OVERFLOW.  The reference grows its
+  Vec instead; the code maps to BackendError (geodesic-core/src/error.rs:
+  SimError::Backend).  The context stays usable: the next host-side build
+  regrows the list.
+* A pair force beyond the fixed-point range (|F| >= 2^22 kcal/mol/A): the
+  force evaluation returns GM_ERR_FIXED_POINT_OVERFLOW and, since the trait's
+  compute_forces is infallible, hands back NaN forces, which the run loop's
+  check_forces_finite turns into NumericalError::NanInForce
+  (geodesic/src/lib.rs:79-92, geodesic-core/src/error.rs:34-38).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from geodesic_cuda import amber, backend
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0)
+
+
+def inert_gas(n, density, seed):
+    """n atoms without LJ parameters or charges (no forces at all) spread
+    uniformly over a ball of the given number density, centred at 5000 A."""
+    rng = np.random.default_rng(seed)
+    radius = (3.0 * n / (4.0 * np.pi * density)) ** (1.0 / 3.0)
+    d = rng.normal(size=(3, n))
+    d *= radius * rng.uniform(0.0, 1.0, n) ** (1.0 / 3.0) / np.linalg.norm(d, axis=0)
+    atoms = amber.AtomData(np.zeros(n), np.zeros(n), np.full(n, 12.0), np.zeros(n), np.full(n, 5, np.uint8),
+                           np.zeros(n, np.uint32), ["C   "] * n)
+    return atoms, np.ascontiguousarray(d + 5000.0)
+
+
+@pytest.mark.parametrize("precision", [backend.PRECISION_MIXED, backend.PRECISION_FP64])
+def test_list_overflow_inside_a_resident_run(precision):
+    n, steps, dt = 1500, 200, 0.002
+    atoms, pos = inert_gas(n, 0.0125, seed=4)
+    # every atom drifts straight to the centre: after `steps` steps the ball
+    # has shrunk to 40 % of its radius, 15.6 times the density it was sized for
+    centre = pos.mean(axis=1, keepdims=True)
+    vel = np.ascontiguousarray(-(pos - centre) * (0.6 / (steps * dt)))
+    be = backend.CudaBackend(atoms, amber.BondedTopology.empty(), backend.SimParams(precision=precision, **PARAMS))
+    with pytest.raises(backend.BackendError) as e:
+        be.steps(pos, vel, dt, steps)
+    assert e.value.status == 7, e.value  # GM_ERR_LIST_OVERFLOW
+    # the context is still usable: a host-side build regrows the list and
+    # finds the oracle's pairs at the compressed positions
+    p2 = np.ascontiguousarray(centre + (pos - centre) * 0.4)
+    be.build_neighbor_list(p2)
+    gi, gj = be.pairs()
+    op = oracle.make_params(box=PARAMS["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0)
+    ri, rj = oracle.neighbor_build(p2.copy(), atoms, amber.BondedTopology.empty(), op, cells=True)
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj)
+    be.close()
+
+
+@pytest.mark.parametrize("precision", [backend.PRECISION_MIXED, backend.PRECISION_FP64])
+def test_fixed_point_overflow_gives_nan_forces(precision):
+    # sigma 3 A, epsilon 0.2 kcal/mol, 0.2 A apart: |F| ~ 1e15 kcal/mol/A
+    atoms = amber.AtomData(np.full(2, 3.0), np.full(2, 0.2), np.full(2, 12.0), np.zeros(2), np.full(2, 5, np.uint8),
+                           np.zeros(2, np.uint32), ["C   "] * 2)
+    pos = np.ascontiguousarray([[5000.0, 5000.2], [5000.0, 5000.0], [5000.0, 5000.0]])
+    be = backend.CudaBackend(atoms, amber.BondedTopology.empty(), backend.SimParams(precision=precision, **PARAMS))
+    be.build_neighbor_list(pos)
+    with pytest.raises(backend.BackendError) as e:
+        be.compute_forces(pos)
+    assert e.value.status == 9, e.value  # GM_ERR_FIXED_POINT_OVERFLOW
+    assert np.all(np.isnan(be.reduce_forces()))
+    # a sane geometry afterwards evaluates normally
+    ok = np.ascontiguousarray([[5000.0, 5003.5], [5000.0, 5000.0], [5000.0, 5000.0]])
+    be.build_neighbor_list(ok)
+    f = be.compute_forces(ok)
+    assert np.all(np.isfinite(f)) and f[0, 0] == -f[0, 1]
+    be.close()

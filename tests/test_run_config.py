@@ -360,7 +360,8 @@ def test_projection_comes_first_and_frames_drain_in_batches(tmp_path):
 
     run.run_from_config_file(cfg, make_backend=make)
     be = made[0]
-    assert be.calls[:4] == [("frames_enable", 5, 3), "constrain_velocities", "upload_state", "forces_resident"]
+    assert be.calls[:5] == [("frames_enable", 5, 3), "build_neighbor_list", "constrain_velocities", "upload_state",
+                            "forces_resident"]
     runs = [c for c in be.calls if isinstance(c, tuple) and c[0] == "run_resident"]
     assert runs == [("run_resident", 15, 0), ("run_resident", 15, 15), ("run_resident", 10, 30)]
     assert be.closed
@@ -444,6 +445,40 @@ def test_periodic_run_wraps_before_frame_zero(tmp_path, centre, min_image):
     assert np.array_equal(dcd.view(np.uint32), frames.view(np.uint32))
     assert np.all((dcd[0] >= 0.0) & (dcd[0] < 60.0))  # frame 0 is already in the box
     assert (tmp_path / "energy.csv").read_text() == expected_csv(tmp_path, n, 5, pot, kin)
+
+
+def test_periodic_run_wraps_once():
+    """A coordinate just below 0 (-1e-17) wraps to exactly the box length L
+    (L - 1e-17 rounds to L); a second wrap would turn it into 0.  The run's
+    initial state wraps once, as the reference's first list build does
+    (lib.rs:261-282, neighbor.rs:10-16): the positions for frame 0 and the
+    projection hold L, and the resident state keeps them.  (An inpcrd file
+    cannot hold such a value, its fields have 7 decimals, so the state is
+    given directly.)"""
+    atoms, topo, state, _ = synth.generate(250, seed=55, h_fraction=0.3, temperature=300.0, relax_iters=200)
+    pos = state.pos - state.pos.mean(axis=1, keepdims=True) + 30.0
+    k = int(np.argmin(pos[0]))
+    pos[0, k] = -1e-17
+    pos = np.ascontiguousarray(pos)
+    vel = np.ascontiguousarray(state.vel.copy())
+    params = backend_params(box_size=(60.0,) * 3, periodic=True)
+    be = oracle_resident.make([atoms], [topo], params)
+    run._initial_state(None, be, pos, vel)
+    assert pos[0, k] == 60.0
+    ref = np.ascontiguousarray(state.pos - state.pos.mean(axis=1, keepdims=True) + 30.0)
+    ref[0, k] = -1e-17
+    oracle.CpuBackend(atoms, topo, be.p).build_neighbor_list(ref)
+    assert np.array_equal(pos, ref)
+    p2, v2 = np.zeros_like(pos), np.zeros_like(vel)
+    be.download_state(p2, v2)
+    assert np.array_equal(p2, ref)
+
+
+def backend_params(**kw):
+    from geodesic_cuda import backend
+    base = dict(r_cutoff=10.0, r_skin=11.0, r_switch=8.0, max_constr_iter=100, constr_tol=1e-8)
+    base.update(kw)
+    return backend.SimParams(**base)
 
 
 def test_periodic_batch_wraps_every_system(tmp_path):

@@ -4,8 +4,10 @@ context's list build (gm_build_list + gm_get_pairs) through the C ABI.
 Pair lists are integer data, so the tolerance is exact equality: the same
 pairs in the same order (i, then j), and the same wrapped positions.  Each
 case calls the static build twice in a row on the same buffers, so leftovers
-in its scratch would show up on the second call.  The module name sorts last
-so that, in a full run, it also runs after every other GPU test.
+in its scratch would show up on the second call, and checks that a warm call
+leaves the device's free memory unchanged (it allocates nothing) and gives
+back the caller's current device.  The module name sorts last so that, in a
+full run, it also runs after every other GPU test.
 """
 import ctypes as C
 
@@ -117,6 +119,29 @@ def test_static_build_matches_context_build(case):
         assert np.all(gi[total:] == np.uint32(0xFFFFFFFF)), call  # nothing past the count
         # positions wrapped in place exactly as the context's build wraps them
         assert np.array_equal(d_pos.cpu().numpy(), pos_ctx), call
+
+    # a warm call allocates nothing: the device's free memory is the same
+    # before and after it (no tensor is created in between)
+    torch.cuda.synchronize(dev)
+    cur = torch.cuda.current_device()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    got = backend.build_pairs_static(d_pos.data_ptr(), n, es_ptr, ex_ptr, p, d_i.data_ptr(), d_j.data_ptr(),
+                                     total + 64, stream)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert got == total and free1 == free0, (free0, free1)
+    assert torch.cuda.current_device() == cur
+
+    # a non-finite position: an error, and the pair buffers untouched
+    d_i.fill_(-1)
+    d_j.fill_(-1)
+    bad = d_pos.clone()
+    bad[0, n // 2] = float("nan")
+    with pytest.raises(backend.BackendError) as e:
+        backend.build_pairs_static(bad.data_ptr(), n, es_ptr, ex_ptr, p, d_i.data_ptr(), d_j.data_ptr(),
+                                   total + 64, stream)
+    assert e.value.status == 6  # GM_ERR_NONFINITE
+    torch.cuda.synchronize(dev)
+    assert np.all(d_i.cpu().numpy() == -1) and np.all(d_j.cpu().numpy() == -1)
 
     # a capacity one short: nothing written, the count reported
     d_i.fill_(-1)
