@@ -2193,6 +2193,17 @@ int32_t gm_ensemble_energies(gm_ctx *c, double *e_pot, double *e_kin) {
 
 /* ---- autotuner ---------------------------------------------------------- */
 
+int32_t gm_pair_shape(gm_ctx *c, int32_t split, int32_t warps_per_block, int32_t grid) {
+    if (!c || split < 1 || split > GM_MAX_SPLIT || grid < 0 ||
+        (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8))
+        return GM_ERR_INVALID_ARGUMENT;
+    c->split = split;
+    c->pair_warps = warps_per_block;
+    c->pair_grid = grid;
+    drop_graph(c);  // the captured step holds the old launch shape
+    return GM_OK;
+}
+
 int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
     if (!c || reps < 1) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));

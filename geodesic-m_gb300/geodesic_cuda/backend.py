@@ -164,6 +164,7 @@ def lib():
         L.gm_ensemble_info.argtypes = [C.c_void_p, P(C.c_int64)]
         L.gm_ensemble_energies.argtypes = [C.c_void_p, _f64p, _f64p]
         L.gm_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int64)]
+        L.gm_pair_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
         L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
         L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
         L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
@@ -285,11 +286,16 @@ class CudaBackend:
         self._steps_out = None  # reused gm_steps out-parameters
 
     def autotune(self, reps=5):
-        """Pick the FP32 pair kernel's split, block size and grid by timing
+        """Pick the pair kernel's split, block size and grid by timing
         (gm_autotune); returns them."""
         out = (C.c_int64 * 3)()
         self._check(lib().gm_autotune(self._h, int(reps), out))
         return dict(split=out[0], warps_per_block=out[1], grid=out[2])
+
+    def pair_shape(self, split, warps_per_block, grid=0):
+        """Sets the pair kernel's launch shape (gm_pair_shape), e.g. a cached
+        autotune() result."""
+        self._check(lib().gm_pair_shape(self._h, int(split), int(warps_per_block), int(grid)))
 
     def ensemble_energies(self):
         """Per-system (potential, kinetic) energies (gm_ensemble_energies)."""

@@ -246,6 +246,11 @@ int32_t gm_frames_take(gm_ctx *ctx, int64_t max_frames, float *xyz, uint64_t *st
  * bits (fixed 32-entry chunks folded into int64 sums).  choice (nullable):
  * split, warps per block, grid (0 = one item per warp). */
 int32_t gm_autotune(gm_ctx *ctx, int32_t reps, int64_t *choice);
+/* Sets the pair kernel's launch shape directly (a choice gm_autotune returned
+ * earlier, e.g. cached across runs): split 1-16, warps per block 2, 4 or 8,
+ * grid 0 (one work item per warp) or a block count.  The forces are the same
+ * bits for every shape. */
+int32_t gm_pair_shape(gm_ctx *ctx, int32_t split, int32_t warps_per_block, int32_t grid);
 
 /* ---- constraint warm start (no reference counterpart) ------------------
  *

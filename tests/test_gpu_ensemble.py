@@ -12,10 +12,20 @@ system's own run bit for bit:
   number of list rebuilds as the single runs together.
 With constraints the batch's SHAKE/RATTLE stop at the batch's largest
 iteration count; every solve still meets the tolerance.
+
+Against the oracle (the reference's one-system run, geodesic/src/lib.rs:
+187-345, restated): each member's forces (1e-10 * max(|F|, 1) per component
+in FP64, 1e-5 mixed) and its positions after 20 resident steps, within
+1e-9 A (FP64) or 1e-5 A (mixed).  With constraints a member iterates SHAKE /
+RATTLE to the batch's largest count where the oracle stops at its own
+(geodesic-engine/src/constraint.rs:62-152, 170-259): the extra iterations
+move atoms by less than the 1e-10 tolerance each step, so the FP64 bound is
+1e-8 A there.
 """
 import numpy as np
 import pytest
 
+import oracle
 from geodesic_cuda import amber, backend, synth
 
 pytestmark = pytest.mark.gpu
@@ -127,3 +137,49 @@ def test_autotuner_keeps_forces_bit_identical():
         assert 1 <= choice["split"] <= 16 and choice["warps_per_block"] in (2, 4, 8) and choice["grid"] >= 0
         f1 = be.compute_forces(pos).copy()
         assert np.array_equal(f0, f1)
+
+
+def oracle_params(p: backend.SimParams):
+    return oracle.make_params(box=p.box_size, periodic=p.periodic, r_cutoff=p.r_cutoff, r_skin=p.r_skin,
+                              r_switch=p.r_switch, max_constr_iter=p.max_constr_iter, constr_tol=p.constr_tol,
+                              n_threads=1, coulomb=p.coulomb, scale14_lj=p.scale14_lj, scale14_coul=p.scale14_coul)
+
+
+@pytest.mark.parametrize("constrained", [False, True])
+@pytest.mark.parametrize("precision", [backend.PRECISION_MIXED, backend.PRECISION_FP64])
+def test_batch_members_follow_the_oracle(precision, constrained):
+    syss = systems(h_fraction=0.4 if constrained else 0.0)
+    p = backend.SimParams(precision=precision, max_constr_iter=200, constr_tol=1e-10, **PHYS)
+    op = oracle_params(p)
+    fp64 = precision == backend.PRECISION_FP64
+    batch = backend.CudaBackend.ensemble([s[0] for s in syss], [s[1] for s in syss], p)
+    off = batch.offsets
+    pos, vel = concat([s[2].pos for s in syss]), concat([s[2].vel for s in syss])
+    # forces of every member at the starting positions
+    pf = pos.copy()
+    batch.build_neighbor_list(pf)
+    f = batch.compute_forces(pf).copy()
+    ftol = 1e-10 if fp64 else 1e-5
+    for k, (atoms, topo, state) in enumerate(syss):
+        ob = oracle.CpuBackend(atoms, topo, op)
+        pr = np.ascontiguousarray(state.pos.copy())
+        ob.build_neighbor_list(pr)
+        fr = ob.compute_forces(pr)
+        fk = f[:, off[k]:off[k + 1]]
+        assert np.all(np.abs(fk - fr) <= ftol * np.maximum(np.abs(fr), 1.0)), (k, np.abs(fk - fr).max())
+    # 20 resident steps at 2 fs after the run loop's initial velocity
+    # projection (lib.rs:270-282), against oracle.run per member
+    batch.constrain_velocities(pos, vel, 0)
+    batch.upload_state(pos, vel)
+    batch.forces_resident()
+    batch.run_resident(0.002, 20)
+    batch.synchronize()
+    pb, vb = np.zeros_like(pos), np.zeros_like(vel)
+    batch.download_state(pb, vb)
+    tol = (1e-8 if constrained else 1e-9) if fp64 else 1e-5
+    for k, (atoms, topo, state) in enumerate(syss):
+        po, vo = np.ascontiguousarray(state.pos.copy()), np.ascontiguousarray(state.vel.copy())
+        oracle.run(atoms, topo, op, po, vo, 0.002, 20, 20)
+        err = np.abs(pb[:, off[k]:off[k + 1]] - po).max()
+        assert err < tol, (k, err)
+    batch.close()
