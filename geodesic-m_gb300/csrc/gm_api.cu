@@ -1777,13 +1777,10 @@ int32_t gm_download_state(gm_ctx *c, double *px, double *py, double *pz, double 
 int32_t gm_forces_resident(gm_ctx *c) {
     if (!c) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
-    if (!c->built) {
-        int rc = do_build(c);
-        if (rc) return rc;
-    }
-    c->launches += seq_forces(c, c->stream);
-    c->forces_current = true;
-    return GM_OK;
+    // the list is rebuilt first when the resident positions moved more than
+    // half the skin from its build (neighbor.rs:60-72), as in a step
+    c->forces_current = false;
+    return ensure_forces(c);
 }
 
 int32_t gm_run_resident(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps) {

@@ -167,7 +167,9 @@ int32_t gm_download_state(gm_ctx *ctx, double *px, double *py, double *pz, doubl
 /* Runs n_steps BAB steps on the resident state (asynchronous on the
  * context's stream; call gm_synchronize to collect errors). */
 int32_t gm_run_resident(gm_ctx *ctx, double dt, uint64_t first_step, int64_t n_steps);
-/* Evaluates forces on the resident positions only (asynchronous). */
+/* Evaluates forces on the resident positions; first rebuilds the list when
+ * an atom moved more than half the skin since the last build (the check is
+ * one host synchronisation; the force launches are asynchronous). */
 int32_t gm_forces_resident(gm_ctx *ctx);
 /* Waits for the stream and reports device-side errors. */
 int32_t gm_synchronize(gm_ctx *ctx, gm_convergence *err);
