@@ -176,7 +176,8 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     from geodesic_cuda import backend
     import oracle
 
-    p = backend.SimParams(precision=backend.PRECISION_MIXED, device=dev, **PHYS)
+    prec = backend.PRECISION_FP64 if args.precision == "fp64" else backend.PRECISION_MIXED
+    p = backend.SimParams(precision=prec, device=dev, **PHYS)
     be = backend.CudaBackend(atoms, topo, p)
     be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
     be.forces_resident()
@@ -203,7 +204,8 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     if args.quick:
         return {"metric": METRIC, "value": round(aggregate_ns_per_day(world, args.steps, sec), 3), "unit": "ns/day",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": round(1e3 * sec / args.steps, 5), "quick": True, "half_list_pairs": pairs,
+                "ms_per_step": round(1e3 * sec / args.steps, 5), "quick": True, "precision": args.precision,
+                "half_list_pairs": pairs,
                 "rebuilds": result["rebuilds"], "gpu_launches": int(result["launches"]),
                 "kernel_ms": {"pair": round(be.profile("pair", 3), 5), "rebuild": round(be.profile("rebuild", 2), 5)},
                 "autotuner": tuned}
@@ -660,6 +662,8 @@ def main():
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no error, CPU-baseline, FP64 or e2e legs); for profiler runs")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
+                    help="with --quick: the precision of the timed steps")
     ap.add_argument("--config", default="headline",
                     choices=["headline", "ensemble", "warm_start", "scale_1m", "small_5k"],
                     help="headline: 50k atoms (the default line); the others print their own line")
