@@ -136,7 +136,7 @@ static int64_t pairs_cells(int64_t n, const double *px, const double *py, const 
         if (!p->periodic && (hi[d] - lo[d]) >= 0.5 * p->box[d] - p->r_skin) {
             /* min-image may fold far pairs: fall back to the double loop */
             free(keys);
-            return or_neighbor_build(n, px, py, pz, p, t, cap, pair_i, pair_j);
+            return pairs_all(n, px, py, pz, p, t, cap, pair_i, pair_j);
         }
     }
     int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];
