@@ -181,7 +181,14 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     be = backend.CudaBackend(atoms, topo, p)
     be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
     be.forces_resident()
-    tuned = be.autotune(reps=3)  # pair kernel split / block size / grid, same bits for every choice
+    if args.pair_shape:
+        # a known launch shape instead of the autotuner (profiler runs, where
+        # the autotuner's timings are distorted); the same bits either way
+        sp, wb, gr = (int(x) for x in args.pair_shape.split(","))
+        be.pair_shape(sp, wb, gr)
+        tuned = {"split": sp, "warps_per_block": wb, "grid": gr, "set": "--pair-shape"}
+    else:
+        tuned = be.autotune(reps=3)  # pair kernel split / block size / grid, same bits for every choice
     be.run_resident(DT_PS, args.warmup)
     be.synchronize()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -664,6 +671,8 @@ def main():
                     help="timed steps only (no error, CPU-baseline, FP64 or e2e legs); for profiler runs")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="with --quick: the precision of the timed steps")
+    ap.add_argument("--pair-shape", default="",
+                    help="SPLIT,WARPS,GRID: the pair kernel's launch shape instead of the autotuner's choice")
     ap.add_argument("--config", default="headline",
                     choices=["headline", "ensemble", "warm_start", "scale_1m", "small_5k"],
                     help="headline: 50k atoms (the default line); the others print their own line")

@@ -102,7 +102,6 @@ struct gm_ctx {
     bool ws_on = false, ws_model = false;
     int ws_rec_stride = 0, ws_rec_cap = 0;
     int *d_atom_cstart = nullptr, *d_atom_cref = nullptr;
-    float4 *d_ws_unit = nullptr;
     float *d_ws_params = nullptr, *d_ws_norm = nullptr, *d_ws_m = nullptr, *d_ws_v = nullptr, *d_ws_feat = nullptr,
           *d_rec_feat = nullptr, *d_rec_t = nullptr, *d_ws_partial = nullptr, *d_ws_out = nullptr;
     double *d_ws_scale = nullptr, *d_ws_t1 = nullptr, *d_ws_lam0 = nullptr, *d_lam_sum = nullptr,
@@ -360,12 +359,8 @@ long long issue_shake(gm_ctx *c, cudaStream_t s, bool resident) {
         f.n_constr = c->n_constr; f.n_atoms = c->n;
         f.constr_i = c->d_ci; f.constr_j = c->d_cj; f.constr_dsq = c->d_cdsq; f.inv_mass = c->d_inv_mass;
         f.atom_cstart = c->d_atom_cstart; f.atom_cref = c->d_atom_cref; f.pos = c->d_pos; f.dref = c->d_dref;
-        f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1; f.unit = c->d_ws_unit;
-        gm_launch_ws_features(f, s); k += 2;
-    }
-    if (c->ws_on) {
-        gm_launch_ws_infer(c->n_constr, c->d_ws_feat, c->d_ws_params, c->d_ws_norm, c->d_ws_scale, c->d_ws_t1,
-                           c->d_ws_lam0, nullptr, s);
+        f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1;
+        gm_launch_ws_predict(f, c->d_ws_params, c->d_ws_norm, c->d_ws_lam0, c->ws_on, s);
         k++;
     }
     k += gm_launch_shake_solve(a, c->n, c->d_pos, s);
@@ -1359,7 +1354,6 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         TRY(dalloc(c, &c->d_ws_scale, (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_ws_t1, (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_ws_feat, (size_t)GM_WS_IN * c->n_constr));
-        TRY(dalloc(c, &c->d_ws_unit, (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_rvec, 3 * (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_cl_iters, (size_t)c->n_clusters));
         TRY(dalloc(c, &c->d_cl_worst, (size_t)c->n_clusters));
@@ -2014,15 +2008,11 @@ int32_t gm_ws_forward(gm_ctx *c, const float *x, int64_t m, float *y) {
     if (!c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model");
     if (!m) return GM_OK;
     GM_CUDA(c, cudaSetDevice(c->device));
-    float *dx = nullptr, *dy = nullptr, *dn = nullptr;
-    std::vector<float> ident(GM_WS_NNORM, 0.0f);
-    for (int f = 0; f < GM_WS_IN; f++) ident[(size_t)(GM_WS_IN + f)] = 1.0f;
-    ident[25] = 1.0f;
+    float *dx = nullptr, *dy = nullptr;
     int rc = dupload(c, &dx, x, (size_t)m * GM_WS_IN);
     if (!rc) rc = dalloc(c, &dy, (size_t)m);
-    if (!rc) rc = dupload(c, &dn, ident.data(), ident.size());
     if (!rc) {
-        gm_launch_ws_infer((int)m, dx, c->d_ws_params, dn, nullptr, nullptr, nullptr, dy, c->stream);
+        gm_launch_ws_forward((int)m, dx, c->d_ws_params, dy, c->stream);
         c->launches++;
         cudaError_t e = cudaMemcpyAsync(y, dy, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -2030,7 +2020,6 @@ int32_t gm_ws_forward(gm_ctx *c, const float *x, int64_t m, float *y) {
     }
     dfree(c, dx);
     dfree(c, dy);
-    dfree(c, dn);
     return rc;
 }
 

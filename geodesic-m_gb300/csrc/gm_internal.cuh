@@ -420,12 +420,14 @@ struct WsFeatureArgs {
     float *feat;                 // [n_constr][12] raw features
     double *scale;               // 2 (1/m_i + 1/m_j) per constraint
     double *t1;                  // first Jacobi step of a cold solve, times scale
-    float4 *unit;                // reference bond direction per constraint (FP32), for the coupling pass
 };
-void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s);
-// lam0[k] = (t1[k] + y_k * t_scale + t_mean) / scale[k] from the raw features
-void gm_launch_ws_infer(int n, const float *feat, const float *params, const float *norm, const double *scale,
-                        const double *t1, double *lam0, float *y_out, cudaStream_t s);
+// One launch per solve: every constraint's raw features, t1 and scale, and
+// with infer the network on the tensor cores and the predicted multipliers
+// lam0[k] = (t1[k] + y_k * t_scale + t_mean) / scale[k].
+void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
+                          cudaStream_t s);
+// The network's output y for m standardised inputs x[m][12] (same kernels).
+void gm_launch_ws_forward(int m, const float *x, const float *params, float *y, cudaStream_t s);
 // records raw features and targets lam_sum * scale - t1 into slot rec_n when
 // step % stride == 0 (resident steps), then advances rec_n
 void gm_launch_ws_record(int n_constr, const float *feat, const double *lam_sum, const double *scale, const double *t1,

@@ -12,10 +12,13 @@
 // relative error of the whole.
 // Numerics: the matmul weights (W1, W2, w3) and the activations (input,
 // both hidden layers) are rounded to BF16 (round to nearest even), biases
-// stay FP32, every sum is FP32 in ascending index order, SiLU(z) =
-// z / (1 + exp(-z)).  Training gradients treat the BF16 roundings as the
-// identity.  Per-block gradient partials are summed in block order, so
-// training is run-to-run identical.
+// stay FP32, SiLU(z) = z / (1 + exp(-z)).  Inference runs both hidden layers
+// on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation,
+// in the tensor cores' own summation order), fused with the feature pass:
+// one kernel per SHAKE solve.  The training kernels sum in FP32 in ascending
+// index order and treat the BF16 roundings as the identity; per-block
+// gradient partials are summed in block order, so training is run-to-run
+// identical.
 #include <cuda_bf16.h>
 
 #include "gm_internal.cuh"
@@ -52,10 +55,8 @@ __device__ __forceinline__ void ref_unit(const WsFeatureArgs &a, int k, float &u
     uz = __fmul_rn(rz, il);
 }
 
-// Pass 1: the constraint's own features 0-7, t1 and the scale.
-__global__ void ws_features_kernel(WsFeatureArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n_constr) return;
+// t1 = (|r_trial|^2 - d0^2) / (r_trial . r_ref) of constraint k, FP64.
+__device__ __forceinline__ double t1_of(const WsFeatureArgs &a, int k, double *t2o = nullptr, double *dro = nullptr) {
     const int i = a.constr_i[k], j = a.constr_j[k], n = a.n_atoms;
     const double d0sq = a.constr_dsq[k];
     const double rx = __dsub_rn(a.dref[i], a.dref[j]), ry = __dsub_rn(a.dref[n + i], a.dref[n + j]),
@@ -64,10 +65,18 @@ __global__ void ws_features_kernel(WsFeatureArgs a) {
                  tz = __dsub_rn(a.pos[2 * n + i], a.pos[2 * n + j]);
     const double t2 = dot3(tx, ty, tz, tx, ty, tz);
     const double dr = dot3(tx, ty, tz, rx, ry, rz);
-    const double t1 = dr == 0.0 ? 0.0 : __ddiv_rn(__dsub_rn(t2, d0sq), dr);
-    a.t1[k] = t1;
-    a.scale[k] = __dmul_rn(2.0, __dadd_rn(a.inv_mass[i], a.inv_mass[j]));
-    float *f = a.feat + (size_t)k * kIn;
+    if (t2o) *t2o = t2;
+    if (dro) *dro = dr;
+    return dr == 0.0 ? 0.0 : __ddiv_rn(__dsub_rn(t2, d0sq), dr);
+}
+
+// The constraint's own features 0-7, its t1 and its scale 2 (1/m_i + 1/m_j).
+__device__ __forceinline__ void own_features(const WsFeatureArgs &a, int k, float *f, double &t1, double &scale) {
+    const int i = a.constr_i[k], j = a.constr_j[k];
+    const double d0sq = a.constr_dsq[k];
+    double t2, dr;
+    t1 = t1_of(a, k, &t2, &dr);
+    scale = __dmul_rn(2.0, __dadd_rn(a.inv_mass[i], a.inv_mass[j]));
     f[0] = (float)__ddiv_rn(__dsub_rn(t2, d0sq), d0sq);
     f[1] = (float)__ddiv_rn(dr, d0sq);
     f[2] = (float)__dsqrt_rn(d0sq);
@@ -76,21 +85,16 @@ __global__ void ws_features_kernel(WsFeatureArgs a) {
     f[5] = (float)(a.atom_cstart[i + 1] - a.atom_cstart[i]);
     f[6] = (float)(a.atom_cstart[j + 1] - a.atom_cstart[j]);
     f[7] = (float)t1;
-    float ux, uy, uz;
-    ref_unit(a, k, ux, uy, uz);
-    a.unit[k] = make_float4(ux, uy, uz, 0.f);
 }
 
-// Pass 2: coupling to the other constraints on the constraint's two atoms
-// (features 8-11) in FP32, atom i's constraints then atom j's, each
-// ascending; masses and t1 enter rounded to FP32.
-__global__ void ws_coupling_kernel(WsFeatureArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n_constr) return;
+// Coupling to the other constraints on the constraint's two atoms (features
+// 8-11) in FP32, atom i's constraints then atom j's, each ascending; masses
+// and the neighbours' t1 enter rounded to FP32.
+__device__ __forceinline__ void coupling_features(const WsFeatureArgs &a, int k, float *f) {
     const int ends[2] = {a.constr_i[k], a.constr_j[k]};
     const float wk = __fadd_rn((float)a.inv_mass[ends[0]], (float)a.inv_mass[ends[1]]);
-    const float4 uk = a.unit[k];
-    const float ux = uk.x, uy = uk.y, uz = uk.z;
+    float ux, uy, uz;
+    ref_unit(a, k, ux, uy, uz);
     float c1 = 0.0f, c2 = 0.0f, cmax = 0.0f, ct = 0.0f;
     for (int e = 0; e < 2; e++) {
         const int at = ends[e];
@@ -101,22 +105,220 @@ __global__ void ws_coupling_kernel(WsFeatureArgs a) {
             const int l = ref >= 0 ? ref : -ref - 1;
             if (l == k) continue;
             const float sl = ref >= 0 ? 1.0f : -1.0f;
-            const float4 ul = a.unit[l];
-            const float cs = dot3f(ux, uy, uz, ul.x, ul.y, ul.z);
+            float vx, vy, vz;
+            ref_unit(a, l, vx, vy, vz);
+            const float cs = dot3f(ux, uy, uz, vx, vy, vz);
             const float wl = __fadd_rn((float)a.inv_mass[a.constr_i[l]], (float)a.inv_mass[a.constr_j[l]]);
             const float coup = __fmul_rn(__fmul_rn(__fdiv_rn(inv_a, wk), cs), __fmul_rn(sk, sl));
-            const float tl = (float)a.t1[l];
+            const float tl = (float)t1_of(a, l);
             c1 = __fadd_rn(c1, __fdiv_rn(__fmul_rn(__fmul_rn(coup, tl), wk), wl));
             c2 = __fadd_rn(c2, __fmul_rn(coup, coup));
             cmax = fmaxf(cmax, fabsf(cs));
             ct = __fadd_rn(ct, tl);
         }
     }
-    float *f = a.feat + (size_t)k * kIn;
     f[8] = c1;
     f[9] = c2;
     f[10] = cmax;
     f[11] = ct;
+}
+
+// ---- the network on the tensor cores ----------------------------------
+//
+// A warp takes 32 constraints (rows) at a time as two m16 tiles.  Layer 1:
+// X [16 x 16] (12 features, 4 zero columns) times W1 [16 x 64]: eight
+// m16n8k16 MMAs.  Its accumulators, after bias, SiLU and BF16 rounding, are
+// already laid out as the A operand of layer 2 (an m16n8 accumulator pair
+// (n-tiles 2kk, 2kk + 1) is the A fragment of k-step kk), so layer 2, [16 x
+// 64] times W2 [64 x 64], is 32 MMAs without leaving registers.  Layer 3 (64
+// -> 1) is a dot product per row over the lane quad that holds it.  The B
+// operands (W1, W2 as BF16 pairs) sit in shared memory in fragment order:
+// one conflict-free 64-bit load per lane per MMA.
+
+struct MlpSmem {
+    uint2 b1f[8][32];     // W1 fragments per n-tile
+    uint2 b2f[4][8][32];  // W2 fragments per (k-step, n-tile)
+    float b1[kH], b2[kH], w3[kH];
+    float b3;
+    float mean[kIn], inv[kIn], tmean, tscale;
+};
+
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint2 b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ float silu(float z) { return z * sigmoid_rcp(z); }
+
+// The parameters in fragment order (BF16 pairs: the lower column index in
+// the low half), biases and the input standardisation (norm may be null:
+// inputs already standardised).
+__device__ void load_mlp(const float *__restrict__ P, const float *__restrict__ norm, MlpSmem &S) {
+    for (int e = threadIdx.x; e < 8 * 32; e += blockDim.x) {
+        const int j = e >> 5, l = e & 31, g = l >> 2, t = l & 3, n = 8 * j + g;
+        float w[4];
+        const int ks[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] = ks[q] < kIn ? P[GM_WS_OFF_W1 + ks[q] * kH + n] : 0.0f;
+        S.b1f[j][l] = make_uint2(pack_bf2(w[0], w[1]), pack_bf2(w[2], w[3]));
+    }
+    for (int e = threadIdx.x; e < 4 * 8 * 32; e += blockDim.x) {
+        const int kk = e >> 8, j = (e >> 5) & 7, l = e & 31, g = l >> 2, t = l & 3;
+        const int n = 8 * j + g, k0 = 16 * kk + 2 * t;
+        const float *W2 = P + GM_WS_OFF_W2;
+        S.b2f[kk][j][l] = make_uint2(pack_bf2(W2[k0 * kH + n], W2[(k0 + 1) * kH + n]),
+                                     pack_bf2(W2[(k0 + 8) * kH + n], W2[(k0 + 9) * kH + n]));
+    }
+    for (int o = threadIdx.x; o < kH; o += blockDim.x) {
+        S.b1[o] = P[GM_WS_OFF_B1 + o];
+        S.b2[o] = P[GM_WS_OFF_B2 + o];
+        S.w3[o] = bf(P[GM_WS_OFF_W3 + o]);
+    }
+    if (threadIdx.x < kIn) {
+        S.mean[threadIdx.x] = norm ? norm[threadIdx.x] : 0.0f;
+        S.inv[threadIdx.x] = norm ? __frcp_rn(norm[kIn + threadIdx.x]) : 1.0f;
+    }
+    if (threadIdx.x == 0) {
+        S.b3 = P[GM_WS_OFF_B3];
+        S.tmean = norm ? norm[24] : 0.0f;
+        S.tscale = norm ? norm[25] : 1.0f;
+    }
+}
+
+// y of the warp's 32 rows: sX[row][c] holds the BF16 input pair (2c, 2c + 1)
+// of the row (c < 6; 6 and 7 are zero); y goes to sy[row].
+__device__ __forceinline__ void mlp_rows32(const MlpSmem &S, const uint32_t (*sX)[8], float *sy) {
+    const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++) {
+        const int r0 = 16 * mt + g, r1 = r0 + 8;
+        const uint32_t a0 = sX[r0][t], a1 = sX[r1][t], a2 = sX[r0][t + 4], a3 = sX[r1][t + 4];
+        float z1[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float c0 = S.b1[8 * j + 2 * t], c1 = S.b1[8 * j + 2 * t + 1];
+            z1[j][0] = c0; z1[j][1] = c1; z1[j][2] = c0; z1[j][3] = c1;
+            mma_bf16(z1[j], a0, a1, a2, a3, S.b1f[j][l]);
+        }
+        uint32_t A2[4][4];
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+            A2[kk][0] = pack_bf2(silu(z1[2 * kk][0]), silu(z1[2 * kk][1]));
+            A2[kk][1] = pack_bf2(silu(z1[2 * kk][2]), silu(z1[2 * kk][3]));
+            A2[kk][2] = pack_bf2(silu(z1[2 * kk + 1][0]), silu(z1[2 * kk + 1][1]));
+            A2[kk][3] = pack_bf2(silu(z1[2 * kk + 1][2]), silu(z1[2 * kk + 1][3]));
+        }
+        float z2[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float c0 = S.b2[8 * j + 2 * t], c1 = S.b2[8 * j + 2 * t + 1];
+            z2[j][0] = c0; z2[j][1] = c1; z2[j][2] = c0; z2[j][3] = c1;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) mma_bf16(z2[j], A2[kk][0], A2[kk][1], A2[kk][2], A2[kk][3], S.b2f[kk][j][l]);
+        float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int c = 8 * j + 2 * t;
+            y0 = fmaf(bf(silu(z2[j][0])), S.w3[c], y0);
+            y0 = fmaf(bf(silu(z2[j][1])), S.w3[c + 1], y0);
+            y1 = fmaf(bf(silu(z2[j][2])), S.w3[c], y1);
+            y1 = fmaf(bf(silu(z2[j][3])), S.w3[c + 1], y1);
+        }
+        y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
+        y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
+        if (t == 0) {
+            sy[r0] = S.b3 + y0;
+            sy[r1] = S.b3 + y1;
+        }
+    }
+}
+
+constexpr int kPredWarps = 4;
+
+// One kernel per SHAKE solve: each lane computes one constraint's features
+// (written out for the recorder, with t1 and the scale), and with `infer`
+// the warp runs the network on its 32 constraints and writes the predicted
+// multipliers lam0 = (t1 + y t_scale + t_mean) / scale.
+__global__ void __launch_bounds__(kPredWarps * 32) ws_predict_kernel(WsFeatureArgs a, const float *__restrict__ P,
+                                                                   const float *__restrict__ norm, double *lam0,
+                                                                   int infer) {
+    __shared__ MlpSmem S;
+    __shared__ uint32_t sX[kPredWarps][32][8];
+    __shared__ float sy[kPredWarps][32];
+    if (infer) load_mlp(P, norm, S);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int n_tiles = (a.n_constr + 31) / 32;
+    for (int tile = blockIdx.x * kPredWarps + w; tile < n_tiles; tile += gridDim.x * kPredWarps) {
+        const int k = tile * 32 + l;
+        const bool live = k < a.n_constr;
+        float f[kIn];
+#pragma unroll
+        for (int q = 0; q < kIn; q++) f[q] = 0.0f;
+        double t1 = 0.0, scale = 1.0;
+        if (live) {
+            own_features(a, k, f, t1, scale);
+            coupling_features(a, k, f);
+            float *fo = a.feat + (size_t)k * kIn;
+#pragma unroll
+            for (int q = 0; q < kIn; q++) fo[q] = f[q];
+            a.t1[k] = t1;
+            a.scale[k] = scale;
+        }
+        if (!infer) continue;  // warp-uniform
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int q0 = 2 * c, q1 = 2 * c + 1;
+            sX[w][l][c] = (live && c < kIn / 2)
+                              ? pack_bf2((f[q0] - S.mean[q0]) * S.inv[q0], (f[q1] - S.mean[q1]) * S.inv[q1])
+                              : 0u;
+        }
+        __syncwarp();
+        mlp_rows32(S, sX[w], sy[w]);
+        __syncwarp();
+        if (live) lam0[k] = (t1 + ((double)sy[w][l] * (double)S.tscale + (double)S.tmean)) / scale;
+        __syncwarp();
+    }
+}
+
+// The network on m standardised inputs x[m][12] (tests and the C ABI's
+// gm_ws_forward): the same tensor-core code as the step's inference.
+__global__ void __launch_bounds__(kPredWarps * 32) ws_forward_kernel(int m, const float *__restrict__ x,
+                                                                   const float *__restrict__ P, float *y) {
+    __shared__ MlpSmem S;
+    __shared__ uint32_t sX[kPredWarps][32][8];
+    __shared__ float sy[kPredWarps][32];
+    load_mlp(P, nullptr, S);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int n_tiles = (m + 31) / 32;
+    for (int tile = blockIdx.x * kPredWarps + w; tile < n_tiles; tile += gridDim.x * kPredWarps) {
+        const int k = tile * 32 + l;
+        const bool live = k < m;
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            sX[w][l][c] = (live && c < kIn / 2) ? pack_bf2(x[(size_t)k * kIn + 2 * c], x[(size_t)k * kIn + 2 * c + 1])
+                                                : 0u;
+        __syncwarp();
+        mlp_rows32(S, sX[w], sy[w]);
+        __syncwarp();
+        if (live) y[k] = sy[w][l];
+        __syncwarp();
+    }
 }
 
 // Weights into shared memory: matmul weights BF16-rounded, biases as is.
@@ -150,91 +352,6 @@ __device__ void load_weights(const float *P, float *sW1, float *sb1, float *sW2,
         }
     }
     if (threadIdx.x == 0) *sb3 = P[GM_WS_OFF_B3];
-}
-
-// Inference: TPC threads per constraint, thread q owning the U = 64 / TPC
-// hidden units [U q, U q + U) of both layers.  Weights are read from shared
-// memory four at a time (128-bit loads) into U independent accumulations; the
-// first layer's activations reach the other threads of the group by
-// shuffles.  Every sum keeps the ascending order of the one-thread form (each
-// unit over its inputs in index order; the output over the units in index
-// order, passed along the group).  Inputs are standardised with the
-// correctly rounded reciprocal of the spread (within an ulp of the division,
-// before their BF16 rounding) and the SiLU's 1 / (1 + exp(-z)) is a
-// correctly rounded reciprocal (equal to the division).
-template <int TPC>
-__global__ void __launch_bounds__(256) ws_infer_kernel(int n, const float *__restrict__ feat,
-                                                       const float *__restrict__ P, const float *__restrict__ norm,
-                                                       const double *__restrict__ scale,
-                                                       const double *__restrict__ t1, double *lam0, float *y_out) {
-    constexpr int U = kH / TPC;
-    static_assert(U % 4 == 0, "units per thread in whole 128-bit loads");
-    __shared__ __align__(16) float sW1[kIn * kH];
-    __shared__ __align__(16) float sW2[kH * kH];
-    __shared__ __align__(16) float sb1[kH];
-    __shared__ __align__(16) float sb2[kH];
-    __shared__ __align__(16) float sw3[kH];
-    __shared__ float sb3, snorm[GM_WS_NNORM], sinv[kIn];
-    load_weights(P, sW1, sb1, sW2, sb2, sw3, &sb3);
-    if (threadIdx.x < GM_WS_NNORM) snorm[threadIdx.x] = norm[threadIdx.x];
-    if (threadIdx.x < kIn) sinv[threadIdx.x] = __frcp_rn(norm[kIn + threadIdx.x]);
-    __syncthreads();
-    const int q = threadIdx.x % TPC, base = (threadIdx.x & 31) - q;
-    const int k = blockIdx.x * (blockDim.x / TPC) + threadIdx.x / TPC;
-    const bool live = k < n;  // a group past n still joins the shuffles
-    const int o0 = U * q;
-    float x[kIn];
-#pragma unroll
-    for (int f = 0; f < kIn; f++) x[f] = live ? bf((feat[(size_t)k * kIn + f] - snorm[f]) * sinv[f]) : 0.f;
-    float z[U];
-#pragma unroll
-    for (int j = 0; j < U; j++) z[j] = sb1[o0 + j];
-#pragma unroll
-    for (int f = 0; f < kIn; f++) {
-        const float4 *w = reinterpret_cast<const float4 *>(sW1 + f * kH + o0);
-#pragma unroll
-        for (int v = 0; v < U / 4; v++) {
-            const float4 w4 = w[v];
-            z[4 * v] = fmaf(x[f], w4.x, z[4 * v]);
-            z[4 * v + 1] = fmaf(x[f], w4.y, z[4 * v + 1]);
-            z[4 * v + 2] = fmaf(x[f], w4.z, z[4 * v + 2]);
-            z[4 * v + 3] = fmaf(x[f], w4.w, z[4 * v + 3]);
-        }
-    }
-    float a1[U];
-#pragma unroll
-    for (int j = 0; j < U; j++) a1[j] = bf(z[j] * sigmoid_rcp(z[j]));
-#pragma unroll
-    for (int j = 0; j < U; j++) z[j] = sb2[o0 + j];
-#pragma unroll
-    for (int src = 0; src < TPC; src++) {
-#pragma unroll
-        for (int jj = 0; jj < U; jj++) {
-            const float a = __shfl_sync(0xffffffffu, a1[jj], base + src);  // unit U src + jj
-            const float4 *w = reinterpret_cast<const float4 *>(sW2 + (U * src + jj) * kH + o0);
-#pragma unroll
-            for (int v = 0; v < U / 4; v++) {
-                const float4 w4 = w[v];
-                z[4 * v] = fmaf(a, w4.x, z[4 * v]);
-                z[4 * v + 1] = fmaf(a, w4.y, z[4 * v + 1]);
-                z[4 * v + 2] = fmaf(a, w4.z, z[4 * v + 2]);
-                z[4 * v + 3] = fmaf(a, w4.w, z[4 * v + 3]);
-            }
-        }
-    }
-    // the output: units 0..63 in order, thread 0's, then thread 1's, ...
-    float y = sb3;
-#pragma unroll
-    for (int src = 0; src < TPC; src++) {
-        if (q == src) {
-#pragma unroll
-            for (int j = 0; j < U; j++) y = fmaf(bf(z[j] * sigmoid_rcp(z[j])), sw3[o0 + j], y);
-        }
-        y = __shfl_sync(0xffffffffu, y, base + src);
-    }
-    if (!live || q != 0) return;
-    if (y_out) y_out[k] = y;
-    if (lam0) lam0[k] = (t1[k] + ((double)y * (double)snorm[25] + (double)snorm[24])) / scale[k];
 }
 
 __global__ void ws_record_kernel(int nc, const float *feat, const double *lam_sum, const double *scale,
@@ -443,18 +560,21 @@ __global__ void ws_update_kernel(int blocks, const float *partial, float *P, flo
 
 }  // namespace
 
-void gm_launch_ws_features(const WsFeatureArgs &a, cudaStream_t s) {
-    if (a.n_constr == 0) return;
-    ws_features_kernel<<<(a.n_constr + 255) / 256, 256, 0, s>>>(a);
-    ws_coupling_kernel<<<(a.n_constr + 255) / 256, 256, 0, s>>>(a);
+int gm_ws_predict_blocks(int n_constr) {
+    const int tiles = (n_constr + 31) / 32;
+    return (tiles + kPredWarps - 1) / kPredWarps;
 }
 
-void gm_launch_ws_infer(int n, const float *feat, const float *params, const float *norm, const double *scale,
-                        const double *t1, double *lam0, float *y_out, cudaStream_t s) {
-    if (n == 0) return;
-    constexpr int kTPC = 16, kThreads = 256, kPerBlock = kThreads / kTPC;
-    ws_infer_kernel<kTPC><<<(n + kPerBlock - 1) / kPerBlock, kThreads, 0, s>>>(n, feat, params, norm, scale, t1, lam0,
-                                                                              y_out);
+void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
+                          cudaStream_t s) {
+    if (a.n_constr == 0) return;
+    ws_predict_kernel<<<gm_ws_predict_blocks(a.n_constr), kPredWarps * 32, 0, s>>>(a, params, norm, lam0,
+                                                                                  infer ? 1 : 0);
+}
+
+void gm_launch_ws_forward(int m, const float *x, const float *params, float *y, cudaStream_t s) {
+    if (m == 0) return;
+    ws_forward_kernel<<<gm_ws_predict_blocks(m), kPredWarps * 32, 0, s>>>(m, x, params, y);
 }
 
 void gm_launch_ws_record(int n_constr, const float *feat, const double *lam_sum, const double *scale, const double *t1,
