@@ -15,10 +15,11 @@
 // stay FP32, SiLU(z) = z / (1 + exp(-z)).  Inference runs both hidden layers
 // on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation,
 // in the tensor cores' own summation order), fused with the feature pass:
-// one kernel per SHAKE solve.  The training kernels sum in FP32 in ascending
-// index order and treat the BF16 roundings as the identity; per-block
-// gradient partials are summed in block order, so training is run-to-run
-// identical.
+// one kernel per SHAKE solve.  Training runs its forward pass, the backward
+// products and the tile's weight-gradient sums on the tensor cores too (the
+// deltas as a BF16 high part plus a BF16 remainder), treats the BF16
+// roundings of the forward pass as the identity, and sums the per-block
+// gradient partials in block order, so training is run-to-run identical.
 #include <cuda_bf16.h>
 
 #include "gm_internal.cuh"
@@ -27,7 +28,6 @@ namespace {
 
 constexpr int kIn = GM_WS_IN, kH = GM_WS_H, kNP = GM_WS_NPAR;
 constexpr int kTile = GM_WS_TILE;
-constexpr int kRow = kH + 1;  // padded shared-memory row (conflict-free per-sample rows)
 
 __device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-z)); }
@@ -321,39 +321,6 @@ __global__ void __launch_bounds__(kPredWarps * 32) ws_forward_kernel(int m, cons
     }
 }
 
-// Weights into shared memory: matmul weights BF16-rounded, biases as is.
-// 128-bit loads, four in flight per thread before their stores (every block
-// loads the 20 KB, so the latency of one load at a time would dominate a
-// short kernel).  The sections start on 16-byte boundaries (offsets are
-// multiples of four floats), and so do the shared arrays.
-__device__ __forceinline__ float4 bf4(float4 v) { return make_float4(bf(v.x), bf(v.y), bf(v.z), bf(v.w)); }
-__device__ __forceinline__ void store_weight4(int o, float4 v, float *sW1, float *sb1, float *sW2, float *sb2,
-                                              float *sw3) {
-    if (o < GM_WS_OFF_B1) *reinterpret_cast<float4 *>(sW1 + o) = bf4(v);
-    else if (o < GM_WS_OFF_W2) *reinterpret_cast<float4 *>(sb1 + o - GM_WS_OFF_B1) = v;
-    else if (o < GM_WS_OFF_B2) *reinterpret_cast<float4 *>(sW2 + o - GM_WS_OFF_W2) = bf4(v);
-    else if (o < GM_WS_OFF_W3) *reinterpret_cast<float4 *>(sb2 + o - GM_WS_OFF_B2) = v;
-    else *reinterpret_cast<float4 *>(sw3 + o - GM_WS_OFF_W3) = bf4(v);
-}
-__device__ void load_weights(const float *P, float *sW1, float *sb1, float *sW2, float *sb2, float *sw3, float *sb3) {
-    const float4 *P4 = reinterpret_cast<const float4 *>(P);
-    constexpr int kW4 = GM_WS_OFF_B3 / 4;
-    for (int t0 = threadIdx.x; t0 < kW4; t0 += 4 * blockDim.x) {
-        float4 v[4];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int t = t0 + r * (int)blockDim.x;
-            v[r] = t < kW4 ? __ldg(P4 + t) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int t = t0 + r * (int)blockDim.x;
-            if (t < kW4) store_weight4(4 * t, v[r], sW1, sb1, sW2, sb2, sw3);
-        }
-    }
-    if (threadIdx.x == 0) *sb3 = P[GM_WS_OFF_B3];
-}
-
 __global__ void ws_record_kernel(int nc, const float *feat, const double *lam_sum, const double *scale,
                                  const double *t1, float *rec_feat, float *rec_t, int stride, int cap,
                                  const DevStatus *st) {
@@ -423,112 +390,294 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     return z ^ (z >> 31);
 }
 
-// Shared-memory layout of the training kernel (floats).
-constexpr int kSmW = kIn * kH + kH + kH * kH + kH + kH + 4;
-constexpr int kSmX = kTile * (kIn + 1);
-constexpr int kSmRows = kTile * kRow;
-constexpr size_t kGradSmem = sizeof(float) * ((size_t)kSmW + kSmX + 4 * (size_t)kSmRows + 2 * kTile);
+// ---- training on the tensor cores -------------------------------------
+//
+// One block of 4 warps per tile of 128 samples (warp w: samples 32 w ..
+// 32 w + 31, two m16 tiles).  Per sample: the forward pass of mlp_rows32,
+// keeping z1, the BF16 layer-1 activations (as layer 2's A fragments) and z2;
+// the residual y - t; delta2 = dy w3 SiLU'(z2); delta_a1 = delta2 W2^T as
+// MMAs (delta2 split into a BF16 high part and a BF16 remainder, two MMAs
+// each, so the operand rounding stays near FP32); delta1 = delta_a1
+// SiLU'(z1).  Then the tile's parameter gradients as MMAs whose K dimension
+// is the 128 samples, read from shared memory: dW2 = A1^T delta2 (one m16
+// tile of W2's rows per warp) and dW1 = X^T delta1 (two n-tiles per warp),
+// again with the deltas as high + remainder.  Bias and w3 gradients and the
+// loss are FP32 sums over the samples in ascending order.  Every sum has a
+// fixed order, so training is run-to-run identical.
 
-// Forward and backward over one tile of 128 samples; one thread per sample
-// for the passes, then one thread per parameter group for the block sums.
-__global__ void __launch_bounds__(kTile) ws_grad_kernel(long long n, const float *__restrict__ feat,
-                                                        const float *__restrict__ tt, const float *__restrict__ norm,
-                                                        int standardized, const float *__restrict__ P,
-                                                        unsigned long long seed, long long iter, long long n_valid,
-                                                        float inv_batch, float *__restrict__ partial) {
-    extern __shared__ float sm[];
-    float *sW1 = sm, *sb1 = sW1 + kIn * kH, *sW2 = sb1 + kH, *sb2 = sW2 + kH * kH, *sw3 = sb2 + kH, *sb3 = sw3 + kH;
-    float *xb = sm + kSmW;
-    float *a1b = xb + kSmX, *a2b = a1b + kSmRows, *d2 = a2b + kSmRows, *d1 = d2 + kSmRows;
-    float *sdy = d1 + kSmRows, *sloss = sdy + kTile;
-    load_weights(P, sW1, sb1, sW2, sb2, sw3, sb3);
-    __syncthreads();
-    const int s = threadIdx.x;
-    const long long row = (long long)blockIdx.x * kTile + s;
-    const bool valid = row < n_valid;
-    long long sample;
-    if (iter < 0) sample = row < n ? row : n - 1;
-    else sample = (long long)(mix64(seed ^ mix64((unsigned long long)iter * 0x100000001B3ull + (unsigned long long)row)) %
-                              (unsigned long long)n);
-    // forward
-    float *xs = xb + s * (kIn + 1);
-    for (int f = 0; f < kIn; f++) {
-        const float v = feat[sample * kIn + f];
-        xs[f] = bf(standardized ? v : (v - norm[f]) / norm[kIn + f]);
+struct GradSmem {
+    MlpSmem m;                          // forward fragments, biases, w3
+    uint2 b2t[4][8][32];                // W2^T fragments (B[k = o][n = q] = W2[q][o])
+    uint32_t x[kTile][8];               // inputs, BF16 pairs
+    __nv_bfloat16 a1[kTile][kH];        // layer-1 activations (BF16, exact)
+    __nv_bfloat16 a2[kTile][kH];        // layer-2 activations
+    __nv_bfloat16 d2h[kTile][kH], d2l[kTile][kH];  // delta2, high part and remainder
+    __nv_bfloat16 d1h[kTile][kH], d1l[kTile][kH];  // delta1
+    float dy[kTile], loss[kTile];
+};
+
+__device__ __forceinline__ float sig_d(float z) {
+    // d SiLU / dz = g (1 + z (1 - g)), g = sigmoid(z)
+    const float g = sigmoid(z);
+    return g * (1.0f + z * (1.0f - g));
+}
+
+__device__ __forceinline__ uint32_t pack_raw(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__global__ void __launch_bounds__(kTile) ws_grad_mma_kernel(long long n, const float *__restrict__ feat,
+                                                            const float *__restrict__ tt,
+                                                            const float *__restrict__ norm, int standardized,
+                                                            const float *__restrict__ P, unsigned long long seed,
+                                                            long long iter, long long n_valid, float inv_batch,
+                                                            float *__restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    GradSmem &G = *reinterpret_cast<GradSmem *>(smraw);
+    load_mlp(P, nullptr, G.m);
+    for (int e = threadIdx.x; e < 4 * 8 * 32; e += blockDim.x) {
+        const int kk = e >> 8, j = (e >> 5) & 7, l = e & 31, g = l >> 2, t = l & 3;
+        const int nq = 8 * j + g, k0 = 16 * kk + 2 * t;  // B[k = o][n = q] = W2[q][o]
+        const float *W2 = P + GM_WS_OFF_W2;
+        G.b2t[kk][j][l] = make_uint2(pack_bf2(W2[nq * kH + k0], W2[nq * kH + k0 + 1]),
+                                     pack_bf2(W2[nq * kH + k0 + 8], W2[nq * kH + k0 + 9]));
     }
-    const float t = standardized ? tt[sample] : (tt[sample] - norm[24]) / norm[25];
-    float sd1[kH];
-    float *a1s = a1b + s * kRow, *a2s = a2b + s * kRow, *d2s = d2 + s * kRow, *d1s = d1 + s * kRow;
-#pragma unroll
-    for (int o = 0; o < kH; o++) {
-        float z = sb1[o];
-        for (int f = 0; f < kIn; f++) z = fmaf(xs[f], sW1[f * kH + o], z);
-        const float g = sigmoid(z);
-        a1s[o] = bf(z * g);
-        sd1[o] = g * (1.0f + z * (1.0f - g));
-    }
-    float y = *sb3;
-    for (int o = 0; o < kH; o++) {
-        float z = sb2[o];
-        for (int q = 0; q < kH; q++) z = fmaf(a1s[q], sW2[q * kH + o], z);
-        const float g = sigmoid(z);
-        const float a2 = bf(z * g);
-        a2s[o] = a2;
-        d2s[o] = g * (1.0f + z * (1.0f - g));
-        y = fmaf(a2, sw3[o], y);
-    }
-    const float r = y - t;
-    const float dy = valid ? 2.0f * r * inv_batch : 0.0f;
-    sdy[s] = dy;
-    sloss[s] = valid ? r * r : 0.0f;
-    // backward through layer 3 and 2
-    for (int o = 0; o < kH; o++) d2s[o] = sw3[o] * dy * d2s[o];
-#pragma unroll
-    for (int q = 0; q < kH; q++) {
-        float da = 0.0f;
-        for (int o = 0; o < kH; o++) da = fmaf(sW2[q * kH + o], d2s[o], da);
-        d1s[q] = da * sd1[q];
-    }
-    __syncthreads();
-    // block sums over the tile's samples, ascending
-    float *out = partial + (size_t)blockIdx.x * (kNP + 1);
+    // the tile's samples and their standardised inputs
     {
-        const int k = s >> 1, o0 = (s & 1) * 32;
-        float acc[32];
+        const int s = threadIdx.x;
+        const long long row = (long long)blockIdx.x * kTile + s;
+        long long sample;
+        if (iter < 0) sample = row < n ? row : n - 1;
+        else sample = (long long)(mix64(seed ^ mix64((unsigned long long)iter * 0x100000001B3ull +
+                                                     (unsigned long long)row)) % (unsigned long long)n);
+        float xv[kIn];
+        for (int f = 0; f < kIn; f++) {
+            const float v = feat[sample * kIn + f];
+            xv[f] = standardized ? v : (v - norm[f]) / norm[kIn + f];
+        }
+        for (int c = 0; c < 8; c++) G.x[s][c] = c < kIn / 2 ? pack_bf2(xv[2 * c], xv[2 * c + 1]) : 0u;
+        const float tv = standardized ? tt[sample] : (tt[sample] - norm[24]) / norm[25];
+        G.dy[s] = tv;  // the target, replaced by dy below
+        G.loss[s] = row < n_valid ? 1.0f : 0.0f;  // validity, replaced by the squared residual
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+#pragma unroll 1
+    for (int mt = 0; mt < 2; mt++) {
+        const int r0 = 32 * w + 16 * mt + g, r1 = r0 + 8;
+        const uint32_t a0 = G.x[r0][t], a1 = G.x[r1][t], a2 = G.x[r0][t + 4], a3 = G.x[r1][t + 4];
+        float z1[8][4];
 #pragma unroll
-        for (int j = 0; j < 32; j++) acc[j] = 0.0f;
-        for (int q = 0; q < kTile; q++) {
-            const float a = a1b[q * kRow + k];
+        for (int j = 0; j < 8; j++) {
+            const float c0 = G.m.b1[8 * j + 2 * t], c1 = G.m.b1[8 * j + 2 * t + 1];
+            z1[j][0] = c0; z1[j][1] = c1; z1[j][2] = c0; z1[j][3] = c1;
+            mma_bf16(z1[j], a0, a1, a2, a3, G.m.b1f[j][l]);
+        }
+        uint32_t A2[4][4];
 #pragma unroll
-            for (int j = 0; j < 32; j++) acc[j] = fmaf(a, d2[q * kRow + o0 + j], acc[j]);
+        for (int kk = 0; kk < 4; kk++) {
+            A2[kk][0] = pack_bf2(silu(z1[2 * kk][0]), silu(z1[2 * kk][1]));
+            A2[kk][1] = pack_bf2(silu(z1[2 * kk][2]), silu(z1[2 * kk][3]));
+            A2[kk][2] = pack_bf2(silu(z1[2 * kk + 1][0]), silu(z1[2 * kk + 1][1]));
+            A2[kk][3] = pack_bf2(silu(z1[2 * kk + 1][2]), silu(z1[2 * kk + 1][3]));
+        }
+        // layer-1 activations to shared memory (rows r0, r1; columns of n-tile j: 8 j + 2 t, + 1)
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = 16 * kk + 8 * h + 2 * t;
+                *reinterpret_cast<uint32_t *>(&G.a1[r0][c]) = A2[kk][2 * h];
+                *reinterpret_cast<uint32_t *>(&G.a1[r1][c]) = A2[kk][2 * h + 1];
+            }
+        float z2[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float c0 = G.m.b2[8 * j + 2 * t], c1 = G.m.b2[8 * j + 2 * t + 1];
+            z2[j][0] = c0; z2[j][1] = c1; z2[j][2] = c0; z2[j][3] = c1;
         }
 #pragma unroll
-        for (int j = 0; j < 32; j++) out[GM_WS_OFF_W2 + k * kH + o0 + j] = acc[j];
-    }
-    for (int e = s; e < kIn * kH; e += kTile) {
-        const int f = e / kH, o = e % kH;
-        float acc = 0.0f;
-        for (int q = 0; q < kTile; q++) acc = fmaf(xb[q * (kIn + 1) + f], d1[q * kRow + o], acc);
-        out[GM_WS_OFF_W1 + e] = acc;
-    }
-    if (s < kH) {
-        float g1 = 0.0f, g3 = 0.0f;
-        for (int q = 0; q < kTile; q++) {
-            g1 += d1[q * kRow + s];
-            g3 = fmaf(a2b[q * kRow + s], sdy[q], g3);
+        for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) mma_bf16(z2[j], A2[kk][0], A2[kk][1], A2[kk][2], A2[kk][3], G.m.b2f[kk][j][l]);
+        float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int c = 8 * j + 2 * t;
+            const float v0 = bf(silu(z2[j][0])), v1 = bf(silu(z2[j][1])), v2 = bf(silu(z2[j][2])),
+                        v3 = bf(silu(z2[j][3]));
+            G.a2[r0][c] = __float2bfloat16_rn(v0);
+            G.a2[r0][c + 1] = __float2bfloat16_rn(v1);
+            G.a2[r1][c] = __float2bfloat16_rn(v2);
+            G.a2[r1][c + 1] = __float2bfloat16_rn(v3);
+            y0 = fmaf(v0, G.m.w3[c], y0);
+            y0 = fmaf(v1, G.m.w3[c + 1], y0);
+            y1 = fmaf(v2, G.m.w3[c], y1);
+            y1 = fmaf(v3, G.m.w3[c + 1], y1);
         }
-        out[GM_WS_OFF_B1 + s] = g1;
-        out[GM_WS_OFF_W3 + s] = g3;
-    } else {
-        const int o = s - kH;
-        float g2 = 0.0f;
-        for (int q = 0; q < kTile; q++) g2 += d2[q * kRow + o];
-        out[GM_WS_OFF_B2 + o] = g2;
-        if (o == 0) {
-            float gb = 0.0f, l = 0.0f;
-            for (int q = 0; q < kTile; q++) { gb += sdy[q]; l += sloss[q]; }
-            out[GM_WS_OFF_B3] = gb;
-            out[kNP] = l;
+        y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
+        y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
+        const float res0 = G.m.b3 + y0 - G.dy[r0], res1 = G.m.b3 + y1 - G.dy[r1];
+        const bool v0ok = G.loss[r0] != 0.0f, v1ok = G.loss[r1] != 0.0f;
+        const float dy0 = v0ok ? 2.0f * res0 * inv_batch : 0.0f, dy1 = v1ok ? 2.0f * res1 * inv_batch : 0.0f;
+        __syncwarp();
+        if (t == 0) {
+            G.dy[r0] = dy0;
+            G.dy[r1] = dy1;
+            G.loss[r0] = v0ok ? res0 * res0 : 0.0f;
+            G.loss[r1] = v1ok ? res1 * res1 : 0.0f;
+        }
+        // delta2 = dy w3 SiLU'(z2), as high + remainder, to shared memory and
+        // as A fragments of delta_a1 = delta2 W2^T
+        uint32_t Dh[4][4], Dl[4][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int c = 8 * j + 2 * t;
+            float d[4];
+            d[0] = dy0 * G.m.w3[c] * sig_d(z2[j][0]);
+            d[1] = dy0 * G.m.w3[c + 1] * sig_d(z2[j][1]);
+            d[2] = dy1 * G.m.w3[c] * sig_d(z2[j][2]);
+            d[3] = dy1 * G.m.w3[c + 1] * sig_d(z2[j][3]);
+            __nv_bfloat16 hi[4], lo[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                hi[q] = __float2bfloat16_rn(d[q]);
+                lo[q] = __float2bfloat16_rn(d[q] - __bfloat162float(hi[q]));
+            }
+            G.d2h[r0][c] = hi[0]; G.d2h[r0][c + 1] = hi[1]; G.d2h[r1][c] = hi[2]; G.d2h[r1][c + 1] = hi[3];
+            G.d2l[r0][c] = lo[0]; G.d2l[r0][c + 1] = lo[1]; G.d2l[r1][c] = lo[2]; G.d2l[r1][c + 1] = lo[3];
+            const int kk = j >> 1, h = j & 1;
+            Dh[kk][2 * h] = pack_raw(hi[0], hi[1]);
+            Dh[kk][2 * h + 1] = pack_raw(hi[2], hi[3]);
+            Dl[kk][2 * h] = pack_raw(lo[0], lo[1]);
+            Dl[kk][2 * h + 1] = pack_raw(lo[2], lo[3]);
+        }
+        float da[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) da[j][0] = da[j][1] = da[j][2] = da[j][3] = 0.0f;
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                mma_bf16(da[j], Dh[kk][0], Dh[kk][1], Dh[kk][2], Dh[kk][3], G.b2t[kk][j][l]);
+                mma_bf16(da[j], Dl[kk][0], Dl[kk][1], Dl[kk][2], Dl[kk][3], G.b2t[kk][j][l]);
+            }
+        // delta1 = delta_a1 SiLU'(z1)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int c = 8 * j + 2 * t;
+            float d[4];
+            d[0] = da[j][0] * sig_d(z1[j][0]);
+            d[1] = da[j][1] * sig_d(z1[j][1]);
+            d[2] = da[j][2] * sig_d(z1[j][2]);
+            d[3] = da[j][3] * sig_d(z1[j][3]);
+            const int rr[4] = {r0, r0, r1, r1}, cc[4] = {c, c + 1, c, c + 1};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const __nv_bfloat16 hi = __float2bfloat16_rn(d[q]);
+                G.d1h[rr[q]][cc[q]] = hi;
+                G.d1l[rr[q]][cc[q]] = __float2bfloat16_rn(d[q] - __bfloat162float(hi));
+            }
+        }
+    }
+    __syncthreads();
+    float *out = partial + (size_t)blockIdx.x * (kNP + 1);
+    // dW2[q][o] = sum_s A1[s][q] delta2[s][o]: warp w takes rows q in [16 w, 16 w + 16)
+    {
+        float acc[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        const int q0 = 16 * w + g, q1 = q0 + 8;
+#pragma unroll 1
+        for (int kk = 0; kk < kTile / 16; kk++) {
+            const int s0 = 16 * kk + 2 * t;
+            const uint32_t A0 = pack_raw(G.a1[s0][q0], G.a1[s0 + 1][q0]);
+            const uint32_t A1 = pack_raw(G.a1[s0][q1], G.a1[s0 + 1][q1]);
+            const uint32_t A2r = pack_raw(G.a1[s0 + 8][q0], G.a1[s0 + 9][q0]);
+            const uint32_t A3 = pack_raw(G.a1[s0 + 8][q1], G.a1[s0 + 9][q1]);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int o = 8 * j + g;
+                const uint2 bh = make_uint2(pack_raw(G.d2h[s0][o], G.d2h[s0 + 1][o]),
+                                            pack_raw(G.d2h[s0 + 8][o], G.d2h[s0 + 9][o]));
+                const uint2 bl = make_uint2(pack_raw(G.d2l[s0][o], G.d2l[s0 + 1][o]),
+                                            pack_raw(G.d2l[s0 + 8][o], G.d2l[s0 + 9][o]));
+                mma_bf16(acc[j], A0, A1, A2r, A3, bh);
+                mma_bf16(acc[j], A0, A1, A2r, A3, bl);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int o = 8 * j + 2 * t;
+            out[GM_WS_OFF_W2 + q0 * kH + o] = acc[j][0];
+            out[GM_WS_OFF_W2 + q0 * kH + o + 1] = acc[j][1];
+            out[GM_WS_OFF_W2 + q1 * kH + o] = acc[j][2];
+            out[GM_WS_OFF_W2 + q1 * kH + o + 1] = acc[j][3];
+        }
+    }
+    // dW1[f][o] = sum_s X[s][f] delta1[s][o]: one m16 tile of f (rows 12-15
+    // are the zero padding), warp w takes n-tiles 2 w and 2 w + 1
+    {
+        float acc[2][4];
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++) acc[jj][0] = acc[jj][1] = acc[jj][2] = acc[jj][3] = 0.0f;
+        const __nv_bfloat16 *xs = reinterpret_cast<const __nv_bfloat16 *>(G.x);  // [s][16]
+#pragma unroll 1
+        for (int kk = 0; kk < kTile / 16; kk++) {
+            const int s0 = 16 * kk + 2 * t;
+            auto X = [&](int sv, int f) { return xs[sv * 16 + f]; };
+            const uint32_t A0 = pack_raw(X(s0, g), X(s0 + 1, g));
+            const uint32_t A1 = pack_raw(X(s0, g + 8), X(s0 + 1, g + 8));
+            const uint32_t A2r = pack_raw(X(s0 + 8, g), X(s0 + 9, g));
+            const uint32_t A3 = pack_raw(X(s0 + 8, g + 8), X(s0 + 9, g + 8));
+#pragma unroll
+            for (int jj = 0; jj < 2; jj++) {
+                const int o = 8 * (2 * w + jj) + g;
+                const uint2 bh = make_uint2(pack_raw(G.d1h[s0][o], G.d1h[s0 + 1][o]),
+                                            pack_raw(G.d1h[s0 + 8][o], G.d1h[s0 + 9][o]));
+                const uint2 bl = make_uint2(pack_raw(G.d1l[s0][o], G.d1l[s0 + 1][o]),
+                                            pack_raw(G.d1l[s0 + 8][o], G.d1l[s0 + 9][o]));
+                mma_bf16(acc[jj], A0, A1, A2r, A3, bh);
+                mma_bf16(acc[jj], A0, A1, A2r, A3, bl);
+            }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++) {
+            const int o = 8 * (2 * w + jj) + 2 * t;
+            if (g < kIn) {
+                out[GM_WS_OFF_W1 + g * kH + o] = acc[jj][0];
+                out[GM_WS_OFF_W1 + g * kH + o + 1] = acc[jj][1];
+            }
+            if (g + 8 < kIn) {
+                out[GM_WS_OFF_W1 + (g + 8) * kH + o] = acc[jj][2];
+                out[GM_WS_OFF_W1 + (g + 8) * kH + o + 1] = acc[jj][3];
+            }
+        }
+    }
+    // biases, w3 and the loss: FP32 sums over the samples, ascending
+    {
+        const int s = threadIdx.x;
+        if (s < kH) {
+            float g1 = 0.0f, g3 = 0.0f;
+            for (int q = 0; q < kTile; q++) {
+                g1 += __bfloat162float(G.d1h[q][s]) + __bfloat162float(G.d1l[q][s]);
+                g3 = fmaf(__bfloat162float(G.a2[q][s]), G.dy[q], g3);
+            }
+            out[GM_WS_OFF_B1 + s] = g1;
+            out[GM_WS_OFF_W3 + s] = g3;
+        } else {
+            const int o = s - kH;
+            float g2 = 0.0f;
+            for (int q = 0; q < kTile; q++) g2 += __bfloat162float(G.d2h[q][o]) + __bfloat162float(G.d2l[q][o]);
+            out[GM_WS_OFF_B2 + o] = g2;
+            if (o == 0) {
+                float gb = 0.0f, lsum = 0.0f;
+                for (int q = 0; q < kTile; q++) { gb += G.dy[q]; lsum += G.loss[q]; }
+                out[GM_WS_OFF_B3] = gb;
+                out[kNP] = lsum;
+            }
         }
     }
 }
@@ -596,12 +745,12 @@ void gm_launch_ws_grad(long long n, const float *feat, const float *t, const flo
                        float *partial, cudaStream_t s) {
     static bool attr = false;  // per process; the attribute is a property of the kernel
     if (!attr) {
-        cudaFuncSetAttribute(ws_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
+        cudaFuncSetAttribute(ws_grad_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
         attr = true;
     }
     const float inv_batch = 1.0f / (float)(n_valid < (long long)blocks * kTile ? n_valid : (long long)blocks * kTile);
-    ws_grad_kernel<<<blocks, kTile, kGradSmem, s>>>(n, feat, t, norm, standardized ? 1 : 0, params, seed, iter,
-                                                     n_valid, inv_batch, partial);
+    ws_grad_mma_kernel<<<blocks, kTile, sizeof(GradSmem), s>>>(n, feat, t, norm, standardized ? 1 : 0, params, seed,
+                                                                iter, n_valid, inv_batch, partial);
 }
 
 void gm_launch_ws_update(int blocks, const float *partial, float *params, float *m, float *v, float lr, float b1,
