@@ -420,10 +420,12 @@ struct WsFeatureArgs {
     float *feat;                 // [n_constr][12] raw features
     double *scale;               // 2 (1/m_i + 1/m_j) per constraint
     double *t1;                  // first Jacobi step of a cold solve, times scale
+    float4 *unit;                // reference bond direction per constraint (FP32), for the coupling pass
 };
-// One launch per solve: every constraint's raw features, t1 and scale, and
-// with infer the network on the tensor cores and the predicted multipliers
-// lam0[k] = (t1[k] + y_k * t_scale + t_mean) / scale[k].
+// Two launches per solve: every constraint's raw features, t1 and scale, and
+// with infer the network on the tensor cores (fused with the coupling pass)
+// and the predicted multipliers lam0[k] = (t1[k] + y_k * t_scale + t_mean) /
+// scale[k].
 void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
                           cudaStream_t s);
 // The network's output y for m standardised inputs x[m][12] (same kernels).

@@ -14,8 +14,8 @@
 // both hidden layers) are rounded to BF16 (round to nearest even), biases
 // stay FP32, SiLU(z) = z / (1 + exp(-z)).  Inference runs both hidden layers
 // on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation,
-// in the tensor cores' own summation order), fused with the feature pass:
-// one kernel per SHAKE solve.  Training runs its forward pass, the backward
+// in the tensor cores' own summation order), fused with the coupling pass:
+// two kernels per SHAKE solve.  Training runs its forward pass, the backward
 // products and the tile's weight-gradient sums on the tensor cores too (the
 // deltas as a BF16 high part plus a BF16 remainder), treats the BF16
 // roundings of the forward pass as the identity, and sums the per-block
@@ -89,12 +89,13 @@ __device__ __forceinline__ void own_features(const WsFeatureArgs &a, int k, floa
 
 // Coupling to the other constraints on the constraint's two atoms (features
 // 8-11) in FP32, atom i's constraints then atom j's, each ascending; masses
-// and the neighbours' t1 enter rounded to FP32.
+// and the neighbours' t1 enter rounded to FP32.  Reads every constraint's t1
+// and reference direction from the first pass.
 __device__ __forceinline__ void coupling_features(const WsFeatureArgs &a, int k, float *f) {
     const int ends[2] = {a.constr_i[k], a.constr_j[k]};
     const float wk = __fadd_rn((float)a.inv_mass[ends[0]], (float)a.inv_mass[ends[1]]);
-    float ux, uy, uz;
-    ref_unit(a, k, ux, uy, uz);
+    const float4 uk = a.unit[k];
+    const float ux = uk.x, uy = uk.y, uz = uk.z;
     float c1 = 0.0f, c2 = 0.0f, cmax = 0.0f, ct = 0.0f;
     for (int e = 0; e < 2; e++) {
         const int at = ends[e];
@@ -105,12 +106,11 @@ __device__ __forceinline__ void coupling_features(const WsFeatureArgs &a, int k,
             const int l = ref >= 0 ? ref : -ref - 1;
             if (l == k) continue;
             const float sl = ref >= 0 ? 1.0f : -1.0f;
-            float vx, vy, vz;
-            ref_unit(a, l, vx, vy, vz);
-            const float cs = dot3f(ux, uy, uz, vx, vy, vz);
+            const float4 ul = a.unit[l];
+            const float cs = dot3f(ux, uy, uz, ul.x, ul.y, ul.z);
             const float wl = __fadd_rn((float)a.inv_mass[a.constr_i[l]], (float)a.inv_mass[a.constr_j[l]]);
             const float coup = __fmul_rn(__fmul_rn(__fdiv_rn(inv_a, wk), cs), __fmul_rn(sk, sl));
-            const float tl = (float)t1_of(a, l);
+            const float tl = (float)a.t1[l];
             c1 = __fadd_rn(c1, __fdiv_rn(__fmul_rn(__fmul_rn(coup, tl), wk), wl));
             c2 = __fadd_rn(c2, __fmul_rn(coup, coup));
             cmax = fmaxf(cmax, fabsf(cs));
@@ -249,10 +249,28 @@ __device__ __forceinline__ void mlp_rows32(const MlpSmem &S, const uint32_t (*sX
 
 constexpr int kPredWarps = 4;
 
-// One kernel per SHAKE solve: each lane computes one constraint's features
-// (written out for the recorder, with t1 and the scale), and with `infer`
-// the warp runs the network on its 32 constraints and writes the predicted
-// multipliers lam0 = (t1 + y t_scale + t_mean) / scale.
+// Pass 1, one thread per constraint: its own features 0-7, t1, the scale and
+// the reference bond direction, each computed once (the FP64 part).
+__global__ void __launch_bounds__(256) ws_own_kernel(WsFeatureArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n_constr) return;
+    float f[8];
+    double t1, scale;
+    own_features(a, k, f, t1, scale);
+    float *fo = a.feat + (size_t)k * kIn;
+#pragma unroll
+    for (int q = 0; q < 8; q++) fo[q] = f[q];
+    a.t1[k] = t1;
+    a.scale[k] = scale;
+    float ux, uy, uz;
+    ref_unit(a, k, ux, uy, uz);
+    a.unit[k] = make_float4(ux, uy, uz, 0.f);
+}
+
+// Pass 2: each lane takes one constraint's coupling features 8-11 (written
+// out for the recorder), and with `infer` the warp runs the network on its 32
+// constraints and writes the predicted multipliers
+// lam0 = (t1 + y t_scale + t_mean) / scale.
 __global__ void __launch_bounds__(kPredWarps * 32) ws_predict_kernel(WsFeatureArgs a, const float *__restrict__ P,
                                                                    const float *__restrict__ norm, double *lam0,
                                                                    int infer) {
@@ -271,13 +289,14 @@ __global__ void __launch_bounds__(kPredWarps * 32) ws_predict_kernel(WsFeatureAr
         for (int q = 0; q < kIn; q++) f[q] = 0.0f;
         double t1 = 0.0, scale = 1.0;
         if (live) {
-            own_features(a, k, f, t1, scale);
-            coupling_features(a, k, f);
             float *fo = a.feat + (size_t)k * kIn;
 #pragma unroll
-            for (int q = 0; q < kIn; q++) fo[q] = f[q];
-            a.t1[k] = t1;
-            a.scale[k] = scale;
+            for (int q = 0; q < 8; q++) f[q] = fo[q];
+            coupling_features(a, k, f);
+#pragma unroll
+            for (int q = 8; q < kIn; q++) fo[q] = f[q];
+            t1 = a.t1[k];
+            scale = a.scale[k];
         }
         if (!infer) continue;  // warp-uniform
 #pragma unroll
@@ -717,6 +736,7 @@ int gm_ws_predict_blocks(int n_constr) {
 void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
                           cudaStream_t s) {
     if (a.n_constr == 0) return;
+    ws_own_kernel<<<(a.n_constr + 255) / 256, 256, 0, s>>>(a);
     ws_predict_kernel<<<gm_ws_predict_blocks(a.n_constr), kPredWarps * 32, 0, s>>>(a, params, norm, lam0,
                                                                                   infer ? 1 : 0);
 }
