@@ -37,11 +37,11 @@ METRIC = "ns/day & pairs/s at 50k atoms: mixed vs FP64 GPU path at ≤1e-5 rel f
 PHYS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
             scale14_lj=0.5, scale14_coul=1.0 / 1.2, max_constr_iter=100, constr_tol=1e-10)
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
-# DRAM bytes (read + write) per launch of the FP32 pair kernel per half-list
+# DRAM bytes (read + write) per launch of the mixed pair kernel per half-list
 # pair, from one ncu capture of the 50k workload at its minimised start
-# (93,724,416 + 3,199,744 B for 10,067,070 pairs); traffic grows with the
+# (93,729,280 + 2,589,952 B for 10,067,070 pairs); traffic grows with the
 # pair count, so the bench scales it to its own count
-PAIR_TRAFFIC_PER_PAIR = 96_924_160 / 10_067_070
+PAIR_TRAFFIC_PER_PAIR = 96_319_232 / 10_067_070
 
 
 def ns_per_day(steps, seconds):
@@ -328,7 +328,7 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
                      "peak_source": peak_kind,
-                     "kernel": "pair_kernel_f32", "algorithmic_bytes": alg_bytes},
+                     "kernel": "pair_kernel_mixed", "algorithmic_bytes": alg_bytes},
         "e2e": {"value": round(ns_per_day(n_e2e, t_e2e), 3), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
         "gpu_launches": int(result["launches"]),

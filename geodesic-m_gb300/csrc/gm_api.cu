@@ -103,6 +103,7 @@ struct gm_ctx {
     int ws_rec_stride = 0, ws_rec_cap = 0;
     int *d_atom_cstart = nullptr, *d_atom_cref = nullptr;
     float4 *d_ws_unit = nullptr;
+    float *d_ws_w = nullptr;
     float *d_ws_params = nullptr, *d_ws_norm = nullptr, *d_ws_m = nullptr, *d_ws_v = nullptr, *d_ws_feat = nullptr,
           *d_rec_feat = nullptr, *d_rec_t = nullptr, *d_ws_partial = nullptr, *d_ws_out = nullptr;
     double *d_ws_scale = nullptr, *d_ws_t1 = nullptr, *d_ws_lam0 = nullptr, *d_lam_sum = nullptr,
@@ -360,7 +361,7 @@ long long issue_shake(gm_ctx *c, cudaStream_t s, bool resident) {
         f.n_constr = c->n_constr; f.n_atoms = c->n;
         f.constr_i = c->d_ci; f.constr_j = c->d_cj; f.constr_dsq = c->d_cdsq; f.inv_mass = c->d_inv_mass;
         f.atom_cstart = c->d_atom_cstart; f.atom_cref = c->d_atom_cref; f.pos = c->d_pos; f.dref = c->d_dref;
-        f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1; f.unit = c->d_ws_unit;
+        f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1; f.unit = c->d_ws_unit; f.w = c->d_ws_w;
         gm_launch_ws_predict(f, c->d_ws_params, c->d_ws_norm, c->d_ws_lam0, c->ws_on, s);
         k += 2;
     }
@@ -1356,6 +1357,13 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
         TRY(dalloc(c, &c->d_ws_t1, (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_ws_feat, (size_t)GM_WS_IN * c->n_constr));
         TRY(dalloc(c, &c->d_ws_unit, (size_t)c->n_constr));
+        {
+            // FP32 1/m_i + 1/m_j per constraint, for the warm start's features
+            std::vector<float> w((size_t)c->n_constr);
+            for (int k = 0; k < c->n_constr; k++)
+                w[(size_t)k] = (float)inv_mass[(size_t)c->h_ci[(size_t)k]] + (float)inv_mass[(size_t)c->h_cj[(size_t)k]];
+            TRY(dupload(c, &c->d_ws_w, w.data(), w.size()));
+        }
         TRY(dalloc(c, &c->d_rvec, 3 * (size_t)c->n_constr));
         TRY(dalloc(c, &c->d_cl_iters, (size_t)c->n_clusters));
         TRY(dalloc(c, &c->d_cl_worst, (size_t)c->n_clusters));

@@ -420,7 +420,8 @@ struct WsFeatureArgs {
     float *feat;                 // [n_constr][12] raw features
     double *scale;               // 2 (1/m_i + 1/m_j) per constraint
     double *t1;                  // first Jacobi step of a cold solve, times scale
-    float4 *unit;                // reference bond direction per constraint (FP32), for the coupling pass
+    float4 *unit;                // (reference bond direction, t1) per constraint (FP32), for the coupling pass
+    const float *w;              // 1/m_i + 1/m_j per constraint, FP32 (each mass rounded first)
 };
 // Two launches per solve: every constraint's raw features, t1 and scale, and
 // with infer the network on the tensor cores (fused with the coupling pass)

@@ -55,45 +55,43 @@ __device__ __forceinline__ void ref_unit(const WsFeatureArgs &a, int k, float &u
     uz = __fmul_rn(rz, il);
 }
 
-// t1 = (|r_trial|^2 - d0^2) / (r_trial . r_ref) of constraint k, FP64.
-__device__ __forceinline__ double t1_of(const WsFeatureArgs &a, int k, double *t2o = nullptr, double *dro = nullptr) {
+// The constraint's own features 0-7, its t1 and its scale 2 (1/m_i + 1/m_j).
+// FP64 only where it cancels: the coordinate differences, |r_trial|^2 - d0^2
+// and r_trial . r_ref; each is then rounded once to FP32, and the ratios,
+// t1 = (|r_trial|^2 - d0^2) / (r_trial . r_ref) and d0 are correctly rounded
+// FP32 operations (the network's inputs are FP32, and t1 only seeds the
+// solve, which then iterates to the unchanged tolerance).
+__device__ __forceinline__ void own_features(const WsFeatureArgs &a, int k, float *f, double &t1, double &scale) {
     const int i = a.constr_i[k], j = a.constr_j[k], n = a.n_atoms;
     const double d0sq = a.constr_dsq[k];
     const double rx = __dsub_rn(a.dref[i], a.dref[j]), ry = __dsub_rn(a.dref[n + i], a.dref[n + j]),
                  rz = __dsub_rn(a.dref[2 * n + i], a.dref[2 * n + j]);
     const double tx = __dsub_rn(a.pos[i], a.pos[j]), ty = __dsub_rn(a.pos[n + i], a.pos[n + j]),
                  tz = __dsub_rn(a.pos[2 * n + i], a.pos[2 * n + j]);
-    const double t2 = dot3(tx, ty, tz, tx, ty, tz);
-    const double dr = dot3(tx, ty, tz, rx, ry, rz);
-    if (t2o) *t2o = t2;
-    if (dro) *dro = dr;
-    return dr == 0.0 ? 0.0 : __ddiv_rn(__dsub_rn(t2, d0sq), dr);
-}
-
-// The constraint's own features 0-7, its t1 and its scale 2 (1/m_i + 1/m_j).
-__device__ __forceinline__ void own_features(const WsFeatureArgs &a, int k, float *f, double &t1, double &scale) {
-    const int i = a.constr_i[k], j = a.constr_j[k];
-    const double d0sq = a.constr_dsq[k];
-    double t2, dr;
-    t1 = t1_of(a, k, &t2, &dr);
+    const float num = (float)__dsub_rn(dot3(tx, ty, tz, tx, ty, tz), d0sq);
+    const float dr = (float)dot3(tx, ty, tz, rx, ry, rz);
+    const float d0f = (float)d0sq;
+    const float t1f = dr == 0.0f ? 0.0f : __fdiv_rn(num, dr);
+    t1 = (double)t1f;
     scale = __dmul_rn(2.0, __dadd_rn(a.inv_mass[i], a.inv_mass[j]));
-    f[0] = (float)__ddiv_rn(__dsub_rn(t2, d0sq), d0sq);
-    f[1] = (float)__ddiv_rn(dr, d0sq);
-    f[2] = (float)__dsqrt_rn(d0sq);
+    f[0] = __fdiv_rn(num, d0f);
+    f[1] = __fdiv_rn(dr, d0f);
+    f[2] = __fsqrt_rn(d0f);
     f[3] = (float)a.inv_mass[i];
     f[4] = (float)a.inv_mass[j];
     f[5] = (float)(a.atom_cstart[i + 1] - a.atom_cstart[i]);
     f[6] = (float)(a.atom_cstart[j + 1] - a.atom_cstart[j]);
-    f[7] = (float)t1;
+    f[7] = t1f;
 }
 
 // Coupling to the other constraints on the constraint's two atoms (features
 // 8-11) in FP32, atom i's constraints then atom j's, each ascending; masses
-// and the neighbours' t1 enter rounded to FP32.  Reads every constraint's t1
-// and reference direction from the first pass.
+// and the neighbours' t1 enter rounded to FP32.  Reads every constraint's
+// (reference direction, t1) from the first pass and its FP32 inverse-mass sum
+// w (two independent loads per neighbour).
 __device__ __forceinline__ void coupling_features(const WsFeatureArgs &a, int k, float *f) {
     const int ends[2] = {a.constr_i[k], a.constr_j[k]};
-    const float wk = __fadd_rn((float)a.inv_mass[ends[0]], (float)a.inv_mass[ends[1]]);
+    const float wk = a.w[k];
     const float4 uk = a.unit[k];
     const float ux = uk.x, uy = uk.y, uz = uk.z;
     float c1 = 0.0f, c2 = 0.0f, cmax = 0.0f, ct = 0.0f;
@@ -108,9 +106,9 @@ __device__ __forceinline__ void coupling_features(const WsFeatureArgs &a, int k,
             const float sl = ref >= 0 ? 1.0f : -1.0f;
             const float4 ul = a.unit[l];
             const float cs = dot3f(ux, uy, uz, ul.x, ul.y, ul.z);
-            const float wl = __fadd_rn((float)a.inv_mass[a.constr_i[l]], (float)a.inv_mass[a.constr_j[l]]);
+            const float wl = a.w[l];
             const float coup = __fmul_rn(__fmul_rn(__fdiv_rn(inv_a, wk), cs), __fmul_rn(sk, sl));
-            const float tl = (float)a.t1[l];
+            const float tl = ul.w;
             c1 = __fadd_rn(c1, __fdiv_rn(__fmul_rn(__fmul_rn(coup, tl), wk), wl));
             c2 = __fadd_rn(c2, __fmul_rn(coup, coup));
             cmax = fmaxf(cmax, fabsf(cs));
@@ -264,7 +262,7 @@ __global__ void __launch_bounds__(256) ws_own_kernel(WsFeatureArgs a) {
     a.scale[k] = scale;
     float ux, uy, uz;
     ref_unit(a, k, ux, uy, uz);
-    a.unit[k] = make_float4(ux, uy, uz, 0.f);
+    a.unit[k] = make_float4(ux, uy, uz, f[7]);
 }
 
 // Pass 2: each lane takes one constraint's coupling features 8-11 (written

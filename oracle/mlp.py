@@ -48,9 +48,11 @@ def features(constr_i, constr_j, dsq, pos, ref, inv_mass):
       9 sum of the squared coupling coefficients   10 max |cos|   11 sum t1_l
 
     (s = +1 where a is the constraint's i, -1 where it is its j; w = 1/m_i +
-    1/m_j.)  Features 0-7 from FP64 operations rounded once, 8-11 in FP32
-    (masses, t1 and the FP64 bond vectors rounded to FP32 first), in the
-    device's order: atom i's constraints, then atom j's, each ascending."""
+    1/m_j.)  FP64 only where it cancels: the coordinate differences,
+    |d|^2 - d0^2 and d . r, each rounded once to FP32; the ratios, t1 and d0
+    are correctly rounded FP32 operations.  Features 8-11 in FP32 (masses, t1
+    and the FP64 bond vectors rounded to FP32 first), in the device's order:
+    atom i's constraints, then atom j's, each ascending."""
     ci = [int(v) for v in constr_i]
     cj = [int(v) for v in constr_j]
     dsq = [float(v) for v in dsq]
@@ -82,12 +84,13 @@ def features(constr_i, constr_j, dsq, pos, ref, inv_mass):
         i, j = ci[k], cj[k]
         rx, ry, rz = RX[i] - RX[j], RY[i] - RY[j], RZ[i] - RZ[j]
         tx, ty, tz = X[i] - X[j], Y[i] - Y[j], Z[i] - Z[j]
-        t2 = dot3(tx, ty, tz, tx, ty, tz)
-        dr = dot3(tx, ty, tz, rx, ry, rz)
-        t1[k] = 0.0 if dr == 0.0 else (t2 - dsq[k]) / dr
+        num = f32(dot3(tx, ty, tz, tx, ty, tz) - dsq[k])
+        dr = f32(dot3(tx, ty, tz, rx, ry, rz))
+        d0f = f32(dsq[k])
+        t1f = f32(0.0) if dr == 0.0 else num / dr
+        t1[k] = float(t1f)
         scale[k] = 2.0 * (inv[i] + inv[j])
-        f[k, :8] = [(t2 - dsq[k]) / dsq[k], dr / dsq[k], np.sqrt(dsq[k]), inv[i], inv[j], len(rows[i]),
-                    len(rows[j]), t1[k]]
+        f[k, :8] = [num / d0f, dr / d0f, np.sqrt(d0f), inv[i], inv[j], len(rows[i]), len(rows[j]), t1f]
     for k in range(C):
         wk = f32(inv[ci[k]]) + f32(inv[cj[k]])
         ux, uy, uz = unit(k)
