@@ -804,6 +804,7 @@ int stage_positions(gm_ctx *c, const double *px, const double *py, const double 
     GM_CUDA(c, cudaMemcpyAsync(&c->h_status->differs, &c->d_status->differs, sizeof(unsigned int),
                                cudaMemcpyDeviceToHost, c->stream));
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->h_status->differs & 2u) return fail(c, GM_ERR_NONFINITE, "non-finite position");
     if (c->h_status->differs) {
         c->forces_current = false;
         GM_CUDA(c, cudaMemcpyAsync(c->d_pos, c->d_dref, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToDevice,
@@ -1856,7 +1857,10 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
     // the call's rebuild base are set on the device.
     if (!c || !(dt > 0) || n_steps < 0) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
-    if (!finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position");
+    // positions are checked for finiteness on the device when the resident
+    // forces are current (the comparison kernel reads them anyway), on the
+    // host otherwise
+    if (!c->forces_current && !finite3(px, py, pz, c->n)) return fail(c, GM_ERR_NONFINITE, "non-finite position");
     if (!c->d_list) {
         int rc = ensure_estimated_buffers(c, px, py, pz);
         if (rc) return rc;

@@ -908,11 +908,18 @@ __global__ void kinetic_final(const double *partial, int blocks, double *out) {
     *out = 0.5 * sum * (1.0 / (20.455 * 20.455));  // lib.rs:25,76
 }
 
+// flag |= 1 when a differs from b anywhere (bit for bit), |= 2 when a holds
+// a non-finite value
 __global__ void differs_kernel(int n3, const double *a, const double *b, unsigned int *flag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int d = 0;
-    if (i < n3) d = __double_as_longlong(a[i]) != __double_as_longlong(b[i]);
-    if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(flag, 1u);
+    int d = 0, bad = 0;
+    if (i < n3) {
+        d = __double_as_longlong(a[i]) != __double_as_longlong(b[i]);
+        bad = !isfinite(a[i]);
+    }
+    d = __syncthreads_or(d);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0 && (d || bad)) atomicOr(flag, (d ? 1u : 0u) | (bad ? 2u : 0u));
 }
 
 __global__ void status_reset_kernel(DevStatus *st, int set_step, unsigned long long step) {

@@ -81,3 +81,20 @@ def test_fixed_point_overflow_gives_nan_forces(precision):
     f = be.compute_forces(ok)
     assert np.all(np.isfinite(f)) and f[0, 0] == -f[0, 1]
     be.close()
+
+
+def test_nonfinite_position_in_a_resident_call():
+    """gm_steps checks the caller's positions on the device when the resident
+    forces are current: a NaN is NumericalError (lib.rs:94-107), and the
+    context carries on with valid positions afterwards."""
+    atoms, pos = inert_gas(400, 0.05, seed=9)
+    vel = np.ascontiguousarray(np.zeros_like(pos))
+    be = backend.CudaBackend(atoms, amber.BondedTopology.empty(), backend.SimParams(**PARAMS))
+    be.steps(pos, vel, 0.002, 3)
+    bad = pos.copy()
+    bad[1, 17] = np.nan
+    with pytest.raises(backend.NumericalError):
+        be.steps(bad, vel, 0.002, 1)
+    be.steps(pos, vel, 0.002, 2)
+    assert np.all(np.isfinite(pos))
+    be.close()
