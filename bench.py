@@ -37,6 +37,7 @@ METRIC = "ns/day & pairs/s at 50k atoms: mixed vs FP64 GPU path at ≤1e-5 rel f
 PHYS = dict(box_size=(10000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
             scale14_lj=0.5, scale14_coul=1.0 / 1.2, max_constr_iter=100, constr_tol=1e-10)
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+STEP_FORMS = {"graph": 0, "persistent": 1}  # gm_step_form: GM_STEP_GRAPH, GM_STEP_PERSISTENT
 # DRAM bytes (read + write) per launch of the mixed pair kernel per half-list
 # pair, from one ncu capture of the 50k workload at its minimised start
 # (93,729,280 + 2,589,952 B for 10,067,070 pairs); traffic grows with the
@@ -179,6 +180,9 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     prec = backend.PRECISION_FP64 if args.precision == "fp64" else backend.PRECISION_MIXED
     p = backend.SimParams(precision=prec, device=dev, **PHYS)
     be = backend.CudaBackend(atoms, topo, p)
+    form = STEP_FORMS[args.step_form]
+    if prec == backend.PRECISION_MIXED:
+        be.step_form(form)
     be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
     be.forces_resident()
     if args.pair_shape:
@@ -222,6 +226,14 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     n_bb = 1000
     t_bb = be.time_steps(DT_PS, n_bb, first_step=args.warmup + args.steps) / 1e3
     reb_bb = be.counters()["rebuilds"] - cb0["rebuilds"]
+    # the other step form on the same state, the same number of flushed steps
+    other = "persistent" if args.step_form == "graph" else "graph"
+    be.step_form(STEP_FORMS[other])
+    be.run_resident(DT_PS, 3)
+    be.synchronize()
+    t_other = be.time_steps(DT_PS, args.steps, first_step=args.warmup + args.steps + n_bb + 3,
+                            flush_ptr=flush.data_ptr(), flush_bytes=L2_FLUSH_BYTES) / 1e3
+    be.step_form(form)
     # roofline of the pair kernel: algorithmic bytes 4 P + 52 N per launch (one
     # int32 index per half-list pair of neighbor.rs:25-43, plus per atom the
     # coordinates, charge, type, force and energy of force/nonbonded.rs:20-82)
@@ -321,6 +333,10 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
         "steady_state": {"ns_per_day": round(ns_per_day(n_bb, t_bb), 3), "steps": n_bb,
                          "ms_per_step": round(1e3 * t_bb / n_bb, 5), "list_rebuilds": int(reb_bb),
                          "note": "back to back, no L2 flush, list rebuilds included (amortised)"},
+        "step_form": args.step_form,
+        "other_step_form": {"form": other, "ns_per_day": round(ns_per_day(args.steps, t_other), 3),
+                            "ms_per_step": round(1e3 * t_other / args.steps, 5),
+                            "note": "same flushed timing, later in the same run"},
         "errors_vs_fp64_oracle": errs,
         "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
                       "pair14": round(t_pair14 * 1e3, 5), "forces": round(t_forces * 1e3, 5),
@@ -442,6 +458,21 @@ def _clock_ok(clk):
     return {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons") if k in clk}
 
 
+def _time_batch(be, args, flush, form):
+    """Resident batch steps in one step form from the state the context
+    holds: warm-up, then args.steps flushed timed steps."""
+    from geodesic_cuda import backend
+    be.step_form(form)
+    be.run_resident(DT_PS, args.warmup)
+    be.synchronize()
+    c0 = be.counters()
+    with ClockSampler(0) as clk:
+        dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
+                               flush_bytes=L2_FLUSH_BYTES)
+    c1 = be.counters()
+    return dev_ms / 1e3, c1["rebuilds"] - c0["rebuilds"], int(c1["launches"] - c0["launches"]), clk.summary()
+
+
 def run_ensemble(args):
     """configs[3]: 256 independent systems, N log-uniform in [500, 20000],
     per-system seeds, MB 300 K, mixed precision: one context, one graph
@@ -467,16 +498,15 @@ def run_ensemble(args):
     be.upload_state(pos, vel)
     be.forces_resident()
     choice = be.autotune(reps=3)
-    be.run_resident(DT_PS, args.warmup)
-    be.synchronize()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
-    c0 = be.counters()
-    with ClockSampler(0) as clk:
-        dev_ms = be.time_steps(DT_PS, args.steps, first_step=args.warmup, flush_ptr=flush.data_ptr(),
-                               flush_bytes=L2_FLUSH_BYTES)
-    c1 = be.counters()
-    sec = dev_ms / 1e3
+    # the whole batch as one persistent launch per step, then the same start
+    # state as the kernel graph
+    sec, reb, launches, clk = _time_batch(be, args, flush, backend.STEP_PERSISTENT)
+    be.upload_state(pos, vel)
+    be.forces_resident()
+    sec_g, reb_g, _, clk_g = _time_batch(be, args, flush, backend.STEP_GRAPH)
     batched = n_sys * ns_per_day(args.steps, sec)
+    batched_graph = n_sys * ns_per_day(args.steps, sec_g)
     be.close()
     # one by one: each system alone, its own context and graph
     k1 = max(20, min(args.steps, args.single_steps))
@@ -500,11 +530,14 @@ def run_ensemble(args):
                                    f"(total {int(sizes.sum())} atoms), per-system seeds, MB 300 K, 2 fs, "
                                    "FIRE 200 iterations", "n_systems": n_sys, "total_atoms": int(sizes.sum()),
                        "l2": "flushed between timed steps"},
+            "step_form": "persistent (one cooperative launch per batch step, rebuild in the graph's IF node)",
             "one_by_one_ns_per_day": round(one_by_one, 2), "batched_over_one_by_one": round(batched / one_by_one, 2),
             "one_by_one_sample": f"{k1} timed steps per system after {args.warmup} warm-up steps, summed",
-            "autotuner": choice, "list_rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
-            "gpu_launches": int(c1["launches"] - c0["launches"]), "generation_s": round(t_gen, 1),
-            "clocks": _clock_ok(clk.summary())}
+            "kernel_graph_form": {"ns_per_day": round(batched_graph, 2), "ms_per_step": round(1e3 * sec_g / args.steps, 4),
+                                  "list_rebuilds_in_timed_region": reb_g, "clocks": _clock_ok(clk_g)},
+            "autotuner": choice, "list_rebuilds_in_timed_region": reb,
+            "gpu_launches": launches, "generation_s": round(t_gen, 1),
+            "clocks": _clock_ok(clk)}
 
 
 def run_warm_start(args):
@@ -671,6 +704,8 @@ def main():
                     help="timed steps only (no error, CPU-baseline, FP64 or e2e legs); for profiler runs")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="with --quick: the precision of the timed steps")
+    ap.add_argument("--step-form", choices=["graph", "persistent"], default="graph",
+                    help="unconstrained mixed-precision steps: the kernel graph, or one persistent launch per step")
     ap.add_argument("--pair-shape", default="",
                     help="SPLIT,WARPS,GRID: the pair kernel's launch shape instead of the autotuner's choice")
     ap.add_argument("--config", default="headline",

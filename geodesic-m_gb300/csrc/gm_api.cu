@@ -129,6 +129,11 @@ struct gm_ctx {
     long long launches_per_step = 0;
     bool forces_current = false;
     bool use_graph = true;           // GM_GRAPH=0: direct launches (profilers)
+    // step form of unconstrained mixed-precision runs: 0 the kernel graph,
+    // 1 one persistent cooperative launch per step (gm_step.cu)
+    int step_form = 0;
+    int persist_blocks = 0;          // its grid: every block resident
+    StepSync *d_sync = nullptr;
     long long rebuild_base = 0;
     unsigned last_shake_T = 0, last_rattle_T = 0;
 };
@@ -538,6 +543,8 @@ int status_result(gm_ctx *c, gm_convergence *conv) {
                     "non-periodic system extent plus the list radius reaches half the box: the reference's "
                     "min-image would fold pairs; use a larger box");
     if (e & GM_DEV_CELL_OVERFLOW) return fail(c, GM_ERR_UNSUPPORTED, "cell grid overflow");
+    if (e & GM_DEV_BARRIER_TIMEOUT)
+        return fail(c, GM_ERR_DEVICE, "a grid barrier of the persistent step kernel timed out");
     if (e & GM_DEV_ITER_MISMATCH)
         return fail(c, GM_ERR_UNSUPPORTED, "constraint cluster iteration counts disagree with the global stop rule");
     return fail(c, GM_ERR_DEVICE, "device status 0x%x", e);
@@ -672,6 +679,42 @@ int download3(gm_ctx *c, const double *src, double *x, double *y, double *z) {
     return GM_OK;
 }
 
+// The persistent form runs unconstrained mixed-precision steps without
+// trajectory frames (frames record each step's energy, which its launches do
+// not sum).
+bool persistent_form(const gm_ctx *c) {
+    return c->step_form == 1 && !c->fp64 && c->n_clusters == 0 && c->frame_interval == 0 && c->n > 0;
+}
+
+// Before the first persistent launch of a call: clear the barrier and queue
+// words.  `fresh`: the force sums hold the forces at the resident positions
+// (the first launch skips its force phase); otherwise they are zeroed and
+// the first launch evaluates them (timed steps each evaluate their forces).
+int persistent_grid(gm_ctx *c) {
+    if (c->persist_blocks) return GM_OK;
+    c->persist_blocks = gm_step_persistent_blocks(force_args(c));
+    if (c->persist_blocks > 0) return GM_OK;
+    c->persist_blocks = 0;
+    return fail(c, GM_ERR_DEVICE, "persistent step kernel: no block fits on an SM");
+}
+
+int begin_persistent(gm_ctx *c, bool fresh) {
+    int rc = persistent_grid(c);
+    if (rc) return rc;
+    GM_CUDA(c, cudaMemsetAsync(c->d_sync, 0, sizeof(StepSync), c->stream));
+    if (fresh) GM_CUDA(c, cudaMemsetAsync(&c->d_sync->fresh, 1, 1, c->stream));
+    else GM_CUDA(c, cudaMemsetAsync(c->d_force, 0, sizeof(long long) * 3 * (size_t)c->n, c->stream));
+    return GM_OK;
+}
+
+// After the last persistent launch of a call: the forces at the final
+// positions, by the force kernels (the launches left the coordinates packed).
+int end_persistent(gm_ctx *c) {
+    c->launches += seq_forces(c, c->stream, false, c->side, true);
+    GM_CUDA(c, cudaGetLastError());
+    return GM_OK;
+}
+
 // One BAB + RATTLE step (lib.rs:292-323) issued on stream s.  With a graph
 // conditional handle the rebuild runs inside an IF node; otherwise the check
 // result is read back on the host.
@@ -680,6 +723,28 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
     const int n = c->n;
     const bool constrained = c->n_clusters > 0;
     const double half_skin = (c->p.r_skin - c->p.r_cutoff) / 2.0;  // neighbor.rs:61-62
+    if (persistent_form(c)) {
+        // forces at the resident positions, kick, drift, check and pack in
+        // one launch; the rebuild follows in the IF node
+        StepArgs sa{};
+        sa.n = n;
+        sa.pos = c->d_pos;
+        sa.vel = c->d_vel;
+        sa.dref = c->d_dref;
+        sa.inv_mass = c->d_inv_mass;
+        sa.ref = c->d_ref;
+        sa.dt_half = dt / 2.0;
+        sa.dt = dt;
+        sa.inv_dt = 1.0 / dt;
+        sa.thr_sq = half_skin * half_skin;
+        sa.cond = cond;
+        sa.atom_sys = c->d_atom_sys;
+        sa.sys_flag = c->d_sys_flag;
+        sa.sync = c->d_sync;
+        gm_launch_step_persistent(force_args(c), sa, pack_args(c), c->persist_blocks, s);
+        *count += 1;
+        return GM_OK;
+    }
     if (!constrained) {
         gm_launch_kick_drift_check(n, c->d_pos, c->d_vel, c->d_dref, c->d_force, c->d_inv_mass, dt / 2.0, dt, c->d_ref,
                                    half_skin * half_skin, c->d_status, cond, c->d_atom_sys, c->d_sys_flag,
@@ -699,6 +764,7 @@ int issue_step(gm_ctx *c, cudaStream_t s, double dt, unsigned long long cond, lo
 }
 
 int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
+    if (persistent_form(c)) return GM_OK;  // the next launch evaluates the forces
     long long k = seq_forces(c, s, false, c->side, c->n_clusters == 0);
     if (c->n_clusters) {
         gm_launch_half_kick(c->n, c->d_vel, c->d_force, c->d_inv_mass, dt / 2.0, c->d_status, s); k++;
@@ -728,6 +794,10 @@ int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
 
 int capture_graph(gm_ctx *c, double dt) {
     if (c->graph_exec && c->graph_dt == dt && c->graph_cap == c->cap) return GM_OK;
+    if (persistent_form(c)) {
+        int rc = persistent_grid(c);  // the grid size goes into the captured launch
+        if (rc) return rc;
+    }
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
     cudaGraph_t g;
@@ -780,15 +850,19 @@ int run_direct(gm_ctx *c, double dt, int64_t n_steps);
 // n resident steps (one graph launch each, or direct launches), then the
 // closing half-kick; nothing waits for the device.
 int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
-    if (!c->use_graph) {
-        int rc = run_direct(c, dt, n_steps);
-        return rc ? rc : finish_steps(c, dt);
-    }
-    int rc = capture_graph(c, dt);
+    const bool pf = persistent_form(c) && n_steps > 0;
+    int rc = pf ? begin_persistent(c, true) : GM_OK;
     if (rc) return rc;
-    for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
-    c->launches += c->launches_per_step * n_steps;
-    return finish_steps(c, dt);
+    if (!c->use_graph) {
+        rc = run_direct(c, dt, n_steps);
+    } else {
+        rc = capture_graph(c, dt);
+        if (rc) return rc;
+        for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        c->launches += c->launches_per_step * n_steps;
+    }
+    if (!rc && pf) rc = end_persistent(c);
+    return rc ? rc : finish_steps(c, dt);
 }
 
 // Caller positions into the context.  When the resident forces are current
@@ -1463,6 +1537,8 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dalloc(c, &c->d_kin_part, 256));
     TRY(dalloc(c, &c->d_ke, 1));
     TRY(dalloc(c, &c->d_status, 1));
+    TRY(dalloc(c, &c->d_sync, 1));
+    if (cudaMemset(c->d_sync, 0, sizeof(StepSync)) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaMallocHost((void **)&c->h_status, sizeof(DevStatus)) != cudaSuccess) return bail(GM_ERR_OUT_OF_MEMORY);
     DevStatus z{};
     z.fail_step = ~0ull;
@@ -1730,7 +1806,12 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
     double total = 0.0;
     ForceArgs fa = force_args(c);
     ListArgs la = list_args(c);
+    const bool pf = which == 3 && persistent_form(c);
     for (int k = 0; k < n_iter; k++) {
+        if (pf) {
+            rc = begin_persistent(c, false);  // the timed launch evaluates its forces
+            if (rc) return rc;
+        }
         cudaEventRecord(e0, c->stream);
         switch (which) {
             case 0: gm_launch_pair(fa, c->fp64, c->stream); break;
@@ -1755,7 +1836,9 @@ int32_t gm_profile(gm_ctx *c, int32_t which, int32_t n_iter, double dt, double *
         cudaEventElapsedTime(&ms, e0, e1);
         total += ms;
         if (which == 3) {
-            rc = finish_steps(c, dt);  // outside the timed span, as after a run
+            // outside the timed span, as after a run
+            rc = pf ? end_persistent(c) : GM_OK;
+            if (!rc) rc = finish_steps(c, dt);
             if (rc) return rc;
         }
     }
@@ -1807,6 +1890,9 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
     if (!rc) rc = set_step(c, first_step);
     if (!rc) rc = ensure_forces(c);
     if (!rc && c->use_graph) rc = capture_graph(c, dt);
+    // every timed persistent launch evaluates its forces
+    const bool pf = persistent_form(c);
+    if (!rc && pf) rc = begin_persistent(c, false);
     if (rc) return rc;
     std::vector<cudaEvent_t> ev((size_t)(2 * n_steps));
     for (auto &e : ev) GM_CUDA(c, cudaEventCreate(&e));
@@ -1826,7 +1912,8 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
             GM_CUDA(c, cudaMemsetAsync(flush_buf, (int)((k + 1) & 0xff), (size_t)flush_bytes, c->stream));
     }
     if (c->use_graph) c->launches += c->launches_per_step * n_steps;
-    rc = finish_steps(c, dt);
+    if (pf) rc = end_persistent(c);
+    if (!rc) rc = finish_steps(c, dt);
     if (rc) return rc;
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     double total = 0.0;
@@ -2201,6 +2288,17 @@ int32_t gm_pair_shape(gm_ctx *c, int32_t split, int32_t warps_per_block, int32_t
     c->pair_warps = warps_per_block;
     c->pair_grid = grid;
     drop_graph(c);  // the captured step holds the old launch shape
+    return GM_OK;
+}
+
+int32_t gm_step_form(gm_ctx *c, int32_t form) {
+    if (!c || (form != GM_STEP_GRAPH && form != GM_STEP_PERSISTENT)) return GM_ERR_INVALID_ARGUMENT;
+    if (form == GM_STEP_PERSISTENT && (c->fp64 || c->n_clusters > 0))
+        return fail(c, GM_ERR_UNSUPPORTED, "the persistent step form runs unconstrained mixed-precision contexts");
+    if (form != c->step_form) {
+        c->step_form = form;
+        drop_graph(c);  // the captured step is the other form's
+    }
     return GM_OK;
 }
 

@@ -22,7 +22,7 @@
 
 namespace {
 
-constexpr double kForceToAccel = 20.455 * 20.455;  // integrator.rs:9
+constexpr double kForceToAccel = GM_FORCE_TO_ACCEL;  // integrator.rs:9
 
 __global__ void half_kick_kernel(int n, double *vel, const long long *force, const double *inv_mass, double dt_half,
                                  const DevStatus *st) {

@@ -25,6 +25,7 @@
 
 #define GM_FIX_SCALE 1099511627776.0        // 2^40
 #define GM_FIX_INV (1.0 / 1099511627776.0)  // 2^-40
+constexpr double GM_FORCE_TO_ACCEL = 20.455 * 20.455;  // kcal/mol/A/amu -> A/ps^2 (integrator.rs:9)
 #define GM_FIX_SCALE_F 1099511627776.0f
 #define GM_FIX_LIMIT 4194304.0              // 2^22: |contribution| must stay below
 
@@ -59,6 +60,7 @@ enum : unsigned int {
     GM_DEV_EXTENT = 1u << 6,       // non-periodic extent too large for min-image
     GM_DEV_CELL_OVERFLOW = 1u << 7,
     GM_DEV_ITER_MISMATCH = 1u << 8,
+    GM_DEV_BARRIER_TIMEOUT = 1u << 9,  // a grid barrier of the persistent step kernel gave up waiting
 };
 
 struct DevStatus {
@@ -355,6 +357,30 @@ struct PackArgs {
     const double *charge64;
     int fp64;
 };
+// The persistent step kernel (gm_step.cu): one cooperative launch per
+// unconstrained mixed-precision step.  Its force phase hands out work items
+// (pair items and 32-term bonded / 1-4 chunks) from `ticket`; one grid
+// barrier separates it from the kick / drift / rebuild check / pack phase.
+struct StepSync {
+    unsigned int arrive;  // blocks arrived at the grid barrier
+    unsigned int gen;     // barrier generation
+    unsigned int ticket;  // next work item of the force phase
+    unsigned int fresh;   // nonzero: the forces at the current positions are summed already (skip the phase)
+};
+struct StepArgs {
+    int n;
+    double *pos, *vel, *dref;
+    const double *inv_mass, *ref;
+    double dt_half, dt, inv_dt, thr_sq;
+    unsigned long long cond;   // graph conditional handle of the rebuild, or 0
+    const int *atom_sys;
+    unsigned int *sys_flag;
+    StepSync *sync;
+};
+// Blocks of the cooperative grid (all co-resident); 0 when the form does not apply.
+int gm_step_persistent_blocks(const ForceArgs &fa);
+void gm_launch_step_persistent(const ForceArgs &fa, const StepArgs &sa, const PackArgs &pk, int blocks,
+                               cudaStream_t s);
 void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, long long *force,
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,

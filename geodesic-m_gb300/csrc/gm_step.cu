@@ -1,0 +1,232 @@
+// gm_step.cu — the unconstrained mixed-precision BAB step (lib.rs:292-323
+// without constraints) as one persistent cooperative launch per step.
+//
+// Launch k of a run starts from the positions x_k that launch k-1 left (and
+// the list that the graph's conditional rebuild left after it):
+//   1. forces F(x_k): every warp takes work items from one queue: the pair
+//      items of the mixed kernel (pair_item_mixed, a 32-atom group's share of
+//      list columns) and 32-term chunks of the bonded terms and 1-4 pairs,
+//      spread evenly through the queue so that each SM mixes FP32 pair work
+//      with FP64 bonded work.  Skipped when the forces at x_k are summed
+//      already (the first launch of a call: the call starts with current
+//      forces).
+//   2. one grid barrier (bounded: a block that waits too long records
+//      GM_DEV_BARRIER_TIMEOUT and returns).
+//   3. per atom, grid-strided: the closing half-kick of step k-1 (when
+//      pending) and the opening half-kick of step k with F(x_k), the drift to
+//      x_{k+1}, the velocity resync, the pack of x_{k+1}, the zeroing of the
+//      force sums and the rebuild check; the last block sets the graph's
+//      rebuild condition.
+// The graph that holds the launch has one more node, the IF node of the list
+// rebuild.  After the last launch of a call the forces F(x_n) are evaluated
+// by the force kernels and the closing half-kick by the tail kernel, as in
+// the kernel-graph form.
+//
+// The launch performs the kernel-graph form's operations in the same order:
+// force sums are integer sums (the order of the work items changes no bit),
+// and phase 3 is written with explicit round-to-nearest operations, so it
+// rounds like the integrator kernels, which are compiled without
+// contraction.  Energies are not summed inside the loop (only the force
+// phase after the last launch sums them), so the bonded chunks drop theirs.
+#include "gm_force_terms.cuh"
+
+namespace {
+
+constexpr int kStepThreads = 128;
+// ~64 ns per poll: about a quarter of a second before a block gives up
+constexpr unsigned kBarrierPolls = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier of a cooperative launch (every block is resident).  The
+// generation is read before arriving, the last block to arrive resets the
+// count and advances the generation.  Returns false (and records the
+// timeout) when the generation did not advance within kBarrierPolls polls.
+__device__ bool grid_barrier(StepSync *sy, DevStatus *st) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned g = ld_acquire(&sy->gen);
+        __threadfence();
+        if (atomicAdd(&sy->arrive, 1u) == gridDim.x - 1) {
+            atomicExch(&sy->arrive, 0u);
+            __threadfence();
+            atomicAdd(&sy->gen, 1u);
+        } else {
+            for (unsigned it = 0; ld_acquire(&sy->gen) == g; it++) {
+                if (it >= kBarrierPolls) {
+                    atomicOr(&st->error, (unsigned)GM_DEV_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <bool PERIODIC, bool COULOMB, bool BATCH, bool MI>
+__global__ void __launch_bounds__(kStepThreads) step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
+    extern __shared__ float4 s_tab[];
+    DevStatus *st = fa.status;
+    StepSync *sy = sa.sync;
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    // read by every block before the barrier; block 0 clears it after
+    const bool fresh = sy->fresh != 0;
+    // ---- 1. forces at the current positions
+    if (!fresh) {
+        if (!BATCH) {
+            for (int t = threadIdx.x; t < fa.ntypes * fa.ntypes; t += blockDim.x) s_tab[t] = fa.tab32[t];
+            __syncthreads();
+        }
+        const long long n_pair = (long long)fa.n_groups * fa.split;
+        const int cb = (fa.n_bonds + fa.n_angles + fa.n_diheds + 31) / 32, c14 = (fa.n14 + 31) / 32;
+        const long long nbw = (long long)cb + c14, total = n_pair + nbw;
+        for (;;) {
+            unsigned t = 0;
+            if (lane == 0) t = atomicAdd(&sy->ticket, 1u);
+            t = __shfl_sync(full, t, 0);
+            if ((long long)t >= total) break;
+            // ticket t is a bonded chunk when the even spread of the nbw
+            // chunks over the total puts one at t
+            const long long before = (long long)t * nbw / total, upto = ((long long)t + 1) * nbw / total;
+            if (upto > before) {
+                const int c = (int)before;
+                unsigned bad = 0;
+                int first = -1;
+                if (c < cb) bonded_term<MI>(fa, c * 32 + lane, bad, first);
+                else pair14_term<MI>(fa, (c - cb) * 32 + lane, bad, first);
+                bad = __reduce_or_sync(full, bad);
+                if (bad && lane == 0) atomicOr(&st->error, bad);
+            } else {
+                pair_item_mixed<PERIODIC, COULOMB, BATCH>((int)((long long)t - upto), lane, fa.n, fa.cap, fa.split,
+                                                          fa.coord, fa.perm, fa.list, fa.count, fa.gmax, fa.ntypes,
+                                                          fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st,
+                                                          fa.group_sys, nullptr);
+            }
+        }
+    }
+    // ---- 2. every force is summed
+    if (!grid_barrier(sy, st)) return;
+    // ---- 3. kick, drift, pack, rebuild check (kick_drift_check_kernel's
+    // operations, one atom at a time)
+    const bool err0 = ld_acquire(&st->error) != 0, tail0 = ld_acquire(&st->tail_pending) != 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sy->ticket = 0;
+        sy->fresh = 0;
+    }
+    const int n = sa.n;
+    int need = 0, bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double np[3];
+        if (!err0) {
+            const double inv_m = sa.inv_mass[i];
+            for (int d = 0; d < 3; d++) {
+                const double f = __dmul_rn((double)__ldcg(fa.force + d * n + i), GM_FIX_INV);
+                const double kick = __dmul_rn(__dmul_rn(__dmul_rn(sa.dt_half, f), inv_m), GM_FORCE_TO_ACCEL);
+                double v = sa.vel[d * n + i];
+                if (tail0) v = __dadd_rn(v, kick);
+                v = __dadd_rn(v, kick);
+                const double p = sa.pos[d * n + i];
+                sa.dref[d * n + i] = p;
+                np[d] = __dadd_rn(p, __dmul_rn(sa.dt, v));
+                sa.pos[d * n + i] = np[d];
+                sa.vel[d * n + i] = gm_div_by_dt(__dsub_rn(np[d], p), sa.dt, sa.inv_dt);
+            }
+        } else {
+            for (int d = 0; d < 3; d++) np[d] = sa.pos[d * n + i];
+        }
+        const int sl = pk.slot_of[i];
+        const GridInfo *g = pk.grid + sa.atom_sys[i];
+        gm_pack_record(pk.coord + 2 * sl, __dsub_rn(np[0], g->origin[0]), __dsub_rn(np[1], g->origin[1]),
+                       __dsub_rn(np[2], g->origin[2]), pk.qw[i]);
+        for (int d = 0; d < 3; d++) fa.force[d * n + i] = 0;
+        bad |= !(isfinite(np[0]) && isfinite(np[1]) && isfinite(np[2]));
+        const double dx = __dsub_rn(np[0], sa.ref[i]), dy = __dsub_rn(np[1], sa.ref[n + i]),
+                     dz = __dsub_rn(np[2], sa.ref[2 * n + i]);
+        const bool moved = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)) > sa.thr_sq;
+        if (moved) {
+            sa.sys_flag[sa.atom_sys[i]] = 1u;
+            need = 1;
+        }
+    }
+    need = __syncthreads_or(need);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        if (need) atomicOr(&st->rebuild, 1u);
+        if (bad) atomicOr(&st->bad_pending, 1u);
+        __threadfence();
+        const unsigned done = atomicAdd(&st->blocks_done, 1u);
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            const unsigned r = atomicOr(&st->rebuild, 0u);
+            st->blocks_done = 0;
+            if (atomicExch(&st->bad_pending, 0u)) atomicOr(&st->error, (unsigned)GM_DEV_NONFINITE_POS);
+            const unsigned e = atomicOr(&st->error, 0u);
+            if (sa.cond) cudaGraphSetConditional((cudaGraphConditionalHandle)sa.cond, (r && !e) ? 1u : 0u);
+            if (!err0) {
+                if (tail0) st->step += 1;
+                st->tail_pending = 1u;
+            }
+        }
+    }
+}
+
+using StepKernel = void (*)(ForceArgs, StepArgs, PackArgs);
+
+StepKernel pick(const ForceArgs &fa, bool gtab) {
+#define GM_STEPK(P, Q, B, M) return step_persistent_kernel<P, Q, B, M>
+#define GM_STEPB(P, Q, M) { if (gtab) GM_STEPK(P, Q, true, M); else GM_STEPK(P, Q, false, M); }
+#define GM_STEPQ(P, M) { if (fa.coulomb) GM_STEPB(P, true, M) else GM_STEPB(P, false, M) }
+    if (fa.bonded_mi) GM_STEPQ(true, true)
+    if (fa.periodic) GM_STEPQ(true, false)
+    GM_STEPQ(false, false)
+#undef GM_STEPQ
+#undef GM_STEPB
+#undef GM_STEPK
+}
+
+// A batch reads its [system][type][type] tables through L1, as does a single
+// system whose table passes 48 KB.
+bool global_table(const ForceArgs &fa) {
+    return fa.e_sys != nullptr || sizeof(float4) * (size_t)fa.ntypes * fa.ntypes > 48 * 1024;
+}
+
+}  // namespace
+
+int gm_step_persistent_blocks(const ForceArgs &fa) {
+    const bool gtab = global_table(fa);
+    const size_t smem = gtab ? 0 : sizeof(float4) * (size_t)fa.ntypes * fa.ntypes;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick(fa, gtab), kStepThreads, smem) != cudaSuccess)
+        return 0;
+    return per_sm * sms;
+}
+
+void gm_launch_step_persistent(const ForceArgs &fa, const StepArgs &sa, const PackArgs &pk, int blocks,
+                               cudaStream_t s) {
+    const bool gtab = global_table(fa);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(kStepThreads);
+    cfg.dynamicSmemBytes = gtab ? 0 : sizeof(float4) * (size_t)fa.ntypes * fa.ntypes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, pick(fa, gtab), fa, sa, pk);
+}

@@ -28,6 +28,7 @@ STATUS_NAMES = {
     7: "LIST_OVERFLOW", 8: "UNSUPPORTED", 9: "FIXED_POINT_OVERFLOW", 10: "NOT_BUILT",
 }
 PRECISION_MIXED, PRECISION_FP64 = 0, 1
+STEP_GRAPH, STEP_PERSISTENT = 0, 1  # gm_step_form
 
 _u32p = C.POINTER(C.c_uint32)
 _f64p = C.POINTER(C.c_double)
@@ -165,6 +166,7 @@ def lib():
         L.gm_ensemble_energies.argtypes = [C.c_void_p, _f64p, _f64p]
         L.gm_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int64)]
         L.gm_pair_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+        L.gm_step_form.argtypes = [C.c_void_p, C.c_int32]
         L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
         L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
         L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
@@ -296,6 +298,12 @@ class CudaBackend:
         """Sets the pair kernel's launch shape (gm_pair_shape), e.g. a cached
         autotune() result."""
         self._check(lib().gm_pair_shape(self._h, int(split), int(warps_per_block), int(grid)))
+
+    def step_form(self, form):
+        """How resident steps are issued (gm_step_form): STEP_GRAPH, the
+        kernel graph, or STEP_PERSISTENT, one persistent cooperative launch per
+        step (unconstrained mixed-precision contexts).  Same bits either way."""
+        self._check(lib().gm_step_form(self._h, int(form)))
 
     def ensemble_energies(self):
         """Per-system (potential, kinetic) energies (gm_ensemble_energies)."""

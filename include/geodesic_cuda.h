@@ -254,6 +254,26 @@ int32_t gm_autotune(gm_ctx *ctx, int32_t reps, int64_t *choice);
  * bits for every shape. */
 int32_t gm_pair_shape(gm_ctx *ctx, int32_t split, int32_t warps_per_block, int32_t grid);
 
+/* ---- step form (no reference counterpart) ------------------------------
+ *
+ * How the resident steps of an unconstrained mixed-precision context are
+ * issued (gm_steps, gm_run_resident, gm_time_steps):
+ *   GM_STEP_GRAPH       one captured graph per step: the fused
+ *                       kick/drift/check/pack kernel, the rebuild IF node,
+ *                       the pair kernel beside the bonded / 1-4 kernel.
+ *   GM_STEP_PERSISTENT  one captured graph per step holding ONE persistent
+ *                       cooperative launch (forces at the current positions
+ *                       from a single work queue of pair items and bonded /
+ *                       1-4 chunks over every system of an ensemble, a grid
+ *                       barrier, then kick/drift/check/pack) and the rebuild
+ *                       IF node.  The forces at the final positions are
+ *                       evaluated by the force kernels after the last launch.
+ * Both forms give the same bits.  GM_ERR_UNSUPPORTED for an FP64 or
+ * constrained context; with trajectory frames enabled the graph form runs.
+ * The default is GM_STEP_GRAPH. */
+enum { GM_STEP_GRAPH = 0, GM_STEP_PERSISTENT = 1 };
+int32_t gm_step_form(gm_ctx *ctx, int32_t form);
+
 /* ---- constraint warm start (no reference counterpart) ------------------
  *
  * A 12-64-64-1 SiLU network (BF16 matmul weights and activations, FP32

@@ -1,0 +1,139 @@
+"""The persistent step form against the kernel-graph form (needs a GPU).
+
+gm_step_form(GM_STEP_PERSISTENT) issues each unconstrained mixed-precision
+step as one cooperative launch: forces at the current positions from one work
+queue (pair items and bonded / 1-4 chunks of every system), a grid barrier,
+then kick, drift, rebuild check and pack; the rebuild stays in the graph's IF
+node.  Its force sums are integer sums and its integrator arithmetic rounds
+like the integrator kernels, so it must reproduce the kernel graph's run bit
+for bit:
+* a single system (non-periodic with Coulomb and 1-4 terms, and periodic
+  with the nearest image in the bonded terms), resident runs over several
+  gm_steps calls with list rebuilds: positions, velocities, potential energy
+  and rebuild counts;
+* a batch of systems of uneven size: every member's state and the
+  per-system energies;
+* gm_time_steps (every timed launch evaluates its forces);
+and it is refused for FP64 and constrained contexts (GM_ERR_UNSUPPORTED).
+"""
+import numpy as np
+import pytest
+
+from geodesic_cuda import amber, backend, synth
+
+pytestmark = pytest.mark.gpu
+
+DT = 0.002
+OPEN = dict(box_size=(1000.0,) * 3, periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
+            scale14_lj=0.5, scale14_coul=1 / 1.2)
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def run(atoms, topo, state, params, form, chunks, ensemble=False):
+    if ensemble:
+        be = backend.CudaBackend.ensemble(atoms, topo, params)
+    else:
+        be = backend.CudaBackend(atoms, topo, params)
+    be.step_form(form)
+    pos = np.ascontiguousarray(state[0].copy())
+    vel = np.ascontiguousarray(state[1].copy())
+    energies, rebuilds = [], 0
+    first = 0
+    for n in chunks:
+        e, nr, _ = be.steps(pos, vel, DT, n, first_step=first)
+        energies.append(e)
+        rebuilds += nr
+        first += n
+    sys_e = be.ensemble_energies()[0].copy() if ensemble else None
+    be.close()
+    return pos, vel, energies, rebuilds, sys_e
+
+
+def assert_same(a, b):
+    pos_a, vel_a, e_a, nr_a, se_a = a
+    pos_b, vel_b, e_b, nr_b, se_b = b
+    assert np.array_equal(bits(pos_a), bits(pos_b))
+    assert np.array_equal(bits(vel_a), bits(vel_b))
+    assert e_a == e_b
+    assert nr_a == nr_b
+    if se_a is not None:
+        assert np.array_equal(bits(se_a), bits(se_b))
+
+
+def test_single_system_bit_identical_over_calls_with_rebuilds():
+    atoms, topo, state, _ = synth.generate(5000, seed=77, temperature=600.0, relax_iters=400)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **OPEN)
+    chunks = (1, 149, 250)  # a one-step call, then longer ones
+    g = run(atoms, topo, (state.pos, state.vel), p, backend.STEP_GRAPH, chunks)
+    q = run(atoms, topo, (state.pos, state.vel), p, backend.STEP_PERSISTENT, chunks)
+    assert g[3] >= 1  # the run rebuilt its list
+    assert_same(g, q)
+
+
+def test_periodic_system_with_bonded_nearest_image():
+    atoms, topo, state, _ = synth.generate(4000, seed=78, temperature=600.0, relax_iters=400)
+    lo = state.pos.min(axis=1, keepdims=True)
+    pos = np.ascontiguousarray(state.pos - lo + 1.0)
+    box = float(np.ceil(pos.max())) + 2.0
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, box_size=(box,) * 3, periodic=True,
+                          bonded_min_image=True, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
+                          scale14_lj=0.5, scale14_coul=1 / 1.2)
+    chunks = (120, 180)
+    g = run(atoms, topo, (pos, state.vel), p, backend.STEP_GRAPH, chunks)
+    q = run(atoms, topo, (pos, state.vel), p, backend.STEP_PERSISTENT, chunks)
+    assert g[3] >= 1
+    assert_same(g, q)
+
+
+def test_batch_of_uneven_systems():
+    syss = [synth.generate(n, seed=s, temperature=600.0, relax_iters=300) for n, s in
+            ((600, 81), (2300, 82), (900, 83), (4100, 84), (1300, 85))]
+    atoms = [s[0] for s in syss]
+    topo = [s[1] for s in syss]
+    pos = np.concatenate([s[2].pos for s in syss], axis=1)
+    vel = np.concatenate([s[2].vel for s in syss], axis=1)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **OPEN)
+    chunks = (50, 250)
+    g = run(atoms, topo, (pos, vel), p, backend.STEP_GRAPH, chunks, ensemble=True)
+    q = run(atoms, topo, (pos, vel), p, backend.STEP_PERSISTENT, chunks, ensemble=True)
+    assert g[3] >= 1
+    assert_same(g, q)
+
+
+def test_timed_steps_evaluate_their_forces():
+    atoms, topo, state, _ = synth.generate(3000, seed=79, temperature=300.0, relax_iters=300)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **OPEN)
+    out = []
+    for form in (backend.STEP_GRAPH, backend.STEP_PERSISTENT):
+        be = backend.CudaBackend(atoms, topo, p)
+        be.step_form(form)
+        be.upload_state(np.ascontiguousarray(state.pos), np.ascontiguousarray(state.vel))
+        be.forces_resident()
+        ms = be.time_steps(DT, 40)
+        assert ms > 0.0
+        pos = np.zeros_like(state.pos)
+        vel = np.zeros_like(state.vel)
+        be.download_state(pos, vel)
+        f = be.compute_forces(pos).copy()  # the resident forces at the final positions
+        out.append((pos, vel, f))
+        be.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(bits(a), bits(b))
+
+
+@pytest.mark.parametrize("case", ["fp64", "constrained"])
+def test_refused_where_it_does_not_apply(case):
+    atoms, topo, state, _ = synth.generate(800, seed=80, h_fraction=0.3 if case == "constrained" else 0.0,
+                                           relax_iters=100)
+    if case == "constrained":
+        topo = amber.promote_hydrogen_bonds(topo, atoms)
+    prec = backend.PRECISION_FP64 if case == "fp64" else backend.PRECISION_MIXED
+    be = backend.CudaBackend(atoms, topo, backend.SimParams(precision=prec, **OPEN))
+    with pytest.raises(backend.BackendError) as e:
+        be.step_form(backend.STEP_PERSISTENT)
+    assert e.value.status == 8  # GM_ERR_UNSUPPORTED
+    be.step_form(backend.STEP_GRAPH)
+    be.close()
