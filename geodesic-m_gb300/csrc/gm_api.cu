@@ -861,6 +861,9 @@ int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
         for (int64_t k = 0; k < n_steps; k++) GM_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
         c->launches += c->launches_per_step * n_steps;
     }
+    // the steps' force evaluations leave the energy partials unsummed (the
+    // flag that seq_forces sets is set only when a graph is captured)
+    if (n_steps > 0) c->energy_stale = true;
     if (!rc && pf) rc = end_persistent(c);
     return rc ? rc : finish_steps(c, dt);
 }
@@ -1912,6 +1915,7 @@ int32_t gm_time_steps(gm_ctx *c, double dt, uint64_t first_step, int64_t n_steps
             GM_CUDA(c, cudaMemsetAsync(flush_buf, (int)((k + 1) & 0xff), (size_t)flush_bytes, c->stream));
     }
     if (c->use_graph) c->launches += c->launches_per_step * n_steps;
+    c->energy_stale = true;  // the steps leave their energy partials unsummed
     if (pf) rc = end_persistent(c);
     if (!rc) rc = finish_steps(c, dt);
     if (rc) return rc;

@@ -15,10 +15,14 @@ for bit:
   per-system energies;
 * gm_time_steps (every timed launch evaluates its forces);
 and it is refused for FP64 and constrained contexts (GM_ERR_UNSUPPORTED).
+The potential energy gm_steps returns is the one at the positions it
+returns, call after call, in both forms (against the oracle, lib.rs:292-323
+reports the energy of the step's closing force evaluation).
 """
 import numpy as np
 import pytest
 
+import oracle
 from geodesic_cuda import amber, backend, synth
 
 pytestmark = pytest.mark.gpu
@@ -71,6 +75,29 @@ def test_single_system_bit_identical_over_calls_with_rebuilds():
     q = run(atoms, topo, (state.pos, state.vel), p, backend.STEP_PERSISTENT, chunks)
     assert g[3] >= 1  # the run rebuilt its list
     assert_same(g, q)
+
+
+@pytest.mark.parametrize("form", [backend.STEP_GRAPH, backend.STEP_PERSISTENT])
+def test_energy_of_every_call_is_current(form):
+    atoms, topo, state, _ = synth.generate(2000, seed=76, temperature=600.0, relax_iters=300)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **OPEN)
+    be = backend.CudaBackend(atoms, topo, p)
+    be.step_form(form)
+    pos = np.ascontiguousarray(state.pos.copy())
+    vel = np.ascontiguousarray(state.vel.copy())
+    op = oracle.make_params(box=OPEN["box_size"], periodic=False, r_cutoff=10.0, r_skin=12.0, r_switch=8.0,
+                            n_threads=0, coulomb=True, scale14_lj=0.5, scale14_coul=1 / 1.2)
+    seen = []
+    for n in (1, 40, 60):
+        e, _, _ = be.steps(pos, vel, DT, n)
+        pi, pj = oracle.neighbor_build(pos.copy(), atoms, topo, op, cells=True)
+        ob = oracle.CpuBackend(atoms, topo, op)
+        ob.set_pairs(pi, pj, pos)
+        ob.compute_forces(pos.copy())
+        assert abs(e - ob.potential_energy) <= 1e-6 * abs(ob.potential_energy), (n, e, ob.potential_energy)
+        seen.append(e)
+    assert len(set(seen)) == 3
+    be.close()
 
 
 def test_periodic_system_with_bonded_nearest_image():
