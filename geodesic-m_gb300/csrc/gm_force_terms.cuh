@@ -63,7 +63,9 @@ __device__ __forceinline__ void image_df(float &dh, float &dl, float L, float Ll
 // 50k-atom system has only 1,563 groups).
 // BATCH: systems of a batch have their own type tables ([system][type][type],
 // read through L1); a single system keeps its table in shared memory.
-template <bool PERIODIC, bool COULOMB, bool BATCH>
+// ENERGY false: the item adds its forces only (no energy partial, no
+// per-system energy); the force bits are the same.
+template <bool PERIODIC, bool COULOMB, bool BATCH, bool ENERGY = true>
 __device__ __forceinline__ void
 pair_item_mixed(int wid, int lane, int n, int cap, int split, const float4 *__restrict__ coord,
                 const int *__restrict__ perm, const int *__restrict__ list, const int *__restrict__ count,
@@ -186,23 +188,26 @@ pair_item_mixed(int wid, int lane, int n, int cap, int split, const float4 *__re
                     sum.l += acc[d].l - er;
                     acc[d] = sum;
                 }
-                ev += v;
+                if (ENERGY) ev += v;
             }
             }
         }
         ax += gm_to_fix_checked(acc[0].h, bad) + gm_f2fix(acc[0].l);
         ay += gm_to_fix_checked(acc[1].h, bad) + gm_f2fix(acc[1].l);
         az += gm_to_fix_checked(acc[2].h, bad) + gm_f2fix(acc[2].l);
-        eacc += (double)ev;
+        if (ENERGY) eacc += (double)ev;
     }
     if (valid && e_begin < e_end) {
         gm_atomic_fix_add(force + atom, ax);
         gm_atomic_fix_add(force + n + atom, ay);
         gm_atomic_fix_add(force + 2 * n + atom, az);
     }
-    for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(full, eacc, o);
-    if (lane == 0) epart[wid] = 0.5 * eacc;
-    if (e_sys && lane == 0) gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
+    if (ENERGY) {
+        for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(full, eacc, o);
+        if (lane == 0) epart[wid] = 0.5 * eacc;
+        if (e_sys && lane == 0)
+            gm_atomic_fix_add(e_sys + group_sys[group], __double2ll_rn(0.5 * eacc * GM_EFIX_SCALE));
+    }
     bad = __reduce_or_sync(full, bad);
     if (bad && lane == 0) atomicOr(&st->error, bad);
 }

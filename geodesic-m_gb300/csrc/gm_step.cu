@@ -5,7 +5,7 @@
 // the list that the graph's conditional rebuild left after it):
 //   1. forces F(x_k): every warp takes work items from one queue: the pair
 //      items of the mixed kernel (pair_item_mixed, a 32-atom group's share of
-//      list columns) and 32-term chunks of the bonded terms and 1-4 pairs,
+//      list columns) and 128-term chunks of the bonded terms and 1-4 pairs,
 //      spread evenly through the queue so that each SM mixes FP32 pair work
 //      with FP64 bonded work.  Skipped when the forces at x_k are summed
 //      already (the first launch of a call: the call starts with current
@@ -26,13 +26,16 @@
 // force sums are integer sums (the order of the work items changes no bit),
 // and phase 3 is written with explicit round-to-nearest operations, so it
 // rounds like the integrator kernels, which are compiled without
-// contraction.  Energies are not summed inside the loop (only the force
-// phase after the last launch sums them), so the bonded chunks drop theirs.
+// contraction.  Energies are not evaluated inside the loop (the force
+// evaluation after the last launch sums them): the pair items and the
+// bonded chunks add forces only.
 #include "gm_force_terms.cuh"
 
 namespace {
 
 constexpr int kStepThreads = 128;
+constexpr int kStepMinBlocks = 6;  // 24 warps per SM: at most 80 registers a thread
+constexpr int kTermsPerTicket = 128;  // bonded terms (or 1-4 pairs) per work item, 32 per lane pass
 // ~64 ns per poll: about a quarter of a second before a block gives up
 constexpr unsigned kBarrierPolls = 1u << 22;
 
@@ -75,7 +78,8 @@ __device__ bool grid_barrier(StepSync *sy, DevStatus *st) {
 }
 
 template <bool PERIODIC, bool COULOMB, bool BATCH, bool MI>
-__global__ void __launch_bounds__(kStepThreads) step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
+__global__ void __launch_bounds__(kStepThreads, kStepMinBlocks)
+step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
     extern __shared__ float4 s_tab[];
     DevStatus *st = fa.status;
     StepSync *sy = sa.sync;
@@ -89,30 +93,36 @@ __global__ void __launch_bounds__(kStepThreads) step_persistent_kernel(ForceArgs
             for (int t = threadIdx.x; t < fa.ntypes * fa.ntypes; t += blockDim.x) s_tab[t] = fa.tab32[t];
             __syncthreads();
         }
-        const long long n_pair = (long long)fa.n_groups * fa.split;
-        const int cb = (fa.n_bonds + fa.n_angles + fa.n_diheds + 31) / 32, c14 = (fa.n14 + 31) / 32;
-        const long long nbw = (long long)cb + c14, total = n_pair + nbw;
+        // tickets: n_pair pair items and nbw bonded tickets (kTermsPerTicket
+        // bonded terms or 1-4 pairs each), the bonded ones at t = k * stride
+        const int n_pair = fa.n_groups * fa.split;
+        const int cb = (fa.n_bonds + fa.n_angles + fa.n_diheds + kTermsPerTicket - 1) / kTermsPerTicket;
+        const int c14 = (fa.n14 + kTermsPerTicket - 1) / kTermsPerTicket;
+        const int nbw = cb + c14, total = n_pair + nbw;
+        const int stride = nbw > 0 ? total / nbw : 1;
         for (;;) {
-            unsigned t = 0;
-            if (lane == 0) t = atomicAdd(&sy->ticket, 1u);
+            int t = 0;
+            if (lane == 0) t = (int)atomicAdd(&sy->ticket, 1u);
             t = __shfl_sync(full, t, 0);
-            if ((long long)t >= total) break;
-            // ticket t is a bonded chunk when the even spread of the nbw
-            // chunks over the total puts one at t
-            const long long before = (long long)t * nbw / total, upto = ((long long)t + 1) * nbw / total;
-            if (upto > before) {
-                const int c = (int)before;
+            if (t >= total) break;
+            const int q = t / stride, r = t - q * stride;
+            if (r == 0 && q < nbw) {
                 unsigned bad = 0;
                 int first = -1;
-                if (c < cb) bonded_term<MI>(fa, c * 32 + lane, bad, first);
-                else pair14_term<MI>(fa, (c - cb) * 32 + lane, bad, first);
+                const bool b14 = q >= cb;
+                const int base = (b14 ? q - cb : q) * kTermsPerTicket + lane;
+                for (int u = 0; u < kTermsPerTicket; u += 32) {
+                    if (b14) pair14_term<MI>(fa, base + u, bad, first);
+                    else bonded_term<MI>(fa, base + u, bad, first);
+                }
                 bad = __reduce_or_sync(full, bad);
                 if (bad && lane == 0) atomicOr(&st->error, bad);
             } else {
-                pair_item_mixed<PERIODIC, COULOMB, BATCH>((int)((long long)t - upto), lane, fa.n, fa.cap, fa.split,
-                                                          fa.coord, fa.perm, fa.list, fa.count, fa.gmax, fa.ntypes,
-                                                          fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st,
-                                                          fa.group_sys, nullptr);
+                // bonded tickets at or before t: min(q + 1, nbw)
+                const int item = t - min(q + 1, nbw);
+                pair_item_mixed<PERIODIC, COULOMB, BATCH, false>(
+                    item, lane, fa.n, fa.cap, fa.split, fa.coord, fa.perm, fa.list, fa.count, fa.gmax, fa.ntypes,
+                    fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st, fa.group_sys, nullptr);
             }
         }
     }
