@@ -151,9 +151,11 @@ pair_item_mixed(int wid, int lane, int n, int cap, int split, const float4 *__re
             }
             if (__any_sync(full, band) && band) {
                 // LJ in FP32 (tiny here), then V S and F_r S - V dS/dr
-                const float xs = p.x * y, x3 = xs * xs * xs;
+                // (products rounded where the compiler could otherwise fuse them
+                // into the sums that follow)
+                const float xs = p.x * y, x3 = __fmul_rn(__fmul_rn(xs, xs), xs);
                 const float vlj = p.z * (1.f / 6.f) * x3 * (x3 - 1.f);
-                const float glj = p.z * x3 * (2.f * x3 - 1.f) * y;
+                const float glj = p.z * x3 * fmaf(2.f, x3, -1.f) * y;
                 const gm_df V = gm_dadd(Vc, gm_df_make(vlj, 0.f));
                 const gm_df G0 = gm_dadd(Gc, gm_df_make(glj, 0.f));
                 const gm_df r = gm_dmul(gm_df_make(Rh, Rl), rinv);
@@ -164,7 +166,7 @@ pair_item_mixed(int wid, int lane, int n, int cap, int split, const float4 *__re
                 // S = 1 + u^3 (-10 + u (15 - 6 u))
                 const float p6 = __fmul_rn(6.f, uu.h), e6 = fmaf(6.f, uu.h, -p6);
                 gm_df t = gm_two_sum(15.f, -p6);
-                t.l -= e6 + 6.f * uu.l;
+                t.l -= fmaf(6.f, uu.l, e6);
                 t = gm_dmul(uu, t);
                 gm_df t3 = gm_two_sum(-10.f, t.h);
                 t3.l += t.l;
@@ -235,10 +237,15 @@ __device__ __forceinline__ V3 pdiff(const ForceArgs &a, int ia, int ib) {
     }
     return d;
 }
+// The FP64 term arithmetic below fixes every fused multiply-add itself
+// (fma where a product feeds a sum, __dmul_rn where a product must stay
+// rounded): the compiler's own contraction choices may differ between the
+// kernels that inline these functions, and both step forms must round alike.
+__device__ __forceinline__ double pmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return {fma(a.y, b.z, -pmul(a.z, b.y)), fma(a.z, b.x, -pmul(a.x, b.z)), fma(a.x, b.y, -pmul(a.y, b.x))};
 }
-__device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double dot(V3 a, V3 b) { return fma(a.z, b.z, fma(a.y, b.y, pmul(a.x, b.x))); }
 
 __device__ __forceinline__ void add_force(long long *f, int n, int a, double x, double y, double z, unsigned &bad) {
     gm_atomic_fix_add(f + a, gm_to_fix_checked(x, bad));
@@ -262,11 +269,12 @@ __device__ __forceinline__ double bonded_term(const ForceArgs &a, int t, unsigne
         const double r2 = dot(d, d);
         if (r2 > 0.0) {
             const double ir = rsqrt(r2);
-            const double dr = r2 * ir - r0;
-            e = k * dr * dr;
-            const double g = 2.0 * k * dr * ir;
-            add_force(a.force, n, i, g * d.x, g * d.y, g * d.z, bad);
-            add_force(a.force, n, j, -g * d.x, -g * d.y, -g * d.z, bad);
+            const double dr = fma(r2, ir, -r0);
+            e = pmul(pmul(k, dr), dr);
+            const double g = pmul(pmul(pmul(2.0, k), dr), ir);
+            const double gx = pmul(g, d.x), gy = pmul(g, d.y), gz = pmul(g, d.z);
+            add_force(a.force, n, i, gx, gy, gz, bad);
+            add_force(a.force, n, j, -gx, -gy, -gz, bad);
         }
     } else if (t < a.n_bonds + a.n_angles) {
         // force/bonded.rs:44-102, V = k (theta - theta0)^2
@@ -277,19 +285,22 @@ __device__ __forceinline__ double bonded_term(const ForceArgs &a, int t, unsigne
         const double q1 = dot(b1, b1), q2 = dot(b2, b2);
         if (q1 != 0.0 && q2 != 0.0) {
             const double i1 = rsqrt(q1), i2 = rsqrt(q2);
-            double c = dot(b1, b2) * i1 * i2;
+            double c = pmul(pmul(dot(b1, b2), i1), i2);
             c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
-            double sn = sqrt(1.0 - c * c);
+            double sn = sqrt(fma(-c, c, 1.0));
             sn = sn > 1e-8 ? sn : 1e-8;
             const double dth = acos(c) - a.angle_th0[q];
             const double k = a.angle_kth[q];
-            e = k * dth * dth;
-            const double aa = 2.0 * k * dth / sn;
-            const double ir12 = i1 * i2, ir11 = i1 * i1, ir22 = i2 * i2;
-            const V3 fi = {aa * (b2.x * ir12 - c * b1.x * ir11), aa * (b2.y * ir12 - c * b1.y * ir11),
-                           aa * (b2.z * ir12 - c * b1.z * ir11)};
-            const V3 fk = {aa * (b1.x * ir12 - c * b2.x * ir22), aa * (b1.y * ir12 - c * b2.y * ir22),
-                           aa * (b1.z * ir12 - c * b2.z * ir22)};
+            e = pmul(pmul(k, dth), dth);
+            const double aa = pmul(pmul(2.0, k), dth) / sn;
+            const double ir12 = pmul(i1, i2), ir11 = pmul(i1, i1), ir22 = pmul(i2, i2);
+            // aa (b2 / (|b1| |b2|) - c b1 / |b1|^2), and the same for k
+            const V3 fi = {pmul(aa, fma(b2.x, ir12, -pmul(pmul(c, b1.x), ir11))),
+                           pmul(aa, fma(b2.y, ir12, -pmul(pmul(c, b1.y), ir11))),
+                           pmul(aa, fma(b2.z, ir12, -pmul(pmul(c, b1.z), ir11)))};
+            const V3 fk = {pmul(aa, fma(b1.x, ir12, -pmul(pmul(c, b2.x), ir22))),
+                           pmul(aa, fma(b1.y, ir12, -pmul(pmul(c, b2.y), ir22))),
+                           pmul(aa, fma(b1.z, ir12, -pmul(pmul(c, b2.z), ir22)))};
             add_force(a.force, n, i, fi.x, fi.y, fi.z, bad);
             add_force(a.force, n, kk, fk.x, fk.y, fk.z, bad);
             add_force(a.force, n, j, -(fi.x + fk.x), -(fi.y + fk.y), -(fi.z + fk.z), bad);
@@ -303,34 +314,36 @@ __device__ __forceinline__ double bonded_term(const ForceArgs &a, int t, unsigne
         const V3 m = cross(b1, b2), nv = cross(b2, b3);
         const double m2 = dot(m, m), n2 = dot(nv, nv), b22 = dot(b2, b2);
         if (m2 != 0.0 && n2 != 0.0 && b22 != 0.0) {
-            const double ib2 = rsqrt(b22), b2l = b22 * ib2;
+            const double ib2 = rsqrt(b22), b2l = pmul(b22, ib2);
             // phi = atan2(y, x) as in the reference; cos(n phi - delta) and
             // sin(n phi - delta) are taken without the transcendentals:
             // (cos phi, sin phi) = (x, y) / |(x, y)|, raised to the n-th
             // power as a complex number, then rotated by delta (the FP64
             // pipe of this part is 1/64 of its FP32 one)
             const double x = dot(m, nv);
-            const double y = dot(cross(m, nv), b2) * ib2;
-            const double ir = rsqrt(x * x + y * y);
-            const double c1 = x * ir, s1 = y * ir;
+            const double y = pmul(dot(cross(m, nv), b2), ib2);
+            const double ir = rsqrt(fma(x, x, pmul(y, y)));
+            const double c1 = pmul(x, ir), s1 = pmul(y, ir);
             const unsigned mult = a.dihed_n[q];
             double cn = 1.0, sn = 0.0;
             for (unsigned it = 0; it < mult; it++) {
-                const double c2 = cn * c1 - sn * s1;
-                sn = sn * c1 + cn * s1;
+                const double c2 = fma(cn, c1, -pmul(sn, s1));
+                sn = fma(sn, c1, pmul(cn, s1));
                 cn = c2;
             }
             const double2 cs = a.dihed_cs[q];  // (cos delta, sin delta)
             const double kphi = a.dihed_kphi[q];
-            e = kphi * (1.0 + (cn * cs.x + sn * cs.y));
-            const double dv = kphi * (double)mult * (sn * cs.x - cn * cs.y);  // -dV/dphi
-            const double imn = dv * b2l / (m2 * n2);
-            const double si = -imn * n2, sl = imn * m2;
-            const V3 fi = {m.x * si, m.y * si, m.z * si}, fl = {nv.x * sl, nv.y * sl, nv.z * sl};
-            const double ib = ib2 * ib2;
-            const double p = dot(b1, b2) * ib, qq = dot(b3, b2) * ib;
-            const V3 fj = {-(p + 1.0) * fi.x + qq * fl.x, -(p + 1.0) * fi.y + qq * fl.y, -(p + 1.0) * fi.z + qq * fl.z};
-            const V3 fk = {p * fi.x - (qq + 1.0) * fl.x, p * fi.y - (qq + 1.0) * fl.y, p * fi.z - (qq + 1.0) * fl.z};
+            e = pmul(kphi, 1.0 + fma(cn, cs.x, pmul(sn, cs.y)));
+            const double dv = pmul(pmul(kphi, (double)mult), fma(sn, cs.x, -pmul(cn, cs.y)));  // -dV/dphi
+            const double imn = pmul(dv, b2l) / pmul(m2, n2);
+            const double si = pmul(-imn, n2), sl = pmul(imn, m2);
+            const V3 fi = {pmul(m.x, si), pmul(m.y, si), pmul(m.z, si)};
+            const V3 fl = {pmul(nv.x, sl), pmul(nv.y, sl), pmul(nv.z, sl)};
+            const double ib = pmul(ib2, ib2);
+            const double p = pmul(dot(b1, b2), ib), qq = pmul(dot(b3, b2), ib);
+            const double p1 = -(p + 1.0), q1 = qq + 1.0;
+            const V3 fj = {fma(qq, fl.x, pmul(p1, fi.x)), fma(qq, fl.y, pmul(p1, fi.y)), fma(qq, fl.z, pmul(p1, fi.z))};
+            const V3 fk = {fma(p, fi.x, -pmul(q1, fl.x)), fma(p, fi.y, -pmul(q1, fl.y)), fma(p, fi.z, -pmul(q1, fl.z))};
             add_force(a.force, n, i, fi.x, fi.y, fi.z, bad);
             add_force(a.force, n, j, fj.x, fj.y, fj.z, bad);
             add_force(a.force, n, k, fk.x, fk.y, fk.z, bad);
@@ -355,12 +368,14 @@ __device__ __forceinline__ double pair14_term(const ForceArgs &a, int t, unsigne
             // (sigma_ij, 4 eps_ij s_lj, 24 eps_ij s_lj, k_C q_i q_j s_coul)
             const double4 p = a.p14par[t];
             const double rinv = rsqrt(r2);
-            const double sr = p.x * rinv, s2 = sr * sr, s4 = s2 * s2, s6 = s2 * s4, s12 = s6 * s6;
-            const double vc = p.w * rinv;
-            e = p.y * (s12 - s6) + vc;
-            const double g = (p.z * (2.0 * s12 - s6) + vc) * rinv * rinv;
-            add_force(a.force, n, i, -g * d.x, -g * d.y, -g * d.z, bad);
-            add_force(a.force, n, j, g * d.x, g * d.y, g * d.z, bad);
+            const double sr = pmul(p.x, rinv), s2 = pmul(sr, sr), s4 = pmul(s2, s2), s6 = pmul(s2, s4);
+            const double s12 = pmul(s6, s6);
+            const double vc = pmul(p.w, rinv);
+            e = fma(p.y, s12 - s6, vc);
+            const double g = pmul(pmul(fma(p.z, fma(2.0, s12, -s6), vc), rinv), rinv);
+            const double gx = pmul(g, d.x), gy = pmul(g, d.y), gz = pmul(g, d.z);
+            add_force(a.force, n, i, -gx, -gy, -gz, bad);
+            add_force(a.force, n, j, gx, gy, gz, bad);
         }
     }
     return e;

@@ -8,7 +8,7 @@ node.  Its force sums are integer sums and its integrator arithmetic rounds
 like the integrator kernels, so it must reproduce the kernel graph's run bit
 for bit:
 * a single system (non-periodic with Coulomb and 1-4 terms, and periodic
-  with the nearest image in the bonded terms), resident runs over several
+  with and without the nearest image in the bonded terms), resident runs over several
   gm_steps calls with list rebuilds: positions, velocities, potential energy
   and rebuild counts;
 * a batch of systems of uneven size: every member's state and the
@@ -100,13 +100,14 @@ def test_energy_of_every_call_is_current(form):
     be.close()
 
 
-def test_periodic_system_with_bonded_nearest_image():
+@pytest.mark.parametrize("bonded_mi", [False, True])
+def test_periodic_system(bonded_mi):
     atoms, topo, state, _ = synth.generate(4000, seed=78, temperature=600.0, relax_iters=400)
     lo = state.pos.min(axis=1, keepdims=True)
     pos = np.ascontiguousarray(state.pos - lo + 1.0)
     box = float(np.ceil(pos.max())) + 2.0
     p = backend.SimParams(precision=backend.PRECISION_MIXED, box_size=(box,) * 3, periodic=True,
-                          bonded_min_image=True, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
+                          bonded_min_image=bonded_mi, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
                           scale14_lj=0.5, scale14_coul=1 / 1.2)
     chunks = (120, 180)
     g = run(atoms, topo, (pos, state.vel), p, backend.STEP_GRAPH, chunks)
