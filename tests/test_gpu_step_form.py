@@ -103,6 +103,11 @@ def test_energy_of_every_call_is_current(form):
 @pytest.mark.parametrize("bonded_mi", [False, True])
 def test_periodic_system(bonded_mi):
     atoms, topo, state, _ = synth.generate(4000, seed=78, temperature=600.0, relax_iters=400)
+    if not bonded_mi:
+        # raw bonded differences across the faces are the reference's
+        # behaviour and blow up once a molecule wraps: without the nearest
+        # image the run is a charged LJ fluid (periodic pair path only)
+        topo = amber.BondedTopology.empty()
     lo = state.pos.min(axis=1, keepdims=True)
     pos = np.ascontiguousarray(state.pos - lo + 1.0)
     box = float(np.ceil(pos.max())) + 2.0
