@@ -100,23 +100,41 @@ def test_energy_of_every_call_is_current(form):
     be.close()
 
 
+def charged_fluid(side=14, spacing=3.7, seed=5):
+    """A periodic charged LJ fluid without bonded terms: a jittered cubic
+    lattice near the LJ minimum (sigma 3 A, epsilon 0.2 kcal/mol, charges
+    +-0.3 e alternating), Maxwell-Boltzmann velocities at 600 K."""
+    rng = np.random.default_rng(seed)
+    g = np.arange(side) * spacing + spacing / 2
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1) + rng.uniform(-0.2, 0.2, (3, side ** 3))
+    n = pos.shape[1]
+    q = np.where(np.arange(n) % 2 == 0, 0.3, -0.3)
+    atoms = amber.AtomData(np.full(n, 3.0), np.full(n, 0.2), np.full(n, 12.0), q, np.full(n, 5, np.uint8),
+                           np.zeros(n, np.uint32), ["C   "] * n)
+    vel = rng.normal(size=(3, n)) * np.sqrt(0.0019872041 * 600.0 / 12.0 * 418.4)
+    return atoms, np.ascontiguousarray(pos), np.ascontiguousarray(vel - vel.mean(axis=1, keepdims=True)), side * spacing
+
+
 @pytest.mark.parametrize("bonded_mi", [False, True])
 def test_periodic_system(bonded_mi):
-    atoms, topo, state, _ = synth.generate(4000, seed=78, temperature=600.0, relax_iters=400)
-    if not bonded_mi:
-        # raw bonded differences across the faces are the reference's
-        # behaviour and blow up once a molecule wraps: without the nearest
-        # image the run is a charged LJ fluid (periodic pair path only)
+    if bonded_mi:
+        atoms, topo, state, _ = synth.generate(4000, seed=78, temperature=600.0, relax_iters=400)
+        lo = state.pos.min(axis=1, keepdims=True)
+        pos = np.ascontiguousarray(state.pos - lo + 1.0)
+        vel = state.vel
+        box = float(np.ceil(pos.max())) + 2.0
+    else:
+        # raw bonded differences across the faces (the reference's
+        # behaviour) blow up once a molecule wraps: without the nearest image
+        # the run is a fluid without bonded terms (the periodic pair path)
+        atoms, pos, vel, box = charged_fluid()
         topo = amber.BondedTopology.empty()
-    lo = state.pos.min(axis=1, keepdims=True)
-    pos = np.ascontiguousarray(state.pos - lo + 1.0)
-    box = float(np.ceil(pos.max())) + 2.0
     p = backend.SimParams(precision=backend.PRECISION_MIXED, box_size=(box,) * 3, periodic=True,
                           bonded_min_image=bonded_mi, r_cutoff=10.0, r_skin=12.0, r_switch=8.0, coulomb=True,
                           scale14_lj=0.5, scale14_coul=1 / 1.2)
     chunks = (120, 180)
-    g = run(atoms, topo, (pos, state.vel), p, backend.STEP_GRAPH, chunks)
-    q = run(atoms, topo, (pos, state.vel), p, backend.STEP_PERSISTENT, chunks)
+    g = run(atoms, topo, (pos, vel), p, backend.STEP_GRAPH, chunks)
+    q = run(atoms, topo, (pos, vel), p, backend.STEP_PERSISTENT, chunks)
     assert g[3] >= 1
     assert_same(g, q)
 
