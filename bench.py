@@ -704,7 +704,7 @@ def main():
                     help="timed steps only (no error, CPU-baseline, FP64 or e2e legs); for profiler runs")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="with --quick: the precision of the timed steps")
-    ap.add_argument("--step-form", choices=["graph", "persistent"], default="graph",
+    ap.add_argument("--step-form", choices=["graph", "persistent"], default="persistent",
                     help="unconstrained mixed-precision steps: the kernel graph, or one persistent launch per step")
     ap.add_argument("--pair-shape", default="",
                     help="SPLIT,WARPS,GRID: the pair kernel's launch shape instead of the autotuner's choice")

@@ -37,6 +37,11 @@ struct gm_ctx {
     int device = 0;
     cudaStream_t stream = nullptr, side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // bonded/1-4 branch beside the pair kernel
+    // gm_steps' host copies beside the device work: the velocity upload
+    // beside the position check, the position download beside the final
+    // force evaluation
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t ev_xfer_in = nullptr, ev_xfer_out = nullptr;
     gm_params p{};
     int n = 0;
     bool fp64 = false;
@@ -130,8 +135,8 @@ struct gm_ctx {
     bool forces_current = false;
     bool use_graph = true;           // GM_GRAPH=0: direct launches (profilers)
     // step form of unconstrained mixed-precision runs: 0 the kernel graph,
-    // 1 one persistent cooperative launch per step (gm_step.cu)
-    int step_form = 0;
+    // 1 one persistent cooperative launch per step (gm_step.cu, the default)
+    int step_form = 1;
     int persist_blocks = 0;          // its grid: every block resident
     StepSync *d_sync = nullptr;
     long long rebuild_base = 0;
@@ -653,29 +658,31 @@ int do_build(gm_ctx *c, bool all = true) {
 
 // Host rows in one contiguous x|y|z block (the caller's 3 x N array) go in
 // one copy; separate rows in three.
-int upload3(gm_ctx *c, double *dst, const double *x, const double *y, const double *z) {
+int upload3(gm_ctx *c, double *dst, const double *x, const double *y, const double *z, cudaStream_t s = nullptr) {
     const size_t b = sizeof(double) * (size_t)c->n;
     if (!c->n) return GM_OK;
+    if (!s) s = c->stream;
     if (y == x + c->n && z == y + c->n) {
-        GM_CUDA(c, cudaMemcpyAsync(dst, x, 3 * b, cudaMemcpyHostToDevice, c->stream));
+        GM_CUDA(c, cudaMemcpyAsync(dst, x, 3 * b, cudaMemcpyHostToDevice, s));
         return GM_OK;
     }
-    GM_CUDA(c, cudaMemcpyAsync(dst, x, b, cudaMemcpyHostToDevice, c->stream));
-    GM_CUDA(c, cudaMemcpyAsync(dst + c->n, y, b, cudaMemcpyHostToDevice, c->stream));
-    GM_CUDA(c, cudaMemcpyAsync(dst + 2 * c->n, z, b, cudaMemcpyHostToDevice, c->stream));
+    GM_CUDA(c, cudaMemcpyAsync(dst, x, b, cudaMemcpyHostToDevice, s));
+    GM_CUDA(c, cudaMemcpyAsync(dst + c->n, y, b, cudaMemcpyHostToDevice, s));
+    GM_CUDA(c, cudaMemcpyAsync(dst + 2 * c->n, z, b, cudaMemcpyHostToDevice, s));
     return GM_OK;
 }
 
-int download3(gm_ctx *c, const double *src, double *x, double *y, double *z) {
+int download3(gm_ctx *c, const double *src, double *x, double *y, double *z, cudaStream_t s = nullptr) {
     const size_t b = sizeof(double) * (size_t)c->n;
     if (!c->n) return GM_OK;
+    if (!s) s = c->stream;
     if (x && y == x + c->n && z == y + c->n) {
-        GM_CUDA(c, cudaMemcpyAsync(x, src, 3 * b, cudaMemcpyDeviceToHost, c->stream));
+        GM_CUDA(c, cudaMemcpyAsync(x, src, 3 * b, cudaMemcpyDeviceToHost, s));
         return GM_OK;
     }
-    if (x) GM_CUDA(c, cudaMemcpyAsync(x, src, b, cudaMemcpyDeviceToHost, c->stream));
-    if (y) GM_CUDA(c, cudaMemcpyAsync(y, src + c->n, b, cudaMemcpyDeviceToHost, c->stream));
-    if (z) GM_CUDA(c, cudaMemcpyAsync(z, src + 2 * c->n, b, cudaMemcpyDeviceToHost, c->stream));
+    if (x) GM_CUDA(c, cudaMemcpyAsync(x, src, b, cudaMemcpyDeviceToHost, s));
+    if (y) GM_CUDA(c, cudaMemcpyAsync(y, src + c->n, b, cudaMemcpyDeviceToHost, s));
+    if (z) GM_CUDA(c, cudaMemcpyAsync(z, src + 2 * c->n, b, cudaMemcpyDeviceToHost, s));
     return GM_OK;
 }
 
@@ -849,7 +856,9 @@ int run_direct(gm_ctx *c, double dt, int64_t n_steps);
 
 // n resident steps (one graph launch each, or direct launches), then the
 // closing half-kick; nothing waits for the device.
-int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
+// The steps themselves: after them the resident positions are final (the
+// rest of the call evaluates forces and the closing half-kick).
+int launch_loop(gm_ctx *c, double dt, int64_t n_steps) {
     const bool pf = persistent_form(c) && n_steps > 0;
     int rc = pf ? begin_persistent(c, true) : GM_OK;
     if (rc) return rc;
@@ -864,18 +873,31 @@ int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
     // the steps' force evaluations leave the energy partials unsummed (the
     // flag that seq_forces sets is set only when a graph is captured)
     if (n_steps > 0) c->energy_stale = true;
-    if (!rc && pf) rc = end_persistent(c);
+    return rc;
+}
+
+// After launch_loop: the persistent form's forces at the final positions,
+// then the pending closing half-kick.
+int launch_end(gm_ctx *c, double dt, int64_t n_steps) {
+    int rc = persistent_form(c) && n_steps > 0 ? end_persistent(c) : GM_OK;
     return rc ? rc : finish_steps(c, dt);
+}
+
+int launch_steps(gm_ctx *c, double dt, int64_t n_steps) {
+    int rc = launch_loop(c, dt, n_steps);
+    return rc ? rc : launch_end(c, dt, n_steps);
 }
 
 // Caller positions into the context.  When the resident forces are current
 // and the caller hands back the resident positions (bit for bit), the forces
 // stay valid; one read of the device's comparison decides.
-int stage_positions(gm_ctx *c, const double *px, const double *py, const double *pz) {
+// `cleared`: the status word's comparison flag is zero already (the status
+// reset kernel ran on the stream).
+int stage_positions(gm_ctx *c, const double *px, const double *py, const double *pz, bool cleared = false) {
     if (!c->forces_current) return upload3(c, c->d_pos, px, py, pz);
     int rc = upload3(c, c->d_dref, px, py, pz);
     if (rc) return rc;
-    GM_CUDA(c, cudaMemsetAsync(&c->d_status->differs, 0, sizeof(unsigned int), c->stream));
+    if (!cleared) GM_CUDA(c, cudaMemsetAsync(&c->d_status->differs, 0, sizeof(unsigned int), c->stream));
     gm_launch_differs(c->n, c->d_dref, c->d_pos, &c->d_status->differs, c->stream);
     c->launches++;
     GM_CUDA(c, cudaMemcpyAsync(&c->h_status->differs, &c->d_status->differs, sizeof(unsigned int),
@@ -1221,6 +1243,10 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     if (cudaSetDevice(c->device) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking) != cudaSuccess) return bail(GM_ERR_DEVICE);
+    if (cudaEventCreateWithFlags(&c->ev_xfer_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_xfer_out, cudaEventDisableTiming) != cudaSuccess)
+        return bail(GM_ERR_DEVICE);
     if (cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         return bail(GM_ERR_DEVICE);
@@ -1571,6 +1597,9 @@ int32_t gm_destroy(gm_ctx *c) {
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->xfer) cudaStreamDestroy(c->xfer);
+    if (c->ev_xfer_in) cudaEventDestroy(c->ev_xfer_in);
+    if (c->ev_xfer_out) cudaEventDestroy(c->ev_xfer_out);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
@@ -1945,7 +1974,9 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
     // Two host synchronisations per call: the check whether the caller's
     // positions are the resident ones (forces stay valid), and the results
     // with the status word at the end.  The status reset, the step number and
-    // the call's rebuild base are set on the device.
+    // the call's rebuild base are set on the device.  The velocity upload
+    // runs on a copy stream beside the position check, the position download
+    // beside the forces at the final positions.
     if (!c || !(dt > 0) || n_steps < 0) return GM_ERR_INVALID_ARGUMENT;
     GM_CUDA(c, cudaSetDevice(c->device));
     // positions are checked for finiteness on the device when the resident
@@ -1958,13 +1989,35 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
     }
     gm_launch_status_reset(c->d_status, 1, first_step, c->stream);
     c->launches++;
-    int rc = stage_positions(c, px, py, pz);
-    if (!rc) rc = upload3(c, c->d_vel, vx, vy, vz);
-    if (!rc) rc = ensure_forces(c);
-    if (!rc) rc = launch_steps(c, dt, n_steps);
+    // the velocities travel on the copy stream, after the work already on
+    // the context's stream and beside the position check
+    GM_CUDA(c, cudaEventRecord(c->ev_xfer_in, c->stream));
+    GM_CUDA(c, cudaStreamWaitEvent(c->xfer, c->ev_xfer_in, 0));
+    int rc = upload3(c, c->d_vel, vx, vy, vz, c->xfer);
     if (rc) return rc;
-    rc = download3(c, c->d_pos, px, py, pz);
-    if (!rc) rc = download3(c, c->d_vel, vx, vy, vz);
+    GM_CUDA(c, cudaEventRecord(c->ev_xfer_out, c->xfer));
+    rc = stage_positions(c, px, py, pz, true);
+    if (!rc) rc = cudaStreamWaitEvent(c->stream, c->ev_xfer_out, 0) == cudaSuccess ? GM_OK
+                  : fail(c, GM_ERR_DEVICE, "cudaStreamWaitEvent");
+    if (!rc) rc = ensure_forces(c);
+    if (!rc) rc = launch_loop(c, dt, n_steps);
+    if (rc) {
+        cudaStreamSynchronize(c->xfer);
+        return rc;
+    }
+    // the final positions go out on the copy stream while the forces at
+    // them and the closing half-kick run
+    GM_CUDA(c, cudaEventRecord(c->ev_xfer_in, c->stream));
+    GM_CUDA(c, cudaStreamWaitEvent(c->xfer, c->ev_xfer_in, 0));
+    rc = download3(c, c->d_pos, px, py, pz, c->xfer);
+    if (!rc) GM_CUDA(c, cudaEventRecord(c->ev_xfer_out, c->xfer));
+    if (!rc) rc = launch_end(c, dt, n_steps);
+    if (!rc) GM_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_xfer_out, 0));
+    if (rc) {
+        cudaStreamSynchronize(c->xfer);
+        return rc;
+    }
+    rc = download3(c, c->d_vel, vx, vy, vz);
     if (!rc && (fx || fy || fz)) {
         gm_launch_forces_out(c->n, c->d_force, c->d_fout, c->stream);
         c->launches++;

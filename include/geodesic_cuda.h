@@ -270,7 +270,8 @@ int32_t gm_pair_shape(gm_ctx *ctx, int32_t split, int32_t warps_per_block, int32
  *                       evaluated by the force kernels after the last launch.
  * Both forms give the same bits.  GM_ERR_UNSUPPORTED for an FP64 or
  * constrained context; with trajectory frames enabled the graph form runs.
- * The default is GM_STEP_GRAPH. */
+ * The default is GM_STEP_PERSISTENT (the kernel graph for FP64 and
+ * constrained contexts). */
 enum { GM_STEP_GRAPH = 0, GM_STEP_PERSISTENT = 1 };
 int32_t gm_step_form(gm_ctx *ctx, int32_t form);
 
