@@ -307,7 +307,7 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     tp, hp = pinned_like(state.pos)
     tv, hv = pinned_like(state.vel)
     be.download_state(hp, hv)
-    n_e2e = max(20, min(args.steps, 500))
+    n_e2e = max(200, min(args.steps, 500))  # host-timed calls: enough of them to average the host jitter
     be.steps(hp, hv, DT_PS, 1)
     t0 = time.perf_counter()
     for _ in range(n_e2e):
