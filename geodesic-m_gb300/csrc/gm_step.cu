@@ -99,23 +99,12 @@ step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
         const int cb = (fa.n_bonds + fa.n_angles + fa.n_diheds + kTermsPerTicket - 1) / kTermsPerTicket;
         const int c14 = (fa.n14 + kTermsPerTicket - 1) / kTermsPerTicket;
         const int nbw = cb + c14, total = n_pair + nbw;
-        // the bonded tickets (FP64, the longest items) spread over the first
-        // three fifths of the queue, so that none of them runs in its tail
-        const int stride = nbw > 0 ? max(1, (int)((long long)total * 3 / 5 / nbw)) : 1;
-        // a warp takes its next ticket before working on the current one and
-        // prefetches that item's list block into L2 meanwhile
-        int t = 0;
-        if (lane == 0) t = (int)atomicAdd(&sy->ticket, 1u);
-        t = __shfl_sync(full, t, 0);
-        while (t < total) {
-            int tn = 0;
-            if (lane == 0) tn = (int)atomicAdd(&sy->ticket, 1u);
-            tn = __shfl_sync(full, tn, 0);
-            if (tn < total) {
-                const int qn = tn / stride;
-                if (!(tn - qn * stride == 0 && qn < nbw))
-                    prefetch_item_list(tn - min(qn + 1, nbw), lane, fa.cap, fa.split, fa.list, fa.gmax);
-            }
+        const int stride = nbw > 0 ? total / nbw : 1;
+        for (;;) {
+            int t = 0;
+            if (lane == 0) t = (int)atomicAdd(&sy->ticket, 1u);
+            t = __shfl_sync(full, t, 0);
+            if (t >= total) break;
             const int q = t / stride, r = t - q * stride;
             if (r == 0 && q < nbw) {
                 unsigned bad = 0;
@@ -135,7 +124,6 @@ step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
                     item, lane, fa.n, fa.cap, fa.split, fa.coord, fa.perm, fa.list, fa.count, fa.gmax, fa.ntypes,
                     fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st, fa.group_sys, nullptr);
             }
-            t = tn;
         }
     }
     // ---- 2. every force is summed
