@@ -126,6 +126,8 @@ struct gm_ctx {
     // status
     DevStatus *d_status = nullptr;
     DevStatus *h_status = nullptr;  // pinned
+    double *h_energy = nullptr;     // pinned: the energy read back with the results (a copy into
+                                    // pageable memory would block the host until it completes)
     // graph
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -1569,6 +1571,7 @@ gm_ctx *create_impl(int n_sys, const gm_atoms *sys_atoms, const gm_topology *sys
     TRY(dalloc(c, &c->d_sync, 1));
     if (cudaMemset(c->d_sync, 0, sizeof(StepSync)) != cudaSuccess) return bail(GM_ERR_DEVICE);
     if (cudaMallocHost((void **)&c->h_status, sizeof(DevStatus)) != cudaSuccess) return bail(GM_ERR_OUT_OF_MEMORY);
+    if (cudaMallocHost((void **)&c->h_energy, sizeof(double)) != cudaSuccess) return bail(GM_ERR_OUT_OF_MEMORY);
     DevStatus z{};
     z.fail_step = ~0ull;
     if (cudaMemcpy(c->d_status, &z, sizeof z, cudaMemcpyHostToDevice) != cudaSuccess) return bail(GM_ERR_DEVICE);
@@ -1595,6 +1598,7 @@ int32_t gm_destroy(gm_ctx *c) {
     if (c->graph) cudaGraphDestroy(c->graph);
     for (void *ptr : c->allocs) cudaFree(ptr);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_energy) cudaFreeHost(c->h_energy);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->xfer) cudaStreamDestroy(c->xfer);
@@ -1657,9 +1661,11 @@ int32_t gm_compute_forces(gm_ctx *c, const double *px, const double *py, const d
     c->launches++;
     rc = download3(c, c->d_fout, fx, fy, fz);
     if (rc) return poison(rc);
-    if (energy) GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (energy)
+        GM_CUDA(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     rc = check_status(c, nullptr);
     if (rc) return poison(rc);
+    if (energy) *energy = *c->h_energy;
     c->forces_current = true;
     return GM_OK;
 }
@@ -2025,11 +2031,12 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
     }
     if (!rc && energy) {
         refresh_energy(c);
-        GM_CUDA(c, cudaMemcpyAsync(energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        GM_CUDA(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
     GM_CUDA(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->stream));
     GM_CUDA(c, cudaStreamSynchronize(c->stream));
     GM_CUDA(c, cudaGetLastError());
+    if (!rc && energy) *energy = *c->h_energy;
     if (n_rebuilds) *n_rebuilds = (int64_t)(c->h_status->n_rebuilds - c->h_status->rebuild_base);
     const int rs = status_result(c, err);
     return rs ? rs : rc;

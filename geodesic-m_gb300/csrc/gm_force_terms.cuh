@@ -39,22 +39,6 @@ __device__ __forceinline__ void image_df(float &dh, float &dl, float L, float Ll
     dh = q;
 }
 
-// The list block of pair item wid (entries [e_begin, e_end) of its group's
-// 32 columns, contiguous: 128 bytes per entry) into L2 with one bulk
-// prefetch, issued by lane 0 ahead of the item.
-__device__ __forceinline__ void prefetch_item_list(int wid, int lane, int cap, int split, const int *list,
-                                                   const int *gmax) {
-    if (lane != 0) return;
-    const int group = wid / split, part = wid - group * split;
-    const int gm = __ldg(gmax + group);
-    const int per = ((gm + split - 1) / split + kChunk - 1) / kChunk * kChunk;
-    const int e_begin = part * per, e_end = min(gm, e_begin + per);
-    if (e_end <= e_begin) return;
-    const int *a = list + (size_t)group * 32 * cap + (size_t)e_begin * 32;
-    const unsigned bytes = (unsigned)(e_end - e_begin) * 128u;
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(bytes) : "memory");
-}
-
 // One work item of the mixed-precision nonbonded kernel (force/nonbonded.rs:20-82
 // physics plus the switched Coulomb term): FP32 operations throughout, arranged as
 // double-float arithmetic so that each pair's force carries ~1e-10 relative
