@@ -410,11 +410,23 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
 // slot, so the order in which the branches add changes no bit.  Without
 // `energy` the partials stay unsummed (energy_stale) until refresh_energy.
 // `packed`: the step kernel before it already packed the coordinates.
+bool persistent_form(const gm_ctx *c);
+int persistent_grid(gm_ctx *c);
+
 int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr, bool packed = false) {
     ListArgs la = list_args(c);
     if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);
     if (!packed) gm_launch_pack(la, c->fp64, s);
     ForceArgs fa = force_args(c);
+    if (persistent_form(c) && persistent_grid(c) == GM_OK) {
+        // the persistent form evaluates forces with its own force phase: the
+        // pair items and the bonded / 1-4 blocks from one queue, one launch,
+        // the same sums and energy partials as the kernels below
+        gm_launch_forces_persistent(fa, c->d_sync, c->persist_blocks, s);
+        if (energy) gm_launch_energy(fa, s);
+        c->energy_stale = !energy;
+        return (packed ? 0 : 1) + 1 + (energy ? 1 : 0);
+    }
     const bool fork = branch && (c->bonded_blocks || c->blocks14);
     const cudaStream_t sb = fork ? branch : s;
     if (fork) {
@@ -717,7 +729,8 @@ int begin_persistent(gm_ctx *c, bool fresh) {
 }
 
 // After the last persistent launch of a call: the forces at the final
-// positions, by the force kernels (the launches left the coordinates packed).
+// positions, by the force phase alone (the launches left the coordinates
+// packed).
 int end_persistent(gm_ctx *c) {
     c->launches += seq_forces(c, c->stream, false, c->side, true);
     GM_CUDA(c, cudaGetLastError());

@@ -381,6 +381,10 @@ struct StepArgs {
 int gm_step_persistent_blocks(const ForceArgs &fa);
 void gm_launch_step_persistent(const ForceArgs &fa, const StepArgs &sa, const PackArgs &pk, int blocks,
                                cudaStream_t s);
+// The persistent kernel's force phase alone, with energies (the force
+// kernels' partials, the same bits), as a plain launch: pair items and bonded
+// / 1-4 blocks from one queue.  The queue words must be zero.
+void gm_launch_forces_persistent(const ForceArgs &fa, StepSync *sync, int blocks, cudaStream_t s);
 void gm_launch_kick_drift_check(int n, double *pos, double *vel, double *dref, long long *force,
                                 const double *inv_mass, double dt_half, double dt, const double *ref, double thr_sq,
                                 DevStatus *st, unsigned long long cond, const int *atom_sys, unsigned int *sys_flag,

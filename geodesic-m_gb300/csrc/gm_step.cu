@@ -77,7 +77,31 @@ __device__ bool grid_barrier(StepSync *sy, DevStatus *st) {
     return s_ok != 0;
 }
 
-template <bool PERIODIC, bool COULOMB, bool BATCH, bool MI>
+// A 64-term block of bonded terms (or 1-4 pairs) by one warp, two terms a
+// lane, with the energy partial and the per-system energies of term_block
+// (gm_force.cu): lane l holds terms l and l + 32, and the shuffle-down tree
+// adds in the order of its shared-memory tree, so the partial has the same
+// bits.
+template <bool MI, bool P14>
+__device__ __forceinline__ void term_block_warp(const ForceArgs &fa, int blk, int lane, unsigned &bad) {
+    int f0 = -1, f1 = -1;
+    const int t = blk * GM_BONDED_THREADS + lane;
+    const double e0 = P14 ? pair14_term<MI>(fa, t, bad, f0) : bonded_term<MI>(fa, t, bad, f0);
+    const double e1 = P14 ? pair14_term<MI>(fa, t + 32, bad, f1) : bonded_term<MI>(fa, t + 32, bad, f1);
+    if (fa.e_sys) {
+        gm_add_sys_energy(fa.e_sys, f0 >= 0 ? fa.atom_sys[f0] : -1, e0);
+        gm_add_sys_energy(fa.e_sys, f1 >= 0 ? fa.atom_sys[f1] : -1, e1);
+    }
+    double v = e0 + e1;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0 && blk < (P14 ? fa.blocks14 : fa.bonded_blocks)) (P14 ? fa.epart14 : fa.epart_bonded)[blk] = v;
+}
+
+// STEP: one BAB step (phases 1-3 above, a cooperative launch).  !STEP: phase
+// 1 alone with energies (the pair items' partials, the 64-term blocks'
+// partials and the per-system energies of the force kernels, the same bits),
+// a plain launch; its last warp clears the queue words.
+template <bool PERIODIC, bool COULOMB, bool BATCH, bool MI, bool STEP>
 __global__ void __launch_bounds__(kStepThreads, kStepMinBlocks)
 step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
     extern __shared__ float4 s_tab[];
@@ -86,7 +110,7 @@ step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
     const int lane = threadIdx.x & 31;
     const unsigned full = 0xffffffffu;
     // read by every block before the barrier; block 0 clears it after
-    const bool fresh = sy->fresh != 0;
+    const bool fresh = STEP && sy->fresh != 0;
     // ---- 1. forces at the current positions
     if (!fresh) {
         if (!BATCH) {
@@ -108,23 +132,43 @@ step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
             const int q = t / stride, r = t - q * stride;
             if (r == 0 && q < nbw) {
                 unsigned bad = 0;
-                int first = -1;
                 const bool b14 = q >= cb;
-                const int base = (b14 ? q - cb : q) * kTermsPerTicket + lane;
-                for (int u = 0; u < kTermsPerTicket; u += 32) {
-                    if (b14) pair14_term<MI>(fa, base + u, bad, first);
-                    else bonded_term<MI>(fa, base + u, bad, first);
+                if (STEP) {
+                    int first = -1;
+                    const int base = (b14 ? q - cb : q) * kTermsPerTicket + lane;
+                    for (int u = 0; u < kTermsPerTicket; u += 32) {
+                        if (b14) pair14_term<MI>(fa, base + u, bad, first);
+                        else bonded_term<MI>(fa, base + u, bad, first);
+                    }
+                } else {
+                    const int blk0 = (b14 ? q - cb : q) * (kTermsPerTicket / GM_BONDED_THREADS);
+                    for (int h = 0; h < kTermsPerTicket / GM_BONDED_THREADS; h++) {
+                        if (b14) term_block_warp<MI, true>(fa, blk0 + h, lane, bad);
+                        else term_block_warp<MI, false>(fa, blk0 + h, lane, bad);
+                    }
                 }
                 bad = __reduce_or_sync(full, bad);
                 if (bad && lane == 0) atomicOr(&st->error, bad);
             } else {
                 // bonded tickets at or before t: min(q + 1, nbw)
                 const int item = t - min(q + 1, nbw);
-                pair_item_mixed<PERIODIC, COULOMB, BATCH, false>(
+                pair_item_mixed<PERIODIC, COULOMB, BATCH, !STEP>(
                     item, lane, fa.n, fa.cap, fa.split, fa.coord, fa.perm, fa.list, fa.count, fa.gmax, fa.ntypes,
-                    fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st, fa.group_sys, nullptr);
+                    fa.tab32, s_tab, fa.pc, fa.force, fa.epart, st, fa.group_sys, STEP ? nullptr : fa.e_sys);
             }
         }
+    }
+    if (!STEP) {
+        // the last warp out leaves the queue words at zero for the next launch
+        if (lane == 0) {
+            __threadfence();
+            const unsigned warps = gridDim.x * (blockDim.x / 32);
+            if (atomicAdd(&sy->arrive, 1u) == warps - 1) {
+                atomicExch(&sy->ticket, 0u);
+                atomicExch(&sy->arrive, 0u);
+            }
+        }
+        return;
     }
     // ---- 2. every force is summed
     if (!grid_barrier(sy, st)) return;
@@ -194,8 +238,9 @@ step_persistent_kernel(ForceArgs fa, StepArgs sa, PackArgs pk) {
 
 using StepKernel = void (*)(ForceArgs, StepArgs, PackArgs);
 
+template <bool STEP>
 StepKernel pick(const ForceArgs &fa, bool gtab) {
-#define GM_STEPK(P, Q, B, M) return step_persistent_kernel<P, Q, B, M>
+#define GM_STEPK(P, Q, B, M) return step_persistent_kernel<P, Q, B, M, STEP>
 #define GM_STEPB(P, Q, M) { if (gtab) GM_STEPK(P, Q, true, M); else GM_STEPK(P, Q, false, M); }
 #define GM_STEPQ(P, M) { if (fa.coulomb) GM_STEPB(P, true, M) else GM_STEPB(P, false, M) }
     if (fa.bonded_mi) GM_STEPQ(true, true)
@@ -220,7 +265,7 @@ int gm_step_persistent_blocks(const ForceArgs &fa) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick(fa, gtab), kStepThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pick<true>(fa, gtab), kStepThreads, smem) != cudaSuccess)
         return 0;
     return per_sm * sms;
 }
@@ -238,5 +283,14 @@ void gm_launch_step_persistent(const ForceArgs &fa, const StepArgs &sa, const Pa
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, pick(fa, gtab), fa, sa, pk);
+    cudaLaunchKernelEx(&cfg, pick<true>(fa, gtab), fa, sa, pk);
+}
+
+void gm_launch_forces_persistent(const ForceArgs &fa, StepSync *sync, int blocks, cudaStream_t s) {
+    const bool gtab = global_table(fa);
+    StepArgs sa{};
+    sa.sync = sync;
+    PackArgs pk{};
+    const size_t smem = gtab ? 0 : sizeof(float4) * (size_t)fa.ntypes * fa.ntypes;
+    pick<false>(fa, gtab)<<<blocks, kStepThreads, smem, s>>>(fa, sa, pk);
 }
