@@ -2411,11 +2411,29 @@ int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
                 c->launches += reps + 1;
                 if (ms < best) { best = ms; bs = sp; bw = w; bg = c->pair_grid; }
             }
+    c->pair_warps = bw;
+    c->pair_grid = bg;
+    if (persistent_form(c) && persistent_grid(c) == GM_OK) {
+        // the persistent form's split is the one its own force phase (pair
+        // items and bonded blocks from one queue) runs fastest with
+        double bestp = 1e300;
+        for (int sp : splits) {
+            c->split = sp;
+            ForceArgs fa = force_args(c);
+            gm_launch_forces_persistent(fa, c->d_sync, c->persist_blocks, c->stream);  // warm-up
+            cudaEventRecord(e0, c->stream);
+            for (int r = 0; r < reps; r++) gm_launch_forces_persistent(fa, c->d_sync, c->persist_blocks, c->stream);
+            cudaEventRecord(e1, c->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            c->launches += reps + 1;
+            if (ms < bestp) { bestp = ms; bs = sp; }
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->split = bs;
-    c->pair_warps = bw;
-    c->pair_grid = bg;
     GM_CUDA(c, cudaGetLastError());
     // the timing runs added forces many times over: evaluate them once more
     c->launches += seq_forces(c, c->stream);

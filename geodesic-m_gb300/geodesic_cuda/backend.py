@@ -286,6 +286,7 @@ class CudaBackend:
         self._forces = np.zeros((3, self.n))
         self._energy = 0.0
         self._steps_out = None  # reused gm_steps out-parameters
+        self._addr_cache = {}   # id(array) -> (array, shape, strides, row addresses)
 
     def autotune(self, reps=5):
         """Pick the pair kernel's split, block size and grid by timing
@@ -439,12 +440,25 @@ class CudaBackend:
         e, nr, conv, e_ref, nr_ref, conv_ref = out
         f = np.zeros((3, self.n)) if want_forces else None
         fr = _row_addrs(f) if want_forces else (None, None, None)
-        rc = lib().gm_steps(self._h, *_row_addrs(pos), *_row_addrs(vel), dt, first_step, n_steps, *fr, e_ref,
+        rc = lib().gm_steps(self._h, *self._addrs(pos), *self._addrs(vel), dt, first_step, n_steps, *fr, e_ref,
                             nr_ref, conv_ref)
         if rc != GM_OK:
             self._check(rc, GmConvergence.from_buffer_copy(conv))
         self._energy = e.value
         return e.value, nr.value, f
+
+    def _addrs(self, a):
+        """Row addresses of a (3, N) float64 array, remembered for the arrays
+        a step loop passes call after call (the cache holds a reference, so
+        numpy cannot move their data)."""
+        hit = self._addr_cache.get(id(a))
+        if hit is not None and hit[0] is a and hit[1] == a.shape and hit[2] == a.strides:
+            return hit[3]
+        addrs = _row_addrs(a)
+        if len(self._addr_cache) >= 8:
+            self._addr_cache.clear()
+        self._addr_cache[id(a)] = (a, a.shape, a.strides, addrs)
+        return addrs
 
     def upload_state(self, pos, vel):
         self._check(lib().gm_upload_state(self._h, *_rows(np.ascontiguousarray(pos)), *_rows(np.ascontiguousarray(vel))))

@@ -244,7 +244,9 @@ int32_t gm_frames_take(gm_ctx *ctx, int64_t max_frames, float *xyz, uint64_t *st
  * (reps launches per candidate, CUDA events on the context's stream) over
  * warps per 32-atom group (1-16: list columns per warp), warps per block (2,
  * 4, 8) and grid (one work item per warp, or a persistent grid of 2-16
- * blocks per SM), and keeps the fastest.  Every candidate computes the same
+ * blocks per SM), and keeps the fastest.  In the persistent step form
+ * (gm_step_form) the split is then timed again on the persistent kernel's
+ * force phase and the fastest kept.  Every candidate computes the same force
  * bits (fixed 32-entry chunks folded into int64 sums).  choice (nullable):
  * split, warps per block, grid (0 = one item per warp). */
 int32_t gm_autotune(gm_ctx *ctx, int32_t reps, int64_t *choice);
