@@ -385,6 +385,21 @@ __device__ __forceinline__ Range dim_range(int mn, int mx, int nc, int periodic,
 
 __device__ __forceinline__ int wrapi(int c, int nc) { return c < 0 ? c + nc : (c >= nc ? c - nc : c); }
 
+// FP32 squared distance of a staged candidate from the lane's atom (both
+// relative to the group's first atom), with the periodic image; every
+// product-sum is an explicit FMA, so the candidate test and the bucket of an
+// accepted candidate see the same value.
+template <bool PERIODIC>
+__device__ __forceinline__ float rel_r2(float4 c, float mx, float my, float mz, const GridInfo &g) {
+    float dx = c.x - mx, dy = c.y - my, dz = c.z - mz;
+    if (PERIODIC) {
+        dx = fmaf(-g.box[0], rintf(dx * g.inv_box[0]), dx);
+        dy = fmaf(-g.box[1], rintf(dy * g.inv_box[1]), dy);
+        dz = fmaf(-g.box[2], rintf(dz * g.inv_box[2]), dz);
+    }
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
 // One block per group, one warp per z layer: warp `seg` tests the candidates
 // of z layer `seg` of each row box its lanes need and stages them; the block
 // then concatenates the layers into each lane's list column.
@@ -502,24 +517,12 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64, float3 bucke
                     // distance tests of all 32 staged candidates: bit k of
                     // `near` within the list radius plus the margin, of `sure`
                     // within it minus the margin
-                    unsigned near = 0, sure = 0, bkt_lo = 0, bkt_hi = 0;
+                    unsigned near = 0, sure = 0;
 #pragma unroll
                     for (int k = 0; k < 32; k++) {
-                        const float4 c = s_rel[wib][k];
-                        float dx = c.x - mx, dy = c.y - my, dz = c.z - mz;
-                        if (PERIODIC) {
-                            dx -= g.box[0] * rintf(dx * g.inv_box[0]);
-                            dy -= g.box[1] * rintf(dy * g.inv_box[1]);
-                            dz -= g.box[2] * rintf(dz * g.inv_box[2]);
-                        }
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float r2 = rel_r2<PERIODIC>(s_rel[wib][k], mx, my, mz, g);
                         near |= (r2 <= rl2_hi ? 1u : 0u) << k;
                         sure |= (r2 <= rl2_lo ? 1u : 0u) << k;
-                        // the bucket, two bits per candidate
-                        const unsigned bk = (r2 > bucket_r2.x ? 1u : 0u) + (r2 > bucket_r2.y ? 1u : 0u) +
-                                            (r2 > bucket_r2.z ? 1u : 0u);
-                        if (k < 16) bkt_lo |= bk << (2 * k);
-                        else bkt_hi |= bk << (2 * (k - 16));
                     }
                     near &= m < 32 ? (1u << m) - 1u : 0xffffffffu;
                     const int self = s - base;
@@ -547,7 +550,10 @@ build_kernel(ListArgs a, float rl2_lo, float rl2_hi, double rl2_64, float3 bucke
                                 for (int q = e0 + 8; q < e1; q++) excluded |= (a.excl[q] == jo);
                             if (excluded) continue;
                         }
-                        const int bk = (int)(((k < 16 ? bkt_lo >> (2 * k) : bkt_hi >> (2 * (k - 16)))) & 3u);
+                        // the distance bucket, for accepted candidates only
+                        // (the same r2 as the test above)
+                        const float r2 = rel_r2<PERIODIC>(s_rel[wib][k], mx, my, mz, g);
+                        const int bk = (r2 > bucket_r2.x ? 1 : 0) + (r2 > bucket_r2.y ? 1 : 0) + (r2 > bucket_r2.z ? 1 : 0);
                         if (cnt < cap_seg) {
                             my_stage[(size_t)cnt * 32] = (base + k) | (bk << GM_BUCKET_SHIFT);
 #pragma unroll
