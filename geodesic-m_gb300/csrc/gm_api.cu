@@ -413,15 +413,20 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
 bool persistent_form(const gm_ctx *c);
 int persistent_grid(gm_ctx *c);
 
+// Mixed-precision contexts in the persistent step form (the default)
+// evaluate forces with the persistent kernel's force phase, constrained ones
+// too: the phase only evaluates forces.
+bool force_phase(const gm_ctx *c) { return c->step_form == 1 && !c->fp64 && c->n > 0; }
+
 int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr, bool packed = false) {
     ListArgs la = list_args(c);
     if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);
     if (!packed) gm_launch_pack(la, c->fp64, s);
     ForceArgs fa = force_args(c);
-    if (persistent_form(c) && persistent_grid(c) == GM_OK) {
-        // the persistent form evaluates forces with its own force phase: the
-        // pair items and the bonded / 1-4 blocks from one queue, one launch,
-        // the same sums and energy partials as the kernels below
+    if (force_phase(c) && persistent_grid(c) == GM_OK) {
+        // the persistent kernel's force phase: the pair items and the bonded
+        // / 1-4 blocks from one queue, one launch, the same sums and energy
+        // partials as the kernels below
         gm_launch_forces_persistent(fa, c->d_sync, c->persist_blocks, s);
         if (energy) gm_launch_energy(fa, s);
         c->energy_stale = !energy;
@@ -816,8 +821,8 @@ int issue_step_tail(gm_ctx *c, cudaStream_t s, double dt, long long *count) {
 
 int capture_graph(gm_ctx *c, double dt) {
     if (c->graph_exec && c->graph_dt == dt && c->graph_cap == c->cap) return GM_OK;
-    if (persistent_form(c)) {
-        int rc = persistent_grid(c);  // the grid size goes into the captured launch
+    if (force_phase(c)) {
+        int rc = persistent_grid(c);  // the grid size goes into the captured launches
         if (rc) return rc;
     }
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
@@ -2413,9 +2418,10 @@ int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
             }
     c->pair_warps = bw;
     c->pair_grid = bg;
-    if (persistent_form(c) && persistent_grid(c) == GM_OK) {
-        // the persistent form's split is the one its own force phase (pair
-        // items and bonded blocks from one queue) runs fastest with
+    if (force_phase(c) && persistent_grid(c) == GM_OK) {
+        // with the persistent kernel's force phase (pair items and bonded
+        // blocks from one queue) the split is the one that phase runs
+        // fastest with
         double bestp = 1e300;
         for (int sp : splits) {
             c->split = sp;

@@ -273,7 +273,10 @@ int32_t gm_pair_shape(gm_ctx *ctx, int32_t split, int32_t warps_per_block, int32
  * Both forms give the same bits.  GM_ERR_UNSUPPORTED for an FP64 or
  * constrained context; with trajectory frames enabled the graph form runs.
  * The default is GM_STEP_PERSISTENT (the kernel graph for FP64 and
- * constrained contexts). */
+ * constrained contexts).  In mixed precision with GM_STEP_PERSISTENT every
+ * force evaluation outside the persistent launches (gm_compute_forces, list
+ * builds, the constrained step graph) runs as the persistent kernel's force
+ * phase alone: one launch over the same work queue, the same bits. */
 enum { GM_STEP_GRAPH = 0, GM_STEP_PERSISTENT = 1 };
 int32_t gm_step_form(gm_ctx *ctx, int32_t form);
 
