@@ -607,8 +607,13 @@ def run_warm_start(args):
     b.close()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
     out = {}
-    for name, warm in (("cold", False), ("warm", True)):
+    # cold and warm with the default force evaluation (the persistent
+    # kernel's force phase), and cold once more with the kernel graph's pair
+    # kernel beside the bonded kernel
+    for name, warm in (("cold", False), ("warm", True), ("cold_kernel_graph_forces", False)):
         be = backend.CudaBackend(ev[0], ev[1], p)
+        if name == "cold_kernel_graph_forces":
+            be.step_form(backend.STEP_GRAPH)
         be.upload_state(np.ascontiguousarray(ev[2].pos), np.ascontiguousarray(ev[2].vel))
         be.forces_resident()
         if warm:
@@ -635,7 +640,7 @@ def run_warm_start(args):
                                    "2 fs, tol 1e-10", "train_seed": SEED + 7, "eval_seed": SEED,
                        "train_steps_recorded": args.train_steps, "train_samples": int(n_samples),
                        "train_iters": args.train_iters, "l2": "flushed between timed steps"},
-            "cold": out["cold"], "warm": out["warm"],
+            "cold": out["cold"], "warm": out["warm"], "cold_kernel_graph_forces": out["cold_kernel_graph_forces"],
             "warm_over_cold_ns_per_day": round(out["warm"]["ns_per_day"] / out["cold"]["ns_per_day"], 3),
             "train_loss_standardised": round(loss, 5), "train_s": round(t_train, 2), "generation_s": round(t_gen, 1)}
 
