@@ -474,11 +474,12 @@ def _time_batch(be, args, flush, form):
 
 
 def run_ensemble(args):
-    """configs[3]: 256 independent systems, N log-uniform in [500, 20000],
-    per-system seeds, MB 300 K, mixed precision: one context, one graph
-    launch per step for the whole batch, pair kernel shape from the
+    """The batched ensemble: 256 independent systems, N log-uniform in
+    [500, 20000], per-system seeds, MB 300 K, mixed precision: one context,
+    one graph launch per step for the whole batch (one persistent launch
+    inside it, and the kernel graph for comparison), split from the
     autotuner; against the same systems run one by one (each in its own
-    context and graph)."""
+    context)."""
     import multiprocessing as mp
     rng = np.random.default_rng(SEED)
     n_sys = args.systems
@@ -541,12 +542,13 @@ def run_ensemble(args):
 
 
 def run_warm_start(args):
-    """configs[4]: 50,000 atoms with 40 % hydrogens (H bonds constrained at
-    1.09 A), FP64 SHAKE/RATTLE to 1e-10: the network is trained on solver
-    multipliers of a different seed (2,000 recorded steps), then the same
-    run is timed cold and warm-started.  At 2 fs: with H at 1.008 amu and only
-    the H bonds constrained this lattice fails within 20 steps at 4 fs and
-    within ~1,000 at 3 fs (the oracle fails the same way)."""
+    """The constrained warm-start workload: 50,000 atoms with 40 % hydrogens
+    (H bonds constrained at 1.09 A), FP64 SHAKE/RATTLE to 1e-10: the network
+    is trained on solver multipliers of a different seed (2,000 recorded
+    steps), then the same run is timed cold and warm-started.  At 2 fs: with
+    H at 1.008 amu and only the H bonds constrained this lattice fails within
+    20 steps at 4 fs and within ~1,000 at 3 fs (the oracle fails the same
+    way)."""
     import torch
     from geodesic_cuda import amber, backend, synth
     torch.cuda.set_device(0)
@@ -646,8 +648,8 @@ def run_warm_start(args):
 
 
 def run_scaled(args, n_atoms, precision, relax, steps_default):
-    """configs[2] (1,000,000 atoms, mixed, 200 steps) and configs[0] (5,000
-    atoms, FP64, 1,000 steps): timed device steps, list rebuild and pair
+    """The 1,000,000-atom scale test (mixed, 200 steps) and the 5,000-atom
+    system (FP64, 1,000 steps): timed device steps, list rebuild and pair
     kernel bandwidth."""
     import torch
     from geodesic_cuda import backend, synth
