@@ -109,6 +109,7 @@ struct gm_ctx {
     int *d_atom_cstart = nullptr, *d_atom_cref = nullptr;
     float4 *d_ws_unit = nullptr;
     float *d_ws_w = nullptr;
+    unsigned char *d_ws_packed = nullptr;  // the parameters in the inference's layout (gm_launch_ws_pack)
     float *d_ws_params = nullptr, *d_ws_norm = nullptr, *d_ws_m = nullptr, *d_ws_v = nullptr, *d_ws_feat = nullptr,
           *d_rec_feat = nullptr, *d_rec_t = nullptr, *d_ws_partial = nullptr, *d_ws_out = nullptr;
     double *d_ws_scale = nullptr, *d_ws_t1 = nullptr, *d_ws_lam0 = nullptr, *d_lam_sum = nullptr,
@@ -374,7 +375,7 @@ long long issue_shake(gm_ctx *c, cudaStream_t s, bool resident) {
         f.constr_i = c->d_ci; f.constr_j = c->d_cj; f.constr_dsq = c->d_cdsq; f.inv_mass = c->d_inv_mass;
         f.atom_cstart = c->d_atom_cstart; f.atom_cref = c->d_atom_cref; f.pos = c->d_pos; f.dref = c->d_dref;
         f.feat = c->d_ws_feat; f.scale = c->d_ws_scale; f.t1 = c->d_ws_t1; f.unit = c->d_ws_unit; f.w = c->d_ws_w;
-        gm_launch_ws_predict(f, c->d_ws_params, c->d_ws_norm, c->d_ws_lam0, c->ws_on, s);
+        gm_launch_ws_predict(f, c->d_ws_packed, c->d_ws_lam0, c->ws_on, s);
         k += 2;
     }
     k += gm_launch_shake_solve(a, c->n, c->d_pos, s);
@@ -1077,6 +1078,7 @@ int ws_alloc_model(gm_ctx *c) {
     if (c->d_ws_params) return GM_OK;
     int rc = dalloc(c, &c->d_ws_params, GM_WS_NPAR);
     if (!rc) rc = dalloc(c, &c->d_ws_norm, GM_WS_NNORM);
+    if (!rc) rc = dalloc(c, &c->d_ws_packed, gm_ws_packed_bytes());
     if (!rc) rc = dalloc(c, &c->d_ws_m, GM_WS_NPAR);
     if (!rc) rc = dalloc(c, &c->d_ws_v, GM_WS_NPAR);
     if (!rc) rc = dalloc(c, &c->d_ws_out, GM_WS_NPAR + 1);
@@ -2149,7 +2151,8 @@ int32_t gm_ws_train(gm_ctx *c, int64_t iters, int32_t blocks, double lr, uint64_
         gm_launch_ws_update(blocks, c->d_ws_partial, c->d_ws_params, c->d_ws_m, c->d_ws_v, (float)lr_t, 0.9f, 0.999f,
                             1e-8f, (int)(it + 1), c->d_ws_out, s);
     }
-    c->launches += 2 + 2 * iters;
+    gm_launch_ws_pack(c->d_ws_params, c->d_ws_norm, c->d_ws_packed, s);  // the inference's layout
+    c->launches += 3 + 2 * iters;
     GM_CUDA(c, cudaGetLastError());
     float loss = 0.0f;
     GM_CUDA(c, cudaMemcpyAsync(&loss, c->d_ws_out, sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -2182,7 +2185,12 @@ int32_t gm_ws_params(gm_ctx *c, float *get_params, float *get_norm, const float 
     if ((get_params || get_norm) && !c->ws_model) return fail(c, GM_ERR_NOT_BUILT, "no warm-start model");
     if (get_params) GM_CUDA(c, cudaMemcpy(get_params, c->d_ws_params, sizeof(float) * GM_WS_NPAR, cudaMemcpyDeviceToHost));
     if (get_norm) GM_CUDA(c, cudaMemcpy(get_norm, c->d_ws_norm, sizeof(float) * GM_WS_NNORM, cudaMemcpyDeviceToHost));
-    if (set_params || set_norm) drop_graph(c);
+    if (set_params || set_norm) {
+        gm_launch_ws_pack(c->d_ws_params, c->d_ws_norm, c->d_ws_packed, c->stream);  // the inference's layout
+        c->launches++;
+        GM_CUDA(c, cudaStreamSynchronize(c->stream));
+        drop_graph(c);
+    }
     return GM_OK;
 }
 

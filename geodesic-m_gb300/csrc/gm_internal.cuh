@@ -456,9 +456,14 @@ struct WsFeatureArgs {
 // Two launches per solve: every constraint's raw features, t1 and scale, and
 // with infer the network on the tensor cores (fused with the coupling pass)
 // and the predicted multipliers lam0[k] = (t1[k] + y_k * t_scale + t_mean) /
-// scale[k].
-void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
-                          cudaStream_t s);
+// scale[k].  `packed`: the parameters and standardisation as gm_launch_ws_pack
+// left them.
+void gm_launch_ws_predict(const WsFeatureArgs &a, const void *packed, double *lam0, bool infer, cudaStream_t s);
+// The inference's parameter block (gm_ws_packed_bytes bytes), written from
+// the parameters and the input standardisation; run after every change of
+// either.
+size_t gm_ws_packed_bytes();
+void gm_launch_ws_pack(const float *params, const float *norm, void *packed, cudaStream_t s);
 // The network's output y for m standardised inputs x[m][12] (same kernels).
 void gm_launch_ws_forward(int m, const float *x, const float *params, float *y, cudaStream_t s);
 // records raw features and targets lam_sum * scale - t1 into slot rec_n when

@@ -247,6 +247,13 @@ __device__ __forceinline__ void mlp_rows32(const MlpSmem &S, const uint32_t (*sX
 
 constexpr int kPredWarps = 4;
 
+// The network's parameters and input standardisation in the shared-memory
+// layout of the inference (fragment order), once per change of the
+// parameters, so that each inference block copies them instead of packing.
+__global__ void __launch_bounds__(256) ws_pack_kernel(const float *P, const float *norm, MlpSmem *out) {
+    load_mlp(P, norm, *out);
+}
+
 // Pass 1, one thread per constraint: its own features 0-7, t1, the scale and
 // the reference bond direction, each computed once (the FP64 part).
 __global__ void __launch_bounds__(256) ws_own_kernel(WsFeatureArgs a) {
@@ -269,13 +276,18 @@ __global__ void __launch_bounds__(256) ws_own_kernel(WsFeatureArgs a) {
 // out for the recorder), and with `infer` the warp runs the network on its 32
 // constraints and writes the predicted multipliers
 // lam0 = (t1 + y t_scale + t_mean) / scale.
-__global__ void __launch_bounds__(kPredWarps * 32) ws_predict_kernel(WsFeatureArgs a, const float *__restrict__ P,
-                                                                   const float *__restrict__ norm, double *lam0,
-                                                                   int infer) {
+__global__ void __launch_bounds__(kPredWarps * 32) ws_predict_kernel(WsFeatureArgs a,
+                                                                   const MlpSmem *__restrict__ packed,
+                                                                   double *lam0, int infer) {
     __shared__ MlpSmem S;
     __shared__ uint32_t sX[kPredWarps][32][8];
     __shared__ float sy[kPredWarps][32];
-    if (infer) load_mlp(P, norm, S);
+    if (infer) {
+        // the weights already in fragment order (ws_pack_kernel): a copy
+        const uint2 *src = reinterpret_cast<const uint2 *>(packed);
+        uint2 *dst = reinterpret_cast<uint2 *>(&S);
+        for (int i = threadIdx.x; i < (int)(sizeof(MlpSmem) / sizeof(uint2)); i += blockDim.x) dst[i] = src[i];
+    }
     __syncthreads();
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     const int n_tiles = (a.n_constr + 31) / 32;
@@ -731,12 +743,17 @@ int gm_ws_predict_blocks(int n_constr) {
     return (tiles + kPredWarps - 1) / kPredWarps;
 }
 
-void gm_launch_ws_predict(const WsFeatureArgs &a, const float *params, const float *norm, double *lam0, bool infer,
-                          cudaStream_t s) {
+void gm_launch_ws_predict(const WsFeatureArgs &a, const void *packed, double *lam0, bool infer, cudaStream_t s) {
     if (a.n_constr == 0) return;
     ws_own_kernel<<<(a.n_constr + 255) / 256, 256, 0, s>>>(a);
-    ws_predict_kernel<<<gm_ws_predict_blocks(a.n_constr), kPredWarps * 32, 0, s>>>(a, params, norm, lam0,
-                                                                                  infer ? 1 : 0);
+    ws_predict_kernel<<<gm_ws_predict_blocks(a.n_constr), kPredWarps * 32, 0, s>>>(
+        a, static_cast<const MlpSmem *>(packed), lam0, infer ? 1 : 0);
+}
+
+size_t gm_ws_packed_bytes() { return sizeof(MlpSmem); }
+
+void gm_launch_ws_pack(const float *params, const float *norm, void *packed, cudaStream_t s) {
+    ws_pack_kernel<<<1, 256, 0, s>>>(params, norm, static_cast<MlpSmem *>(packed));
 }
 
 void gm_launch_ws_forward(int m, const float *x, const float *params, float *y, cudaStream_t s) {
