@@ -43,6 +43,28 @@ STEP_FORMS = {"graph": 0, "persistent": 1}  # gm_step_form: GM_STEP_GRAPH, GM_ST
 # (93,729,280 + 2,589,952 B for 10,067,070 pairs); traffic grows with the
 # pair count, so the bench scales it to its own count
 PAIR_TRAFFIC_PER_PAIR = 96_319_232 / 10_067_070
+# The dominant kernel of a step in the persistent form, step_persistent_kernel:
+# ncu's DRAM read + write of one launch of the 50k workload at its minimised
+# start (552.3 GB/s over 197.4 us), and that launch's algorithmic bytes
+# (step_kernel_bytes of 10,067,070 pairs, 50,000 atoms, 49,999 bonds, 49,998
+# angles, 49,997 dihedrals and 1-4 pairs); the bench scales the traffic by
+# its own algorithmic bytes
+STEP_TRAFFIC_CAPTURE = 109_037_824
+STEP_BYTES_CAPTURE = 62_067_948
+
+
+def step_kernel_bytes(pairs, n_atoms, topo):
+    """Algorithmic bytes of one persistent step launch: the pair part (one
+    int32 index per half-list pair of neighbor.rs:25-43, plus per atom the
+    coordinates, charge, type, force and energy of force/nonbonded.rs:20-82:
+    4 P + 52 N), each bonded term's indices and parameters read once (bond 24
+    B, angle 28 B, dihedral 44 B, 1-4 pair 40 B: one 1-4 pair per dihedral of
+    the chain), and per atom the integrator phase's reads (position,
+    velocity, force, inverse mass, build reference, slot, charge word, system:
+    120 B) and writes (position, velocity, drift reference, the packed
+    coordinate record, the cleared force: 128 B)."""
+    nb, na, nd = len(topo.bond_i), len(topo.angle_i), len(topo.dihed_i)
+    return 4 * pairs + 52 * n_atoms + 24 * nb + 28 * na + 44 * nd + 40 * nd + 248 * n_atoms
 
 
 def ns_per_day(steps, seconds):
@@ -249,6 +271,11 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     alg_bytes = 4 * pairs + 52 * N_ATOMS
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_pair / 1e9
+    # the dominant kernel of the timed steps: in the persistent form each
+    # timed graph launch is one step_persistent_kernel (plus the rebuild IF
+    # node, which ran result["rebuilds"] times in the timed region)
+    step_bytes = step_kernel_bytes(pairs, N_ATOMS, topo)
+    t_launch = sec / args.steps
     # force / energy error of both device paths vs the FP64 oracle, at the
     # generator's raw lattice (before minimisation), at the minimised start
     # (step 0: net forces ~12x smaller than the individual terms, the hardest
@@ -341,10 +368,24 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
         "kernel_ms": {"pair": round(t_pair * 1e3, 5), "bonded": round(t_bonded * 1e3, 5),
                       "pair14": round(t_pair14 * 1e3, 5), "forces": round(t_forces * 1e3, 5),
                       "list_rebuild": round(t_rebuild * 1e3, 4), "build_kernel": round(t_build * 1e3, 4)},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
-                     "peak_source": peak_kind,
-                     "kernel": "pair_kernel_mixed", "algorithmic_bytes": alg_bytes},
+        "roofline": ({"bound": "hbm", "achieved": round(step_bytes / t_launch / 1e9, 1), "peak": peak, "unit": "GB/s",
+                      "frac": round(step_bytes / t_launch / 1e9 / peak, 4),
+                      "traffic": round(STEP_TRAFFIC_CAPTURE * step_bytes / STEP_BYTES_CAPTURE),
+                      "peak_source": peak_kind, "kernel": "step_persistent_kernel", "algorithmic_bytes": step_bytes,
+                      "launch_ms": round(t_launch * 1e3, 5),
+                      "timing": "CUDA events around each timed graph launch (one launch of the kernel, no list "
+                                "rebuild in the timed region)" if result["rebuilds"] == 0 else
+                                "CUDA events around each timed graph launch; the average includes the timed "
+                                "region's list rebuilds"}
+                     if args.step_form == "persistent" else
+                     {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                      "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
+                      "peak_source": peak_kind, "kernel": "pair_kernel_mixed", "algorithmic_bytes": alg_bytes}),
+        "pair_kernel_roofline": {"kernel": "pair_kernel_mixed", "achieved": round(achieved, 1), "unit": "GB/s",
+                                 "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
+                                 "algorithmic_bytes": alg_bytes, "ms": round(t_pair * 1e3, 5),
+                                 "note": "the pair kernel alone (gm_profile, 30 launches, warm): the pair items' "
+                                         "work without the bonded terms and the integrator"},
         "e2e": {"value": round(ns_per_day(n_e2e, t_e2e), 3), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "gm_steps (C ABI), one step per call, pinned host buffers"},
         "gpu_launches": int(result["launches"]),
