@@ -248,17 +248,27 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     n_bb = 1000
     t_bb = be.time_steps(DT_PS, n_bb, first_step=args.warmup + args.steps) / 1e3
     reb_bb = be.counters()["rebuilds"] - cb0["rebuilds"]
+    # roofline leg: 20 flushed steps at one state (the pair count and the
+    # per-launch bytes of that state), their rebuilds counted
+    n_roof = 20
+    cr0 = be.counters()
+    t_roof = be.time_steps(DT_PS, n_roof, first_step=args.warmup + args.steps + n_bb, flush_ptr=flush.data_ptr(),
+                           flush_bytes=L2_FLUSH_BYTES) / 1e3 / n_roof
+    cr1 = be.counters()
+    pairs_roof, reb_roof = cr1["pairs"], cr1["rebuilds"] - cr0["rebuilds"]
     # the other step form on the same state, the same number of flushed steps
     other = "persistent" if args.step_form == "graph" else "graph"
     be.step_form(STEP_FORMS[other])
     be.run_resident(DT_PS, 3)
     be.synchronize()
-    t_other = be.time_steps(DT_PS, args.steps, first_step=args.warmup + args.steps + n_bb + 3,
+    t_other = be.time_steps(DT_PS, args.steps, first_step=args.warmup + args.steps + n_bb + n_roof + 3,
                             flush_ptr=flush.data_ptr(), flush_bytes=L2_FLUSH_BYTES) / 1e3
     be.step_form(form)
     # roofline of the pair kernel: algorithmic bytes 4 P + 52 N per launch (one
     # int32 index per half-list pair of neighbor.rs:25-43, plus per atom the
     # coordinates, charge, type, force and energy of force/nonbonded.rs:20-82)
+    # at the list it is timed on
+    pairs_prof = be.counters()["pairs"]
     t_pair = be.profile("pair", 30) / 1e3
     t_bonded = be.profile("bonded", 30) / 1e3
     t_rebuild = be.profile("rebuild", 5) / 1e3
@@ -268,14 +278,14 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     t_pair14 = be.profile("pair14", 30) / 1e3
     t_build = be.profile("build", 5) / 1e3
     t_forces = be.profile("forces", 30) / 1e3
-    alg_bytes = 4 * pairs + 52 * N_ATOMS
+    alg_bytes = 4 * pairs_prof + 52 * N_ATOMS
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_pair / 1e9
     # the dominant kernel of the timed steps: in the persistent form each
     # timed graph launch is one step_persistent_kernel (plus the rebuild IF
-    # node, which ran result["rebuilds"] times in the timed region)
-    step_bytes = step_kernel_bytes(pairs, N_ATOMS, topo)
-    t_launch = sec / args.steps
+    # node); its bytes and time from the roofline leg's state
+    step_bytes = step_kernel_bytes(pairs_roof, N_ATOMS, topo)
+    t_launch = t_roof
     # force / energy error of both device paths vs the FP64 oracle, at the
     # generator's raw lattice (before minimisation), at the minimised start
     # (step 0: net forces ~12x smaller than the individual terms, the hardest
@@ -372,17 +382,17 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
                       "frac": round(step_bytes / t_launch / 1e9 / peak, 4),
                       "traffic": round(STEP_TRAFFIC_CAPTURE * step_bytes / STEP_BYTES_CAPTURE),
                       "peak_source": peak_kind, "kernel": "step_persistent_kernel", "algorithmic_bytes": step_bytes,
-                      "launch_ms": round(t_launch * 1e3, 5),
-                      "timing": "CUDA events around each timed graph launch (one launch of the kernel, no list "
-                                "rebuild in the timed region)" if result["rebuilds"] == 0 else
-                                "CUDA events around each timed graph launch; the average includes the timed "
-                                "region's list rebuilds"}
+                      "launch_ms": round(t_launch * 1e3, 5), "half_list_pairs": pairs_roof,
+                      "timing": f"CUDA events around each of {n_roof} graph launches (one launch of the kernel "
+                                f"each), L2 flushed between them, at the state after the timed steps; "
+                                f"{reb_roof} list rebuilds among them"}
                      if args.step_form == "persistent" else
                      {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                      "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
+                      "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs_prof),
                       "peak_source": peak_kind, "kernel": "pair_kernel_mixed", "algorithmic_bytes": alg_bytes}),
         "pair_kernel_roofline": {"kernel": "pair_kernel_mixed", "achieved": round(achieved, 1), "unit": "GB/s",
-                                 "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs),
+                                 "frac": round(achieved / peak, 4),
+                                 "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs_prof), "half_list_pairs": pairs_prof,
                                  "algorithmic_bytes": alg_bytes, "ms": round(t_pair * 1e3, 5),
                                  "note": "the pair kernel alone (gm_profile, 30 launches, warm): the pair items' "
                                          "work without the bonded terms and the integrator"},
