@@ -248,14 +248,17 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
     n_bb = 1000
     t_bb = be.time_steps(DT_PS, n_bb, first_step=args.warmup + args.steps) / 1e3
     reb_bb = be.counters()["rebuilds"] - cb0["rebuilds"]
-    # roofline leg: 20 flushed steps at one state (the pair count and the
-    # per-launch bytes of that state), their rebuilds counted
+    # roofline leg: 20 single flushed steps, each timed alone with the pair
+    # count it ran on; the median (a step that rebuilt the list is an outlier)
     n_roof = 20
-    cr0 = be.counters()
-    t_roof = be.time_steps(DT_PS, n_roof, first_step=args.warmup + args.steps + n_bb, flush_ptr=flush.data_ptr(),
-                           flush_bytes=L2_FLUSH_BYTES) / 1e3 / n_roof
-    cr1 = be.counters()
-    pairs_roof, reb_roof = cr1["pairs"], cr1["rebuilds"] - cr0["rebuilds"]
+    roof = []
+    for k in range(n_roof):
+        pr = be.counters()["pairs"]
+        ms = be.time_steps(DT_PS, 1, first_step=args.warmup + args.steps + n_bb + k, flush_ptr=flush.data_ptr(),
+                           flush_bytes=L2_FLUSH_BYTES)
+        roof.append((ms, pr))
+    roof.sort()
+    t_roof, pairs_roof = roof[n_roof // 2][0] / 1e3, roof[n_roof // 2][1]
     # the other step form on the same state, the same number of flushed steps
     other = "persistent" if args.step_form == "graph" else "graph"
     be.step_form(STEP_FORMS[other])
@@ -383,9 +386,8 @@ def _cuda_arm(args, rank, world, dev, atoms, topo, state):
                       "traffic": round(STEP_TRAFFIC_CAPTURE * step_bytes / STEP_BYTES_CAPTURE),
                       "peak_source": peak_kind, "kernel": "step_persistent_kernel", "algorithmic_bytes": step_bytes,
                       "launch_ms": round(t_launch * 1e3, 5), "half_list_pairs": pairs_roof,
-                      "timing": f"CUDA events around each of {n_roof} graph launches (one launch of the kernel "
-                                f"each), L2 flushed between them, at the state after the timed steps; "
-                                f"{reb_roof} list rebuilds among them"}
+                      "timing": f"median of {n_roof} single graph launches (one launch of the kernel each, CUDA "
+                                f"events, L2 flushed before each), at the state after the timed steps"}
                      if args.step_form == "persistent" else
                      {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                       "frac": round(achieved / peak, 4), "traffic": round(PAIR_TRAFFIC_PER_PAIR * pairs_prof),
