@@ -139,7 +139,7 @@ struct gm_ctx {
     bool use_graph = true;           // GM_GRAPH=0: direct launches (profilers)
     // step form of unconstrained mixed-precision runs: 0 the kernel graph,
     // 1 one persistent cooperative launch per step (gm_step.cu, the default)
-    int step_form = 1;
+    int step_form = GM_STEP_PERSISTENT;
     int persist_blocks = 0;          // its grid: every block resident
     StepSync *d_sync = nullptr;
     long long rebuild_base = 0;
@@ -417,7 +417,7 @@ int persistent_grid(gm_ctx *c);
 // Mixed-precision contexts in the persistent step form (the default)
 // evaluate forces with the persistent kernel's force phase, constrained ones
 // too: the phase only evaluates forces.
-bool force_phase(const gm_ctx *c) { return c->step_form == 1 && !c->fp64 && c->n > 0; }
+bool force_phase(const gm_ctx *c) { return c->step_form == GM_STEP_PERSISTENT && !c->fp64 && c->n > 0; }
 
 int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr, bool packed = false) {
     ListArgs la = list_args(c);
@@ -710,7 +710,8 @@ int download3(gm_ctx *c, const double *src, double *x, double *y, double *z, cud
 // trajectory frames (frames record each step's energy, which its launches do
 // not sum).
 bool persistent_form(const gm_ctx *c) {
-    return c->step_form == 1 && !c->fp64 && c->n_clusters == 0 && c->frame_interval == 0 && c->n > 0;
+    return c->step_form == GM_STEP_PERSISTENT && !c->fp64 && c->n_clusters == 0 && c->frame_interval == 0 &&
+           c->n > 0;
 }
 
 // Before the first persistent launch of a call: clear the barrier and queue
