@@ -50,21 +50,21 @@ PAIR_TRAFFIC_PER_PAIR = 96_319_232 / 10_067_070
 # angles, 49,997 dihedrals and 1-4 pairs); the bench scales the traffic by
 # its own algorithmic bytes
 STEP_TRAFFIC_CAPTURE = 109_037_824
-STEP_BYTES_CAPTURE = 62_067_948
+STEP_BYTES_CAPTURE = 58_668_176
 
 
 def step_kernel_bytes(pairs, n_atoms, topo):
     """Algorithmic bytes of one persistent step launch: the pair part (one
     int32 index per half-list pair of neighbor.rs:25-43, plus per atom the
     coordinates, charge, type, force and energy of force/nonbonded.rs:20-82:
-    4 P + 52 N), each bonded term's indices and parameters read once (bond 24
-    B, angle 28 B, dihedral 44 B, 1-4 pair 40 B: one 1-4 pair per dihedral of
-    the chain), and per atom the integrator phase's reads (position,
+    4 P + 52 N), the bonded part (8 B of indices per bond, 12 per angle, 16
+    per dihedral, 8 per 1-4 pair: one per dihedral of the chain; 24 B of force
+    traffic per atom), and per atom the integrator phase's reads (position,
     velocity, force, inverse mass, build reference, slot, charge word, system:
     120 B) and writes (position, velocity, drift reference, the packed
     coordinate record, the cleared force: 128 B)."""
     nb, na, nd = len(topo.bond_i), len(topo.angle_i), len(topo.dihed_i)
-    return 4 * pairs + 52 * n_atoms + 24 * nb + 28 * na + 44 * nd + 40 * nd + 248 * n_atoms
+    return 4 * pairs + 52 * n_atoms + 8 * nb + 12 * na + 16 * nd + 8 * nd + 24 * n_atoms + 248 * n_atoms
 
 
 def ns_per_day(steps, seconds):
