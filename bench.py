@@ -551,8 +551,22 @@ def run_ensemble(args):
     be = backend.CudaBackend.ensemble([s[0] for s in syss], [s[1] for s in syss], p)
     be.upload_state(pos, vel)
     be.forces_resident()
-    choice = be.autotune(reps=3)
+    if args.pair_shape:
+        # a known split instead of the autotuner (profiler runs)
+        sp, wb, gr = (int(x) for x in args.pair_shape.split(","))
+        be.pair_shape(sp, wb, gr)
+        choice = {"split": sp, "warps_per_block": wb, "grid": gr, "set": "--pair-shape"}
+    else:
+        choice = be.autotune(reps=3)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:0")
+    if args.quick:
+        # the batch's persistent steps only (profiler runs)
+        sec, reb, launches, _ = _time_batch(be, args, flush, backend.STEP_PERSISTENT)
+        be.close()
+        return {"metric": "aggregate ns/day of a 256-system batch (quick)", "value": round(n_sys * ns_per_day(
+                args.steps, sec), 2), "unit": "ns/day", "steps": args.steps, "quick": True,
+                "ms_per_step": round(1e3 * sec / args.steps, 4), "list_rebuilds_in_timed_region": reb,
+                "gpu_launches": launches, "autotuner": choice}
     # the whole batch as one persistent launch per step, then the same start
     # state as the kernel graph
     sec, reb, launches, clk = _time_batch(be, args, flush, backend.STEP_PERSISTENT)
