@@ -142,6 +142,7 @@ struct gm_ctx {
     int step_form = GM_STEP_PERSISTENT;
     int persist_blocks = 0;          // its grid: every block resident
     StepSync *d_sync = nullptr;
+    bool stall_barrier = false;      // gm_stall_next_barrier: the next persistent call's barrier cannot release
     long long rebuild_base = 0;
     unsigned last_shake_T = 0, last_rattle_T = 0;
 };
@@ -427,7 +428,9 @@ int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branc
     if (force_phase(c) && persistent_grid(c) == GM_OK) {
         // the persistent kernel's force phase: the pair items and the bonded
         // / 1-4 blocks from one queue, one launch, the same sums and energy
-        // partials as the kernels below
+        // partials as the kernels below; the queue words start cleared (a
+        // step launch that gave up at its barrier leaves them set)
+        cudaMemsetAsync(c->d_sync, 0, sizeof(StepSync), s);
         gm_launch_forces_persistent(fa, c->d_sync, c->persist_blocks, s);
         if (energy) gm_launch_energy(fa, s);
         c->energy_stale = !energy;
@@ -730,6 +733,12 @@ int begin_persistent(gm_ctx *c, bool fresh) {
     int rc = persistent_grid(c);
     if (rc) return rc;
     GM_CUDA(c, cudaMemsetAsync(c->d_sync, 0, sizeof(StepSync), c->stream));
+    if (c->stall_barrier) {
+        // the arrival count starts far past the grid: no block is the last to
+        // arrive, every block waits out the poll limit and reports the timeout
+        GM_CUDA(c, cudaMemsetAsync(&c->d_sync->arrive, 0x40, sizeof(unsigned int), c->stream));
+        c->stall_barrier = false;
+    }
     if (fresh) GM_CUDA(c, cudaMemsetAsync(&c->d_sync->fresh, 1, 1, c->stream));
     else GM_CUDA(c, cudaMemsetAsync(c->d_force, 0, sizeof(long long) * 3 * (size_t)c->n, c->stream));
     return GM_OK;
@@ -2060,6 +2069,9 @@ int32_t gm_steps(gm_ctx *c, double *px, double *py, double *pz, double *vx, doub
     if (!rc && energy) *energy = *c->h_energy;
     if (n_rebuilds) *n_rebuilds = (int64_t)(c->h_status->n_rebuilds - c->h_status->rebuild_base);
     const int rs = status_result(c, err);
+    // after a failed step the force sums may not be the forces at the
+    // resident positions: the next call evaluates them afresh
+    if (rs) c->forces_current = false;
     return rs ? rs : rc;
 }
 
@@ -2382,6 +2394,13 @@ int32_t gm_pair_shape(gm_ctx *c, int32_t split, int32_t warps_per_block, int32_t
     return GM_OK;
 }
 
+int32_t gm_stall_next_barrier(gm_ctx *c) {
+    if (!c) return GM_ERR_INVALID_ARGUMENT;
+    if (!persistent_form(c)) return fail(c, GM_ERR_UNSUPPORTED, "the context does not step in the persistent form");
+    c->stall_barrier = true;
+    return GM_OK;
+}
+
 int32_t gm_step_form(gm_ctx *c, int32_t form) {
     if (!c || (form != GM_STEP_GRAPH && form != GM_STEP_PERSISTENT)) return GM_ERR_INVALID_ARGUMENT;
     if (form == GM_STEP_PERSISTENT && (c->fp64 || c->n_clusters > 0))
@@ -2432,6 +2451,7 @@ int32_t gm_autotune(gm_ctx *c, int32_t reps, int64_t *choice) {
         // blocks from one queue) the split is the one that phase runs
         // fastest with
         double bestp = 1e300;
+        GM_CUDA(c, cudaMemsetAsync(c->d_sync, 0, sizeof(StepSync), c->stream));
         for (int sp : splits) {
             c->split = sp;
             ForceArgs fa = force_args(c);

@@ -167,6 +167,7 @@ def lib():
         L.gm_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int64)]
         L.gm_pair_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
         L.gm_step_form.argtypes = [C.c_void_p, C.c_int32]
+        L.gm_stall_next_barrier.argtypes = [C.c_void_p]
         L.gm_ws_record.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
         L.gm_ws_samples.argtypes = [C.c_void_p, C.c_int64, _f32p, _f32p, P(C.c_int64)]
         L.gm_ws_train.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_uint64, P(C.c_double)]
@@ -446,6 +447,11 @@ class CudaBackend:
             self._check(rc, GmConvergence.from_buffer_copy(conv))
         self._energy = e.value
         return e.value, nr.value, f
+
+    def stall_next_barrier(self):
+        """gm_stall_next_barrier: the next persistent call's grid barrier
+        waits out its poll limit and the call fails (error-path test)."""
+        self._check(lib().gm_stall_next_barrier(self._h))
 
     def _addrs(self, a):
         """Row addresses of a (3, N) float64 array, remembered for the arrays

@@ -279,6 +279,14 @@ int32_t gm_pair_shape(gm_ctx *ctx, int32_t split, int32_t warps_per_block, int32
  * phase alone: one launch over the same work queue, the same bits. */
 enum { GM_STEP_GRAPH = 0, GM_STEP_PERSISTENT = 1 };
 int32_t gm_step_form(gm_ctx *ctx, int32_t form);
+/* Error-path test of the persistent form's grid barrier: the next call that
+ * runs persistent steps starts with the barrier's arrival count far past the
+ * grid, so no block can release it.  Every block waits out the barrier's
+ * poll limit (a fraction of a second), records the timeout and returns; the
+ * call returns GM_ERR_DEVICE with nothing stepped, and the context is usable
+ * afterwards.  GM_ERR_UNSUPPORTED unless the context steps in the
+ * persistent form. */
+int32_t gm_stall_next_barrier(gm_ctx *ctx);
 
 /* ---- constraint warm start (no reference counterpart) ------------------
  *

@@ -16,12 +16,17 @@ word into an error code.
   compute_forces is infallible, hands back NaN forces, which the run loop's
   check_forces_finite turns into NumericalError::NanInForce
   (geodesic/src/lib.rs:79-92, geodesic-core/src/error.rs:34-38).
+* The persistent step's grid barrier is bounded: with its arrival count
+  preset past the grid from the host (gm_stall_next_barrier), no block can
+  release it, every block waits out the poll limit (a fraction of a second),
+  records the timeout and returns.  gm_steps reports GM_ERR_DEVICE with
+  nothing stepped, and the next call steps normally.
 """
 import numpy as np
 import pytest
 
 import oracle
-from geodesic_cuda import amber, backend
+from geodesic_cuda import amber, backend, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -97,4 +102,42 @@ def test_nonfinite_position_in_a_resident_call():
         be.steps(bad, vel, 0.002, 1)
     be.steps(pos, vel, 0.002, 2)
     assert np.all(np.isfinite(pos))
+    be.close()
+
+
+def test_persistent_barrier_timeout_is_reported_and_recovered():
+    atoms, topo, state, _ = synth.generate(2000, seed=12, temperature=300.0, relax_iters=100)
+    params = backend.SimParams(precision=backend.PRECISION_MIXED, **PARAMS)
+    be = backend.CudaBackend(atoms, topo, params)
+    pos = np.ascontiguousarray(state.pos.copy())
+    vel = np.ascontiguousarray(state.vel.copy())
+    be.steps(pos, vel, 0.002, 5)
+    p0, v0 = pos.copy(), vel.copy()
+    be.stall_next_barrier()
+    with pytest.raises(backend.BackendError) as e:
+        be.steps(pos, vel, 0.002, 3)
+    assert e.value.status == 4 and "barrier" in str(e.value), e.value  # GM_ERR_DEVICE
+    # nothing was stepped: the caller's state is the state it handed in
+    assert np.array_equal(pos, p0) and np.array_equal(vel, v0)
+    # the context carries on: three steps from there agree with a fresh
+    # context's three steps from the same state (lists built at different
+    # positions hold the same in-cutoff pairs; only summation order differs)
+    be.steps(pos, vel, 0.002, 3)
+    fresh = backend.CudaBackend(atoms, topo, params)
+    p1, v1 = p0.copy(), v0.copy()
+    fresh.steps(p1, v1, 0.002, 3)
+    assert np.all(np.isfinite(pos)) and np.allclose(pos, p1, rtol=0, atol=1e-8)
+    assert np.allclose(vel, v1, rtol=0, atol=1e-6)
+    fresh.close()
+    be.close()
+
+
+def test_barrier_stall_needs_the_persistent_form():
+    atoms = amber.AtomData(np.full(2, 3.0), np.full(2, 0.2), np.full(2, 12.0), np.zeros(2), np.full(2, 5, np.uint8),
+                           np.zeros(2, np.uint32), ["C   "] * 2)
+    be = backend.CudaBackend(atoms, amber.BondedTopology.empty(),
+                             backend.SimParams(precision=backend.PRECISION_FP64, **PARAMS))
+    with pytest.raises(backend.BackendError) as e:
+        be.stall_next_barrier()
+    assert e.value.status == 8  # GM_ERR_UNSUPPORTED
     be.close()
