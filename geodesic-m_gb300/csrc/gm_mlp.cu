@@ -193,46 +193,72 @@ __device__ void load_mlp(const float *__restrict__ P, const float *__restrict__ 
 }
 
 // y of the warp's 32 rows: sX[row][c] holds the BF16 input pair (2c, 2c + 1)
-// of the row (c < 6; 6 and 7 are zero); y goes to sy[row].
+// of the row (c < 6; 6 and 7 are zero); y goes to sy[row].  The two m16
+// tiles go through each layer together, so every step of the dependent
+// chain (layer-1 MMAs, SiLU, layer-2 MMAs, layer 3) has both tiles'
+// independent work in flight; each row's arithmetic is the same as one tile
+// at a time.
 __device__ __forceinline__ void mlp_rows32(const MlpSmem &S, const uint32_t (*sX)[8], float *sy) {
     const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+    uint32_t a[2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; mt++) {
         const int r0 = 16 * mt + g, r1 = r0 + 8;
-        const uint32_t a0 = sX[r0][t], a1 = sX[r1][t], a2 = sX[r0][t + 4], a3 = sX[r1][t + 4];
-        float z1[8][4];
+        a[mt][0] = sX[r0][t];
+        a[mt][1] = sX[r1][t];
+        a[mt][2] = sX[r0][t + 4];
+        a[mt][3] = sX[r1][t + 4];
+    }
+    float z1[2][8][4];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const float c0 = S.b1[8 * j + 2 * t], c1 = S.b1[8 * j + 2 * t + 1];
-            z1[j][0] = c0; z1[j][1] = c1; z1[j][2] = c0; z1[j][3] = c1;
-            mma_bf16(z1[j], a0, a1, a2, a3, S.b1f[j][l]);
+    for (int j = 0; j < 8; j++) {
+        const float c0 = S.b1[8 * j + 2 * t], c1 = S.b1[8 * j + 2 * t + 1];
+        const uint2 bw = S.b1f[j][l];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            z1[mt][j][0] = c0; z1[mt][j][1] = c1; z1[mt][j][2] = c0; z1[mt][j][3] = c1;
+            mma_bf16(z1[mt][j], a[mt][0], a[mt][1], a[mt][2], a[mt][3], bw);
         }
-        uint32_t A2[4][4];
+    }
+    uint32_t A2[2][4][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
 #pragma unroll
         for (int kk = 0; kk < 4; kk++) {
-            A2[kk][0] = pack_bf2(silu(z1[2 * kk][0]), silu(z1[2 * kk][1]));
-            A2[kk][1] = pack_bf2(silu(z1[2 * kk][2]), silu(z1[2 * kk][3]));
-            A2[kk][2] = pack_bf2(silu(z1[2 * kk + 1][0]), silu(z1[2 * kk + 1][1]));
-            A2[kk][3] = pack_bf2(silu(z1[2 * kk + 1][2]), silu(z1[2 * kk + 1][3]));
+            A2[mt][kk][0] = pack_bf2(silu(z1[mt][2 * kk][0]), silu(z1[mt][2 * kk][1]));
+            A2[mt][kk][1] = pack_bf2(silu(z1[mt][2 * kk][2]), silu(z1[mt][2 * kk][3]));
+            A2[mt][kk][2] = pack_bf2(silu(z1[mt][2 * kk + 1][0]), silu(z1[mt][2 * kk + 1][1]));
+            A2[mt][kk][3] = pack_bf2(silu(z1[mt][2 * kk + 1][2]), silu(z1[mt][2 * kk + 1][3]));
         }
-        float z2[8][4];
+    float z2[2][8][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const float c0 = S.b2[8 * j + 2 * t], c1 = S.b2[8 * j + 2 * t + 1];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            z2[mt][j][0] = c0; z2[mt][j][1] = c1; z2[mt][j][2] = c0; z2[mt][j][3] = c1;
+        }
+    }
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++)
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-            const float c0 = S.b2[8 * j + 2 * t], c1 = S.b2[8 * j + 2 * t + 1];
-            z2[j][0] = c0; z2[j][1] = c1; z2[j][2] = c0; z2[j][3] = c1;
+            const uint2 bw = S.b2f[kk][j][l];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+                mma_bf16(z2[mt][j], A2[mt][kk][0], A2[mt][kk][1], A2[mt][kk][2], A2[mt][kk][3], bw);
         }
 #pragma unroll
-        for (int kk = 0; kk < 4; kk++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) mma_bf16(z2[j], A2[kk][0], A2[kk][1], A2[kk][2], A2[kk][3], S.b2f[kk][j][l]);
+    for (int mt = 0; mt < 2; mt++) {
+        const int r0 = 16 * mt + g, r1 = r0 + 8;
         float y0 = 0.0f, y1 = 0.0f;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             const int c = 8 * j + 2 * t;
-            y0 = fmaf(bf(silu(z2[j][0])), S.w3[c], y0);
-            y0 = fmaf(bf(silu(z2[j][1])), S.w3[c + 1], y0);
-            y1 = fmaf(bf(silu(z2[j][2])), S.w3[c], y1);
-            y1 = fmaf(bf(silu(z2[j][3])), S.w3[c + 1], y1);
+            y0 = fmaf(bf(silu(z2[mt][j][0])), S.w3[c], y0);
+            y0 = fmaf(bf(silu(z2[mt][j][1])), S.w3[c + 1], y0);
+            y1 = fmaf(bf(silu(z2[mt][j][2])), S.w3[c], y1);
+            y1 = fmaf(bf(silu(z2[mt][j][3])), S.w3[c + 1], y1);
         }
         y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
         y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
