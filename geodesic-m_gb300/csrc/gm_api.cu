@@ -406,12 +406,6 @@ int seq_rebuild(gm_ctx *c, cudaStream_t s, bool all) {
     return (all ? 1 : 0) + 9 + (a.periodic || a.n > 0 ? 1 : 0);
 }
 
-// Force evaluation at the resident positions.  With a branch stream the
-// bonded and 1-4 kernels run on it beside the pair kernel: every force and
-// per-system energy sum is an integer sum and every energy partial has its own
-// slot, so the order in which the branches add changes no bit.  Without
-// `energy` the partials stay unsummed (energy_stale) until refresh_energy.
-// `packed`: the step kernel before it already packed the coordinates.
 bool persistent_form(const gm_ctx *c);
 int persistent_grid(gm_ctx *c);
 
@@ -420,6 +414,13 @@ int persistent_grid(gm_ctx *c);
 // too: the phase only evaluates forces.
 bool force_phase(const gm_ctx *c) { return c->step_form == GM_STEP_PERSISTENT && !c->fp64 && c->n > 0; }
 
+// Force evaluation at the resident positions: the persistent kernel's force
+// phase (force_phase), or the pair kernel with the bonded and 1-4 kernels.
+// With a branch stream those run on it beside the pair kernel: every force
+// and per-system energy sum is an integer sum and every energy partial has its
+// own slot, so the order in which the branches add changes no bit.  Without
+// `energy` the partials stay unsummed (energy_stale) until refresh_energy.
+// `packed`: the step kernel before it already packed the coordinates.
 int seq_forces(gm_ctx *c, cudaStream_t s, bool energy = true, cudaStream_t branch = nullptr, bool packed = false) {
     ListArgs la = list_args(c);
     if (c->n_sys > 1) cudaMemsetAsync(c->d_e_sys, 0, sizeof(long long) * (size_t)c->n_sys, s);

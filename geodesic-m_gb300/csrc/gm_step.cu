@@ -19,8 +19,9 @@
 //      rebuild condition.
 // The graph that holds the launch has one more node, the IF node of the list
 // rebuild.  After the last launch of a call the forces F(x_n) are evaluated
-// by the force kernels and the closing half-kick by the tail kernel, as in
-// the kernel-graph form.
+// by this kernel's force phase alone (the STEP = false instantiation, with
+// energies) and the closing half-kick by the tail kernel, so a call ends as
+// in the kernel-graph form.
 //
 // The launch performs the kernel-graph form's operations in the same order:
 // force sums are integer sums (the order of the work items changes no bit),
