@@ -14,6 +14,8 @@ for bit:
 * a batch of systems of uneven size: every member's state and the
   per-system energies;
 * gm_time_steps (every timed launch evaluates its forces);
+* the force phase alone (gm_compute_forces in the persistent form) against
+  the force kernels: the same forces, energy and per-system energies;
 and it is refused for FP64 and constrained contexts (GM_ERR_UNSUPPORTED).
 The potential energy gm_steps returns is the one at the positions it
 returns, call after call, in both forms (against the oracle, lib.rs:292-323
@@ -188,3 +190,30 @@ def test_refused_where_it_does_not_apply(case):
     assert e.value.status == 8  # GM_ERR_UNSUPPORTED
     be.step_form(backend.STEP_GRAPH)
     be.close()
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_force_phase_matches_force_kernels(batch):
+    if batch:
+        syss = [synth.generate(n, seed=s_, relax_iters=200) for n, s_ in ((800, 91), (2600, 92), (1400, 93))]
+        atoms, topo = [x[0] for x in syss], [x[1] for x in syss]
+        pos = np.ascontiguousarray(np.concatenate([x[2].pos for x in syss], axis=1))
+    else:
+        atoms, topo, state, _ = synth.generate(4000, seed=94, relax_iters=300)
+        pos = np.ascontiguousarray(state.pos)
+    p = backend.SimParams(precision=backend.PRECISION_MIXED, **OPEN)
+    out = []
+    for form in (backend.STEP_GRAPH, backend.STEP_PERSISTENT):
+        be = backend.CudaBackend.ensemble(atoms, topo, p) if batch else backend.CudaBackend(atoms, topo, p)
+        be.step_form(form)
+        q = pos.copy()
+        be.build_neighbor_list(q)
+        f = be.compute_forces(q).copy()
+        e = be.potential_energy()
+        sys_e = be.ensemble_energies()[0].copy() if batch else None
+        out.append((f, e, sys_e))
+        be.close()
+    assert np.array_equal(bits(out[0][0]), bits(out[1][0]))
+    assert out[0][1] == out[1][1]
+    if batch:
+        assert np.array_equal(bits(out[0][2]), bits(out[1][2]))
